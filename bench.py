@@ -1,0 +1,367 @@
+"""Benchmark of the batched C2C FP32 FFT engine (one JSON line on rank 0).
+
+Workload (the sweep configuration): N = 2^10 .. 2^24, batch = 2^27 / N
+(1 GiB of complex64 per direction), inputs i.i.d. uniform[-1, 1) from a seeded
+generator; one step = a forward and a backward transform at every N.
+Metric: compulsory HBM GB/s = 16 bytes per complex element and direction
+(one complex64 read + one write, out-of-place) / device time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's own algorithm for the path on the
+host cores instead (the FP32 restatement of FFT_OpenCL_Contiguous in
+oracle/ref_contiguous.c; neither the OpenCL original nor FFTW3 can run here).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FFT GB/s (% of HBM roofline) vs plain; batched-conv req/s, p99 at rel-L2≤1e-6"
+SWEEP_LOGN = list(range(10, 25))
+TOTAL = 1 << 27  # complex elements per direction
+KIND_NAMES = ("single", "col", "row", "copy")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
+    ap.add_argument("--elements-log", type=int, default=27,
+                    help="log2 complex elements per direction (27 = the 1 GiB sweep; smaller for ncu captures)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kind, logn):
+    """DRAM bytes per launch of a kernel from the committed ncu summary
+    (profiles/traffic.txt: '<kind> <log2 N> <bytes per launch> ...')."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = line.split()
+        if len(f) >= 3 and not line.startswith("#") and f[0] == kind and f[1] == str(logn):
+            return float(f[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline_sample(logns, threads, budget_s=20.0):
+    """The reference's contiguous Stockham algorithm (FP32 restatement) on the
+    host cores: every N of the sweep, forward + backward, on 2^22 complex per
+    size (one transform where N > 2^22).  Returns (GB/s, description)."""
+    import numpy as np
+
+    import oracle
+    rng = np.random.default_rng(2)
+    tot_bytes, tot_s = 0.0, 0.0
+    done = []
+    for logn in logns:
+        n = 1 << logn
+        batch = max(1, (1 << 22) // n)
+        x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
+        for sign in (-1, +1):
+            t0 = time.perf_counter()
+            oracle.ref_contiguous_fft(x, sign, nthreads=threads)
+            tot_s += time.perf_counter() - t0
+            tot_bytes += 16.0 * n * batch
+        done.append(logn)
+        if tot_s > budget_s:
+            break
+    desc = (f"FP32 restatement of FFT_OpenCL_Contiguous (radix-16 Stockham, runtime twiddles), {threads} threads; "
+            f"N=2^{done[0]}..2^{done[-1]}, max(2^22, N) complex per size, forward+backward")
+    return tot_bytes / tot_s / 1e9, desc
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    logns = [int(v) for v in args.logn.split(",")] if args.logn else SWEEP_LOGN
+    for _ in range(args.warmup):
+        cpu_baseline_sample(logns[:2], threads, budget_s=2.0)
+    vals = []
+    t0 = time.perf_counter()
+    desc = ""
+    for _ in range(args.steps):
+        v, desc = cpu_baseline_sample(logns, threads, budget_s=6.0)
+        vals.append(v)
+    elapsed = time.perf_counter() - t0
+    value = sum(vals) / len(vals)
+    peak, src = measured_peak()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C2C FP32 FFT sweep N=2^10..2^24, forward+backward (bounded host sample)",
+                   "sample": desc, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "FFTW3 (the reference's CPU backend) is not installed on this box; MKL backend does not compile",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    import estl_gb300 as estl
+
+    global TOTAL
+    TOTAL = 1 << args.elements_log
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    estl.init(local)
+    logns = [int(v) for v in args.logn.split(",")] if args.logn else SWEEP_LOGN
+    logns = [v for v in logns if v <= args.elements_log]
+
+    # inputs: 1 GiB of uniform[-1,1) complex64 (larger than the 126 MB L2)
+    g = torch.Generator(device="cuda").manual_seed(2 + rank)
+    xin = torch.view_as_complex((torch.rand((TOTAL, 2), device="cuda", generator=g) * 2 - 1).contiguous())
+    yfwd = torch.empty_like(xin)
+    zbwd = torch.empty_like(xin)
+    plans = {}
+    for logn in logns:
+        n = 1 << logn
+        plans[logn] = (estl.Plan(n, TOTAL // n, estl.FORWARD), estl.Plan(n, TOTAL // n, estl.BACKWARD))
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def step(events=None):
+        for logn in logns:
+            f, b = plans[logn]
+            if events is not None:
+                events[logn][0].record(stream)
+            f.execute_ptr(xin.data_ptr(), yfwd.data_ptr(), sh)
+            b.execute_ptr(yfwd.data_ptr(), zbwd.data_ptr(), sh)
+            if events is not None:
+                events[logn][1].record(stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region (device): K steps bracketed by barrier + synchronize
+    per_n = {logn: [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for logn in logns}
+    per_n_ms = {logn: 0.0 for logn in logns}
+    for p in plans.values():
+        p[0].set_profiling(True)
+        p[1].set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(per_n)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    total_ms = e0.elapsed_time(e1)
+    # per-N times of the last step (events re-recorded each step)
+    for logn in logns:
+        per_n_ms[logn] = per_n[logn][0].elapsed_time(per_n[logn][1])
+    stats = {}
+    for logn, (f, b) in plans.items():
+        for p in (f, b):
+            for kind, (cnt, ms, byts) in p.kernel_stats().items():
+                s = stats.setdefault((kind, logn), [0, 0.0, 0.0])
+                s[0] += cnt
+                s[1] += ms
+                s[2] += byts
+            p.set_profiling(False)
+    launches = sum(st[0] for st in stats.values())
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    bytes_per_step = sum(2 * 16.0 * TOTAL for _ in logns)
+    value = world * bytes_per_step * args.steps / (total_ms / 1e3) / 1e9
+    peak, peak_src = measured_peak()
+
+    # dominant kernel: largest share of the profiled device time
+    dom_key = max(stats, key=lambda k: stats[k][1])
+    cnt, ms, byts = stats[dom_key]
+    ach = (byts / cnt) / (ms / cnt / 1e3) / 1e9
+    traffic = ncu_traffic(dom_key[0], dom_key[1])
+    roofline = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": traffic,
+                "kernel": f"{dom_key[0]} tile, N=2^{dom_key[1]}", "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_src == "measured" else "fallback 6.8 TB/s",
+                "bytes_per_launch": byts / cnt, "avg_launch_us": round(1e3 * ms / cnt, 2),
+                "share_of_device_time": round(ms / sum(v[1] for v in stats.values()), 3)}
+    per_n_out = {}
+    for logn in logns:
+        n = 1 << logn
+        ms_n = per_n_ms[logn]
+        gbs = 2 * 16.0 * TOTAL / (ms_n / 1e3) / 1e9
+        gflops = 2 * 5.0 * n * logn * (TOTAL // n) / (ms_n / 1e3) / 1e9
+        passes = plans[logn][0].describe()["hbm_passes"]
+        per_n_out[f"2^{logn}"] = {"gbs": round(gbs, 1), "frac": round(gbs / peak, 3), "gflops": round(gflops, 1),
+                                  "hbm_passes": passes, "actual_traffic_gbs": round(gbs * passes, 1)}
+
+    # end to end through the C ABI with pinned host buffers (H2D + D2H inside)
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 3))
+    io_bytes = 2 * 8 * TOTAL * len(logns)  # per step: forward + backward, each copies TOTAL complex in and out
+    e2e = None
+    if e2e_steps > 0:
+        hin = torch.empty((TOTAL,), dtype=torch.complex64).pin_memory()
+        hin.copy_(xin.cpu())
+        hmid = torch.empty_like(hin).pin_memory()
+        hout = torch.empty_like(hin).pin_memory()
+        hin_np, hmid_np, hout_np = hin.numpy(), hmid.numpy(), hout.numpy()
+
+        def e2e_step():
+            for logn in logns:
+                f, b = plans[logn]
+                f.execute_host(hin_np, hmid_np)
+                b.execute_host(hmid_np, hout_np)
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        t1 = time.perf_counter()
+        barrier()
+        e2e_s = t1 - t0
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_s = float(tt.item())
+        e2e = {"value": round(world * bytes_per_step * e2e_steps / e2e_s / 1e9, 2), "unit": "GB/s",
+               "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
+               "path": "estl_execute_host (C ABI), pinned host buffers, chunked H2D/compute/D2H pipeline"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, desc = cpu_baseline_sample(logns, threads, budget_s=20.0)
+        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched C2C FP32 FFT sweep N=2^{logns[0]}..2^{logns[-1]}, "
+                                   f"batch=2^{args.elements_log}/N ({8 * TOTAL / 2**30:g} GiB complex64 per "
+                                   "direction), forward+backward per N, uniform[-1,1) seed 2",
+                       "l2": f"inputs larger than L2 ({8 * TOTAL / 2**20:g} MiB per direction)", "parallelism": f"replicas x{world}",
+                       "bytes_counted": "16 B per complex element per direction (compulsory read + write)"},
+            "roofline": roofline,
+            "frac_of_hbm_roofline": round(value / peak, 4),
+            "per_n": per_n_out,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

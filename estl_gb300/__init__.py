@@ -1,0 +1,157 @@
+"""estl_gb300 — GB300-native (sm_103a) FFT engine with ESTL's plugin semantics.
+
+The engine is the C-ABI library libestl_cuda.so (include/estl_cuda.h); this
+package is its Python binding.  PyTorch provides device memory and streams:
+
+    import torch, estl_gb300 as estl
+    estl.init()
+    x = torch.randn(256, 4096, dtype=torch.complex64, device="cuda")
+    y = estl.fft(x)                      # forward, unnormalised (FFTW_FORWARD)
+    z = estl.fft(y, inverse=True) / 4096  # round trip
+
+Plan objects mirror the reference's FFT<D> objects (FFT.h:19-36): a plan is
+created for (size, batchCount, forward) and executed repeatedly.
+"""
+import ctypes
+import json
+
+from ._lib import BACKWARD, FORWARD, PREC_FP32, EstlError, check, lib
+
+__all__ = ["init", "shutdown", "Plan", "fft", "autotune", "max_batch", "memory_usage", "EstlError",
+           "FORWARD", "BACKWARD"]
+
+_initialised = False
+
+
+def init(device=0, hbm_budget_bytes=0):
+    """Select the CUDA device and set the engine's HBM budget (0 = 90% of free)."""
+    global _initialised
+    check(lib().estl_init(int(device), int(hbm_budget_bytes)))
+    _initialised = True
+
+
+def shutdown():
+    global _initialised
+    _plan_cache.clear()
+    check(lib().estl_shutdown())
+    _initialised = False
+
+
+def _ensure_init():
+    if not _initialised:
+        init()
+
+
+def max_batch(n):
+    """FFT_OpenCL_Contiguous::getMaxBatchSize equivalent against the HBM budget."""
+    _ensure_init()
+    return int(lib().estl_max_batch(int(n)))
+
+
+def memory_usage():
+    used, budget = ctypes.c_size_t(), ctypes.c_size_t()
+    check(lib().estl_memory_usage(ctypes.byref(used), ctypes.byref(budget)))
+    return used.value, budget.value
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Plan:
+    """`batch` transforms of length n, forward (-1) or backward (+1)."""
+
+    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32):
+        _ensure_init()
+        self.n, self.batch, self.direction = int(n), int(batch), int(direction)
+        h = ctypes.c_void_p()
+        check(lib().estl_plan_create(self.n, self.batch, self.direction, int(precision), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(2048)
+        check(lib().estl_plan_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    @property
+    def launches(self):
+        return int(lib().estl_plan_launches(self._h))
+
+    def execute_ptr(self, d_in, d_out, stream=0):
+        """Device pointers (ints) of n*batch complex64 elements."""
+        check(lib().estl_execute(self._h, ctypes.c_void_p(d_in), ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+    def execute(self, x, out=None, stream=None):
+        """x: contiguous complex64 CUDA tensor with n*batch elements."""
+        import torch
+        if x.dtype != torch.complex64 or not x.is_cuda or not x.is_contiguous():
+            raise EstlError(1, "input must be a contiguous complex64 CUDA tensor")
+        if x.numel() != self.n * self.batch:
+            raise EstlError(1, f"input has {x.numel()} elements, plan expects {self.n * self.batch}")
+        if out is None:
+            out = torch.empty_like(x)
+        self.execute_ptr(x.data_ptr(), out.data_ptr(), _stream_handle(stream))
+        return out
+
+    def execute_host(self, x, out):
+        """Host numpy complex64 arrays (pinned memory recommended)."""
+        check(lib().estl_execute_host(self._h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(out.ctypes.data)))
+        return out
+
+    KERNEL_KINDS = ("single", "col", "row", "copy")
+
+    def set_profiling(self, enable=True):
+        """Bracket every launch with CUDA events (per-kernel timers)."""
+        check(lib().estl_plan_set_profiling(self._h, 1 if enable else 0))
+
+    def kernel_stats(self):
+        """{kind: (launches, total_ms, algorithmic_bytes)} of profiled launches."""
+        L = (ctypes.c_int64 * 4)()
+        T = (ctypes.c_double * 4)()
+        B = (ctypes.c_double * 4)()
+        check(lib().estl_plan_kernel_stats(self._h, L, T, B))
+        return {k: (int(L[i]), float(T[i]), float(B[i])) for i, k in enumerate(self.KERNEL_KINDS) if L[i]}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().estl_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_plan_cache = {}
+
+
+def fft(x, inverse=False, out=None, stream=None):
+    """Batched FFT over the last dimension of a complex64 CUDA tensor."""
+    n = x.shape[-1]
+    batch = x.numel() // n
+    key = (n, batch, BACKWARD if inverse else FORWARD)
+    p = _plan_cache.get(key)
+    if p is None:
+        p = _plan_cache[key] = Plan(n, batch, key[2])
+    return p.execute(x.contiguous(), out=out, stream=stream)
+
+
+def autotune(n, batch, iters=5):
+    """Time every candidate plan for (n, batch); cache and return the best."""
+    _ensure_init()
+    buf = ctypes.create_string_buffer(4096)
+    check(lib().estl_autotune(int(n), int(batch), int(iters), buf, len(buf)))
+    for key in [k for k in _plan_cache if k[0] == n and k[1] == batch]:
+        _plan_cache.pop(key).close()
+    return json.loads(buf.value.decode())

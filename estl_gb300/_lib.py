@@ -1,0 +1,88 @@
+"""ctypes binding of libestl_cuda.so (include/estl_cuda.h).
+
+The shared library is the product: it is loaded from the package directory
+and a missing library is an error, never a reason to fall back to another
+implementation.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libestl_cuda.so")
+
+STATUS = {
+    0: "ESTL_OK",
+    1: "ESTL_INVALID_ARG",
+    2: "ESTL_UNSUPPORTED_SIZE",
+    3: "ESTL_OUT_OF_MEMORY",
+    4: "ESTL_ADMISSION_REJECTED",
+    5: "ESTL_DEVICE_ERROR",
+    6: "ESTL_TIMEOUT",
+    7: "ESTL_NOT_INITIALIZED",
+}
+
+FORWARD = -1
+BACKWARD = +1
+PREC_FP32 = 0
+
+
+class EstlError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_SZ = ctypes.c_size_t
+_INT = ctypes.c_int
+
+# name -> (restype, argtypes); the C declarations are in include/estl_cuda.h
+SIGNATURES = {
+    "estl_init": (_INT, [_INT, _SZ]),
+    "estl_shutdown": (_INT, []),
+    "estl_last_error": (ctypes.c_char_p, []),
+    "estl_status_string": (ctypes.c_char_p, [_INT]),
+    "estl_max_batch": (_I64, [_I64]),
+    "estl_plan_create": (_INT, [_I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
+    "estl_plan_destroy": (_INT, [_P]),
+    "estl_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
+    "estl_plan_launches": (_I64, [_P]),
+    "estl_execute": (_INT, [_P, _P, _P, _P]),
+    "estl_execute_host": (_INT, [_P, _P, _P]),
+    "estl_plan_set_profiling": (_INT, [_P, _INT]),
+    "estl_plan_kernel_stats": (_INT, [_P, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "estl_host_register": (_INT, [_P, _SZ]),
+    "estl_host_unregister": (_INT, [_P]),
+    "estl_autotune": (_INT, [_I64, _I64, _INT, ctypes.c_char_p, _SZ]),
+    "estl_memory_usage": (_INT, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
+}
+
+
+def lib():
+    """Load libestl_cuda.so (built by estl_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+                "(the FFT engine has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    """Raise EstlError for a non-zero estl_status."""
+    if status != 0:
+        msg = lib().estl_last_error()
+        raise EstlError(status, msg.decode() if msg else "")
+    return status

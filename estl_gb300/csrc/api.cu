@@ -1,0 +1,601 @@
+// api.cu — the C ABI of include/estl_cuda.h: initialisation, plans, device
+// and host execution.
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "engine.h"
+#include "kernels.cuh"
+#include "tuner.h"
+
+namespace estl {
+
+// --------------------------------------------------------------------------
+// errors
+// --------------------------------------------------------------------------
+static thread_local std::string t_last_error;
+
+estl_status fail(estl_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+  return s;
+}
+
+estl_status ok() { return ESTL_OK; }
+
+estl_status check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ESTL_OK;
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return fail(ESTL_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  }
+  return fail(ESTL_DEVICE_ERROR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+Engine& engine() {
+  static Engine e;
+  return e;
+}
+
+estl_status require_init() {
+  Engine& E = engine();
+  if (!E.inited) return fail(ESTL_NOT_INITIALIZED, "estl_init has not been called");
+  return check_cuda(cudaSetDevice(E.device), "cudaSetDevice");
+}
+
+estl_status dev_alloc(void** p, size_t bytes, const char* what) {
+  Engine& E = engine();
+  *p = nullptr;
+  if (bytes == 0) return ESTL_OK;
+  size_t prev = E.used.fetch_add(bytes);
+  if (prev + bytes > E.budget) {
+    E.used.fetch_sub(bytes);
+    return fail(ESTL_OUT_OF_MEMORY, "%s: %zu bytes exceed the HBM budget (%zu of %zu bytes in use)", what, bytes,
+                prev, E.budget);
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    E.used.fetch_sub(bytes);
+    *p = nullptr;
+    return check_cuda(e, what);
+  }
+  return ESTL_OK;
+}
+
+void dev_free(void* p, size_t bytes) {
+  if (!p) return;
+  cudaFree(p);
+  engine().used.fetch_sub(bytes);
+}
+
+// --------------------------------------------------------------------------
+// twiddle bank
+// --------------------------------------------------------------------------
+// bank[2^k + j] = w_{2^k}^j (k <= kBankLog), then 4096-entry low tables of
+// w_N^j for N = 2^(kBankLog+1) .. 2^kMaxLog.  FP64 sincospi, rounded to FP32.
+__global__ void bank_init_kernel(cf32* bank) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= kBankSize) return;
+  double x;
+  if (idx < kBankDirect) {
+    if (idx < 2) {
+      bank[idx] = cf32{1.f, 0.f};
+      return;
+    }
+    int k = 63 - __clzll(idx);
+    long long j = idx - (1LL << k);
+    x = -(double)j / (double)(1LL << (k - 1));
+  } else {
+    long long r = idx - kBankDirect;
+    int n = kBankLog + 1 + (int)(r >> kLoLog);
+    long long j = r & ((1LL << kLoLog) - 1);
+    x = -(double)j / (double)(1LL << (n - 1));
+  }
+  double s, c;
+  sincospi(x, &s, &c);
+  bank[idx] = cf32{(float)c, (float)s};
+}
+
+// --------------------------------------------------------------------------
+// kernel lookup
+// --------------------------------------------------------------------------
+struct KernelTable {
+  std::vector<KernelDesc> descs;
+  std::vector<char> attr_set;
+};
+
+static KernelTable& ktable() {
+  static KernelTable t = [] {
+    KernelTable k;
+    const KernelDesc* d;
+    int n = registry_single(&d);
+    k.descs.insert(k.descs.end(), d, d + n);
+    n = registry_col(&d);
+    k.descs.insert(k.descs.end(), d, d + n);
+    n = registry_row(&d);
+    k.descs.insert(k.descs.end(), d, d + n);
+    k.attr_set.assign(k.descs.size(), 0);
+    return k;
+  }();
+  return t;
+}
+
+static std::mutex g_attr_mu;
+
+static estl_status lookup_kernel(const Step& st, const KernelDesc** out) {
+  KernelTable& kt = ktable();
+  for (size_t i = 0; i < kt.descs.size(); ++i) {
+    const KernelDesc& d = kt.descs[i];
+    if (d.kind == st.kind && d.logm == st.logm && d.loge == st.loge && d.logr == st.logr && d.logc == st.logc) {
+      if (!kt.attr_set[i]) {
+        std::lock_guard<std::mutex> g(g_attr_mu);
+        if (!kt.attr_set[i]) {
+          estl_status s = check_cuda(
+              cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem_bytes),
+              "cudaFuncSetAttribute(max dynamic shared memory)");
+          if (s != ESTL_OK) return s;
+          kt.attr_set[i] = 1;
+        }
+      }
+      *out = &d;
+      return ESTL_OK;
+    }
+  }
+  return fail(ESTL_UNSUPPORTED_SIZE, "no kernel instantiated for step kind %d logm %d loge %d logc %d", st.kind,
+              st.logm, st.loge, st.logc);
+}
+
+estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
+                         cudaStream_t stream) {
+  Engine& E = engine();
+  for (const Step& st : plan.steps) {
+    const cf32* src = st.src == BUF_IN ? in : (st.src == BUF_SCRATCH ? scratch : out);
+    cf32* dst = st.dst == BUF_OUT ? out : scratch;
+    if (st.kind == STEP_COPY) {
+      estl_status s = check_cuda(cudaMemcpyAsync(dst + st.dst_off, src + st.src_off, st.rows * sizeof(cf32),
+                                                 cudaMemcpyDeviceToDevice, stream),
+                                 "cudaMemcpyAsync(copy step)");
+      if (s != ESTL_OK) return s;
+      continue;
+    }
+    const KernelDesc* d = nullptr;
+    estl_status s = lookup_kernel(st, &d);
+    if (s != ESTL_OK) return s;
+    if (st.grid < 1 || st.grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "grid of %lld CTAs", st.grid);
+    TileArgs a;
+    a.in = Ptr<const cf32>{src + st.src_off, st.src_len};
+    a.out = Ptr<cf32>{dst + st.dst_off, st.dst_len};
+    a.bank = Ptr<const cf32>{E.bank, kBankSize};
+    a.rows = st.rows;
+    a.logn = st.logn;
+    a.logn1 = 0;
+    a.sgn = sgn;
+    void* args[] = {&a};
+    s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)st.grid), dim3(d->nthreads), args, d->smem_bytes, stream),
+                   "cudaLaunchKernel");
+    if (s != ESTL_OK) return s;
+  }
+  return ESTL_OK;
+}
+
+}  // namespace estl
+
+using namespace estl;
+
+// --------------------------------------------------------------------------
+// plans
+// --------------------------------------------------------------------------
+struct estl_plan_s {
+  Plan1D layout;
+  float sgn = 1.f;
+  int direction = ESTL_FORWARD;
+  cf32* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  std::mutex mu;
+  cudaEvent_t done = nullptr;  // last execute of this plan (scratch reuse order)
+  bool done_recorded = false;
+  // host pipeline (lazily created by estl_execute_host)
+  bool host_ready = false;
+  long long host_chunk = 0;
+  Plan1D host_plan_full, host_plan_tail;
+  cf32* din[2] = {nullptr, nullptr};
+  cf32* dout[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+  cudaStream_t st[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_h2d[2] = {}, ev_comp[2] = {}, ev_d2h[2] = {};
+  // per-launch profiling (estl_plan_set_profiling)
+  bool profiling = false;
+  struct Rec {
+    int kind;
+    double bytes;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> event_pool;
+  long long prof_launches[4] = {0, 0, 0, 0};
+  double prof_ms[4] = {0, 0, 0, 0}, prof_bytes[4] = {0, 0, 0, 0};
+};
+
+static std::mutex g_plans_mu;
+static std::unordered_set<estl_plan> g_plans;
+
+static void plan_release(estl_plan p) {
+  if (!p) return;
+  dev_free(p->scratch, p->scratch_bytes);
+  for (int s = 0; s < 2; ++s) {
+    dev_free(p->din[s], p->stage_bytes);
+    dev_free(p->dout[s], p->stage_bytes);
+    if (p->ev_h2d[s]) cudaEventDestroy(p->ev_h2d[s]);
+    if (p->ev_comp[s]) cudaEventDestroy(p->ev_comp[s]);
+    if (p->ev_d2h[s]) cudaEventDestroy(p->ev_d2h[s]);
+  }
+  for (int s = 0; s < 3; ++s)
+    if (p->st[s]) cudaStreamDestroy(p->st[s]);
+  if (p->done) cudaEventDestroy(p->done);
+  for (auto& r : p->pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : p->event_pool) cudaEventDestroy(e);
+  delete p;
+}
+
+extern "C" {
+
+estl_status estl_init(int device, size_t hbm_budget_bytes) {
+  Engine& E = engine();
+  std::lock_guard<std::mutex> g(E.mu);
+  if (E.inited) {
+    if (device != E.device) return fail(ESTL_INVALID_ARG, "already initialised on device %d", E.device);
+    if (hbm_budget_bytes) E.budget = hbm_budget_bytes;
+    return ESTL_OK;
+  }
+  int count = 0;
+  estl_status s = check_cuda(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+  if (s != ESTL_OK) return s;
+  if (device < 0 || device >= count) return fail(ESTL_INVALID_ARG, "device %d not present (%d devices)", device, count);
+  s = check_cuda(cudaSetDevice(device), "cudaSetDevice");
+  if (s != ESTL_OK) return s;
+  size_t free_b = 0, total_b = 0;
+  s = check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  if (s != ESTL_OK) return s;
+  cudaDeviceProp prop;
+  s = check_cuda(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+  if (s != ESTL_OK) return s;
+  if (prop.major < 10) return fail(ESTL_DEVICE_ERROR, "device %d is sm_%d%d; this build targets sm_103a", device, prop.major, prop.minor);
+  E.device = device;
+  E.num_sms = prop.multiProcessorCount;
+  E.budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)(0.9 * (double)free_b);
+  E.used = 0;
+  void* b = nullptr;
+  E.inited = true;  // dev_alloc needs the budget
+  s = dev_alloc(&b, kBankSize * sizeof(cf32), "twiddle bank");
+  if (s != ESTL_OK) {
+    E.inited = false;
+    return s;
+  }
+  E.bank = (cf32*)b;
+  bank_init_kernel<<<(unsigned)((kBankSize + 255) / 256), 256>>>(E.bank);
+  s = check_cuda(cudaGetLastError(), "bank_init_kernel launch");
+  if (s == ESTL_OK) s = check_cuda(cudaDeviceSynchronize(), "bank_init_kernel");
+  if (s != ESTL_OK) {
+    dev_free(E.bank, kBankSize * sizeof(cf32));
+    E.bank = nullptr;
+    E.inited = false;
+    return s;
+  }
+  tuner_load_cache();
+  return ESTL_OK;
+}
+
+estl_status estl_shutdown(void) {
+  Engine& E = engine();
+  {
+    std::lock_guard<std::mutex> g(g_plans_mu);
+    for (estl_plan p : g_plans) plan_release(p);
+    g_plans.clear();
+  }
+  std::lock_guard<std::mutex> g(E.mu);
+  if (!E.inited) return ESTL_OK;
+  cudaDeviceSynchronize();
+  dev_free(E.bank, kBankSize * sizeof(cf32));
+  E.bank = nullptr;
+  E.inited = false;
+  return ESTL_OK;
+}
+
+const char* estl_last_error(void) { return t_last_error.c_str(); }
+
+const char* estl_status_string(estl_status s) {
+  switch (s) {
+    case ESTL_OK: return "ESTL_OK";
+    case ESTL_INVALID_ARG: return "ESTL_INVALID_ARG";
+    case ESTL_UNSUPPORTED_SIZE: return "ESTL_UNSUPPORTED_SIZE";
+    case ESTL_OUT_OF_MEMORY: return "ESTL_OUT_OF_MEMORY";
+    case ESTL_ADMISSION_REJECTED: return "ESTL_ADMISSION_REJECTED";
+    case ESTL_DEVICE_ERROR: return "ESTL_DEVICE_ERROR";
+    case ESTL_TIMEOUT: return "ESTL_TIMEOUT";
+    case ESTL_NOT_INITIALIZED: return "ESTL_NOT_INITIALIZED";
+  }
+  return "ESTL_UNKNOWN";
+}
+
+int64_t estl_max_batch(int64_t n) {
+  Engine& E = engine();
+  if (!E.inited || ilog2_exact(n) < 0 || ilog2_exact(n) > kMaxLogN) return 0;
+  size_t used = E.used.load();
+  if (used >= E.budget) return 0;
+  long long b = (long long)((E.budget - used) / (3 * sizeof(cf32) * (size_t)n));
+  return b > INT32_MAX ? INT32_MAX : b;
+}
+
+estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precision, estl_plan* plan) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "plan output pointer is NULL");
+  *plan = nullptr;
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  if (direction != ESTL_FORWARD && direction != ESTL_BACKWARD)
+    return fail(ESTL_INVALID_ARG, "direction must be ESTL_FORWARD (-1) or ESTL_BACKWARD (+1), got %d", direction);
+  if (precision != ESTL_PREC_FP32) return fail(ESTL_INVALID_ARG, "unknown precision %d", precision);
+  if (batch < 1) return fail(ESTL_INVALID_ARG, "batch must be >= 1 (got %lld)", (long long)batch);
+  int logn = ilog2_exact(n);
+  if (logn < 0 || logn > kMaxLogN)
+    return fail(ESTL_UNSUPPORTED_SIZE, "transform length %lld is not a power of two in [1, 2^%d]", (long long)n,
+                kMaxLogN);
+  PlanChoice choice;
+  tuner_lookup(n, batch, &choice);
+  std::unique_ptr<estl_plan_s> p(new estl_plan_s);
+  std::string err;
+  if (!make_plan(n, batch, choice, &p->layout, &err)) {
+    // a stale tuning entry must not make a valid size fail: fall back to defaults
+    if (!make_plan(n, batch, PlanChoice{}, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  }
+  p->direction = direction;
+  p->sgn = direction == ESTL_FORWARD ? 1.f : -1.f;
+  p->scratch_bytes = (size_t)p->layout.scratch_elems * sizeof(cf32);
+  s = dev_alloc((void**)&p->scratch, p->scratch_bytes, "plan scratch");
+  if (s != ESTL_OK) return s;
+  s = check_cuda(cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming), "cudaEventCreate");
+  if (s != ESTL_OK) {
+    plan_release(p.release());
+    return s;
+  }
+  estl_plan out = p.release();
+  {
+    std::lock_guard<std::mutex> g(g_plans_mu);
+    g_plans.insert(out);
+  }
+  *plan = out;
+  return ESTL_OK;
+}
+
+estl_status estl_plan_destroy(estl_plan plan) {
+  if (!plan) return ESTL_OK;
+  {
+    std::lock_guard<std::mutex> g(g_plans_mu);
+    if (!g_plans.erase(plan)) return fail(ESTL_INVALID_ARG, "unknown plan handle");
+  }
+  if (plan->done_recorded) cudaEventSynchronize(plan->done);
+  plan_release(plan);
+  return ESTL_OK;
+}
+
+estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len) {
+  if (!plan || !buf || len == 0) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
+  std::string d = plan->layout.describe();
+  std::snprintf(buf, len, "%s", d.c_str());
+  return ESTL_OK;
+}
+
+int64_t estl_plan_launches(estl_plan plan) { return plan ? (int64_t)plan->layout.steps.size() : 0; }
+
+static estl_status check_buffers(const void* in, const void* out) {
+  if (!in || !out) return fail(ESTL_INVALID_ARG, "NULL data pointer");
+  if (((uintptr_t)in & 7) || ((uintptr_t)out & 7)) return fail(ESTL_INVALID_ARG, "data pointers must be 8-byte aligned");
+  if (in == out) return fail(ESTL_INVALID_ARG, "in-place execution is not supported (d_in == d_out)");
+  return ESTL_OK;
+}
+
+static estl_status pool_event(estl_plan p, cudaEvent_t* e) {
+  if (!p->event_pool.empty()) {
+    *e = p->event_pool.back();
+    p->event_pool.pop_back();
+    return ESTL_OK;
+  }
+  return check_cuda(cudaEventCreate(e), "cudaEventCreate");
+}
+
+// Resolves recorded launch events into the per-kind accumulators (blocks
+// until the last recorded launch has finished).
+static estl_status resolve_profile(estl_plan p) {
+  if (p->pending.empty()) return ESTL_OK;
+  estl_status s = check_cuda(cudaEventSynchronize(p->pending.back().b), "cudaEventSynchronize");
+  if (s != ESTL_OK) return s;
+  for (auto& r : p->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    p->prof_launches[r.kind] += 1;
+    p->prof_ms[r.kind] += ms;
+    p->prof_bytes[r.kind] += r.bytes;
+    p->event_pool.push_back(r.a);
+    p->event_pool.push_back(r.b);
+  }
+  p->pending.clear();
+  return ESTL_OK;
+}
+
+static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const cf32* in, cf32* out, cudaStream_t stream) {
+  if (p->pending.size() > 65536) {
+    estl_status s = resolve_profile(p);
+    if (s != ESTL_OK) return s;
+  }
+  for (const Step& st : layout.steps) {
+    Plan1D one = layout;
+    one.steps.assign(1, st);
+    estl_plan_s::Rec r{st.kind, 16.0 * (double)st.src_len, nullptr, nullptr};
+    estl_status s = pool_event(p, &r.a);
+    if (s == ESTL_OK) s = pool_event(p, &r.b);
+    if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.a, stream), "cudaEventRecord");
+    if (s == ESTL_OK) s = launch_steps(one, in, out, p->scratch, p->sgn, stream);
+    if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.b, stream), "cudaEventRecord");
+    if (s != ESTL_OK) return s;
+    p->pending.push_back(r);
+  }
+  return ESTL_OK;
+}
+
+static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const cf32* in, cf32* out, cudaStream_t stream) {
+  std::lock_guard<std::mutex> g(plan->mu);
+  estl_status s;
+  if (plan->done_recorded) {
+    s = check_cuda(cudaStreamWaitEvent(stream, plan->done, 0), "cudaStreamWaitEvent");
+    if (s != ESTL_OK) return s;
+  }
+  if (plan->profiling)
+    s = launch_profiled(plan, layout, in, out, stream);
+  else
+    s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream);
+  if (s != ESTL_OK) return s;
+  s = check_cuda(cudaEventRecord(plan->done, stream), "cudaEventRecord");
+  if (s != ESTL_OK) return s;
+  plan->done_recorded = true;
+  return ESTL_OK;
+}
+
+estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* stream) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  s = check_buffers(d_in, d_out);
+  if (s != ESTL_OK) return s;
+  return run_plan_on(plan, plan->layout, (const cf32*)d_in, (cf32*)d_out, (cudaStream_t)stream);
+}
+
+static estl_status host_pipeline_setup(estl_plan p) {
+  if (p->host_ready) return ESTL_OK;
+  const long long n = p->layout.n, batch = p->layout.batch;
+  // ~64 MiB chunks: large enough to reach copy-engine bandwidth, small
+  // enough that the copy in, the transform and the copy out overlap.
+  long long chunk = std::max(1LL, (64LL << 20) / (8 * n));
+  chunk = std::min(chunk, batch);
+  std::string err;
+  if (!make_plan(n, chunk, p->layout.choice, &p->host_plan_full, &err))
+    return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  long long tail = batch % chunk;
+  if (tail && !make_plan(n, tail, p->layout.choice, &p->host_plan_tail, &err))
+    return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  if ((size_t)p->host_plan_full.scratch_elems * sizeof(cf32) > p->scratch_bytes)
+    return fail(ESTL_DEVICE_ERROR, "chunk plan needs more scratch than the plan holds");
+  p->stage_bytes = (size_t)(chunk * n) * sizeof(cf32);
+  estl_status s;
+  for (int i = 0; i < 2; ++i) {
+    s = dev_alloc((void**)&p->din[i], p->stage_bytes, "host pipeline staging");
+    if (s != ESTL_OK) return s;
+    s = dev_alloc((void**)&p->dout[i], p->stage_bytes, "host pipeline staging");
+    if (s != ESTL_OK) return s;
+    if ((s = check_cuda(cudaEventCreateWithFlags(&p->ev_h2d[i], cudaEventDisableTiming), "cudaEventCreate")) != ESTL_OK ||
+        (s = check_cuda(cudaEventCreateWithFlags(&p->ev_comp[i], cudaEventDisableTiming), "cudaEventCreate")) != ESTL_OK ||
+        (s = check_cuda(cudaEventCreateWithFlags(&p->ev_d2h[i], cudaEventDisableTiming), "cudaEventCreate")) != ESTL_OK)
+      return s;
+  }
+  for (int i = 0; i < 3; ++i) {
+    s = check_cuda(cudaStreamCreateWithFlags(&p->st[i], cudaStreamNonBlocking), "cudaStreamCreate");
+    if (s != ESTL_OK) return s;
+  }
+  p->host_chunk = chunk;
+  p->host_ready = true;
+  return ESTL_OK;
+}
+
+estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  s = check_buffers(h_in, h_out);
+  if (s != ESTL_OK) return s;
+  s = host_pipeline_setup(plan);
+  if (s != ESTL_OK) return s;
+  const long long n = plan->layout.n, batch = plan->layout.batch, chunk = plan->host_chunk;
+  const long long nchunks = (batch + chunk - 1) / chunk;
+  cudaStream_t sh = plan->st[0], sc = plan->st[1], sd = plan->st[2];
+  for (long long i = 0; i < nchunks; ++i) {
+    const int k = (int)(i & 1);
+    const long long b0 = i * chunk, cnt = std::min(chunk, batch - b0);
+    const size_t bytes = (size_t)(cnt * n) * sizeof(cf32);
+    const Plan1D& lay = cnt == chunk ? plan->host_plan_full : plan->host_plan_tail;
+    if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sh, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaMemcpyAsync(plan->din[k], h_in + 2 * b0 * n, bytes, cudaMemcpyHostToDevice, sh),
+                        "cudaMemcpyAsync(H2D)")) != ESTL_OK)
+      return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_h2d[k], sh), "record")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_h2d[k], 0), "wait")) != ESTL_OK) return s;
+    if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_d2h[k], 0), "wait")) != ESTL_OK) return s;
+    if ((s = run_plan_on(plan, lay, plan->din[k], plan->dout[k], sc)) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_comp[k], sc), "record")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaStreamWaitEvent(sd, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaMemcpyAsync(h_out + 2 * b0 * n, plan->dout[k], bytes, cudaMemcpyDeviceToHost, sd),
+                        "cudaMemcpyAsync(D2H)")) != ESTL_OK)
+      return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_d2h[k], sd), "record")) != ESTL_OK) return s;
+  }
+  return check_cuda(cudaStreamSynchronize(sd), "cudaStreamSynchronize");
+}
+
+estl_status estl_plan_set_profiling(estl_plan plan, int enable) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> g(plan->mu);
+  estl_status s = resolve_profile(plan);
+  if (s != ESTL_OK) return s;
+  plan->profiling = enable != 0;
+  for (int k = 0; k < 4; ++k) {
+    plan->prof_launches[k] = 0;
+    plan->prof_ms[k] = 0;
+    plan->prof_bytes[k] = 0;
+  }
+  return ESTL_OK;
+}
+
+estl_status estl_plan_kernel_stats(estl_plan plan, int64_t* launches, double* total_ms, double* bytes) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> g(plan->mu);
+  estl_status s = resolve_profile(plan);
+  if (s != ESTL_OK) return s;
+  for (int k = 0; k < 4; ++k) {
+    if (launches) launches[k] = plan->prof_launches[k];
+    if (total_ms) total_ms[k] = plan->prof_ms[k];
+    if (bytes) bytes[k] = plan->prof_bytes[k];
+  }
+  return ESTL_OK;
+}
+
+estl_status estl_host_register(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return fail(ESTL_INVALID_ARG, "NULL pointer or zero size");
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  return check_cuda(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault), "cudaHostRegister");
+}
+
+estl_status estl_host_unregister(void* ptr) {
+  if (!ptr) return fail(ESTL_INVALID_ARG, "NULL pointer");
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  return check_cuda(cudaHostUnregister(ptr), "cudaHostUnregister");
+}
+
+estl_status estl_memory_usage(size_t* used_bytes, size_t* budget_bytes) {
+  Engine& E = engine();
+  if (used_bytes) *used_bytes = E.used.load();
+  if (budget_bytes) *budget_bytes = E.budget;
+  return ESTL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+// engine.h — internal state shared by the C-ABI translation units:
+// device selection, the HBM budget accounting allocator, the twiddle bank,
+// kernel lookup and the plan executor.
+//
+// Replaces the reference's OpenCL runtime wrapper (uOpenCL.h:275-348:
+// context, queue, buffers, profiling) with the CUDA runtime: streams and
+// events instead of a profiling queue, a budgeted device allocator instead of
+// per-object clCreateBuffer.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <mutex>
+#include <string>
+
+#include "../../include/estl_cuda.h"
+#include "fft_core.cuh"
+#include "planner.h"
+
+namespace estl {
+
+struct Engine {
+  std::mutex mu;
+  bool inited = false;
+  int device = -1;
+  size_t budget = 0;
+  std::atomic<size_t> used{0};
+  cf32* bank = nullptr;  // twiddle bank, kBankSize entries
+  int num_sms = 0;
+};
+
+Engine& engine();
+
+// Sets the calling thread's last-error message and returns `s`.
+estl_status fail(estl_status s, const char* fmt, ...);
+estl_status ok();
+estl_status check_cuda(cudaError_t e, const char* what);
+estl_status require_init();
+
+// Budgeted device allocation (counted against Engine::budget).
+estl_status dev_alloc(void** p, size_t bytes, const char* what);
+void dev_free(void* p, size_t bytes);
+
+// Launches one plan's steps on `stream`.  in/out/scratch are device
+// pointers of interleaved complex64; sgn = +1 forward, -1 backward.
+estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
+                         cudaStream_t stream);
+
+}  // namespace estl

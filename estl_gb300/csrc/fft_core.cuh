@@ -1,0 +1,497 @@
+// fft_core.cuh — FFT tile machinery shared by the sm_103a kernels and the
+// host-side index emulator.
+//
+// The reference computes one Stockham pass per OpenCL kernel
+// (FFT_OpenCL_Contiguous.h:144-184): one work-item loads B_q points, applies
+// the pass twiddle, runs an unrolled radix-2 B_q-point DFT in registers
+// (OpenCLFFTAlgorithm.h:14-43) and stores them, with a full global-memory
+// round trip per pass.  Here a CTA keeps a whole tile of transforms on chip
+// and runs every pass of the tile in one launch:
+//
+//   global --(coalesced ld)--> registers --radix-R butterfly--> shared
+//          --> registers --butterfly--> ... --> registers --(coalesced st)--> global
+//
+// Stockham pass p (radix R, Ns = product of earlier radices), butterfly b:
+//   inputs   b + r*(M/R)                          r = 0..R-1
+//   twiddle  x_r *= w_{Ns*R}^{r*k},  k = b mod Ns (w_M = exp(-2*pi*i/M))
+//   outputs  (b div Ns)*Ns*R + k + r*Ns           (natural order after the last pass)
+// Thread t of a row owns butterflies b = t + T*i, so every pass reads the
+// thread's slots at positions t + T*j (j = i + r*E/R): the first-pass loads and
+// the last-pass stores are both unit-stride across a warp.
+//
+// All index arithmetic lives in ESTL_HD functions so that the same code runs
+// under the host emulator (ESTL_EMU: every global/shared access is bounds
+// checked, barriers are std::barrier) before it ever runs on a GPU.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define ESTL_HD __device__ __forceinline__
+#define ESTL_CX __host__ __device__ constexpr
+#else
+#define ESTL_HD inline
+#define ESTL_CX constexpr
+#endif
+
+#ifdef ESTL_EMU
+void estl_emu_sync();
+[[noreturn]] void estl_emu_fail(const char* what, long long idx, long long n);
+#define ESTL_SYNC() estl_emu_sync()
+#define ESTL_CHECK(i, n, what)                                                       \
+  do {                                                                               \
+    if (!((long long)(i) >= 0 && (long long)(i) < (long long)(n)))                   \
+      estl_emu_fail(what, (long long)(i), (long long)(n));                           \
+  } while (0)
+#else
+#define ESTL_SYNC() __syncthreads()
+#define ESTL_CHECK(i, n, what) ((void)0)
+#endif
+
+namespace estl {
+
+// Interleaved complex64, the device image of Complex<float> in the
+// SplitInterleavedDataInterface(n, false) layout (DataInterface.h:37-45,
+// Complex.h:177-180): re at 2i, im at 2i+1.
+struct alignas(8) cf32 {
+  float x, y;
+};
+
+ESTL_HD cf32 cadd(cf32 a, cf32 b) { return {a.x + b.x, a.y + b.y}; }
+ESTL_HD cf32 csub(cf32 a, cf32 b) { return {a.x - b.x, a.y - b.y}; }
+ESTL_HD cf32 cmul(cf32 a, cf32 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+ESTL_HD cf32 mul_mi(cf32 a) { return {a.y, -a.x}; }  // a * (-i)
+
+// Pointer with an element count.  The count is only checked by the emulator.
+template <class T>
+struct Ptr {
+  T* p;
+  long long n;
+  ESTL_HD T& operator[](long long i) const {
+    ESTL_CHECK(i, n, "global/shared index");
+    return p[i];
+  }
+  // Sub-range [off, off + len): lets the hot loops index with 32-bit offsets.
+  ESTL_HD Ptr sub(long long off, long long len) const {
+    ESTL_CHECK(off, n + 1, "sub-range start");
+    ESTL_CHECK(off + len, n + 1, "sub-range end");
+    return Ptr{p + off, len};
+  }
+};
+
+// Read-only global load through the non-coherent path.
+ESTL_HD cf32 ldg(const Ptr<const cf32>& q, long long i) {
+  ESTL_CHECK(i, q.n, "global load");
+#if defined(__CUDA_ARCH__)
+  float2 v = __ldg(reinterpret_cast<const float2*>(q.p) + i);
+  return {v.x, v.y};
+#else
+  return q.p[i];
+#endif
+}
+
+// Streaming global load/store: the input of a transform is read once and its
+// output written once, so they are marked evict-first in L1/L2.
+ESTL_HD cf32 ldcs(const Ptr<const cf32>& q, long long i) {
+  ESTL_CHECK(i, q.n, "global load");
+#if defined(__CUDA_ARCH__)
+  float2 v = __ldcs(reinterpret_cast<const float2*>(q.p) + i);
+  return {v.x, v.y};
+#else
+  return q.p[i];
+#endif
+}
+ESTL_HD void stcs(const Ptr<cf32>& q, long long i, cf32 v) {
+  ESTL_CHECK(i, q.n, "global store");
+#if defined(__CUDA_ARCH__)
+  __stcs(reinterpret_cast<float2*>(q.p) + i, make_float2(v.x, v.y));
+#else
+  q.p[i] = v;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Register DFTs (forward, e^{-2 pi i / R}), natural-order in and out.
+// The reference generates these as fully unrolled radix-2 networks with
+// 6-significant-digit twiddle literals (KernelGenerator.h:53-69,100-142); here
+// they are radix-4 based with exactly rounded FP32 constants.
+// ---------------------------------------------------------------------------
+constexpr float kC8 = 0.70710678118654752440f;   // cos(pi/4)
+constexpr float kC16 = 0.92387953251128675613f;  // cos(pi/8)
+constexpr float kS16 = 0.38268343236508977173f;  // sin(pi/8)
+
+ESTL_HD cf32 cmulc(cf32 a, float c, float s) { return {a.x * c - a.y * s, a.x * s + a.y * c}; }
+
+ESTL_HD void dft2(cf32& a, cf32& b) {
+  cf32 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+ESTL_HD void dft4(cf32& x0, cf32& x1, cf32& x2, cf32& x3) {
+  cf32 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = mul_mi(csub(x1, x3));
+  x0 = cadd(a, c);
+  x2 = csub(a, c);
+  x1 = cadd(b, d);
+  x3 = csub(b, d);
+}
+
+// x * w8^1 = x * (c, -c)
+ESTL_HD cf32 mul_w8_1(cf32 a) { return {kC8 * (a.x + a.y), kC8 * (a.y - a.x)}; }
+// x * w8^3 = x * (-c, -c)
+ESTL_HD cf32 mul_w8_3(cf32 a) { return {kC8 * (a.y - a.x), -kC8 * (a.x + a.y)}; }
+
+template <int R>
+struct DFT;
+
+template <>
+struct DFT<1> {
+  ESTL_HD static void run(cf32*) {}
+};
+template <>
+struct DFT<2> {
+  ESTL_HD static void run(cf32* x) { dft2(x[0], x[1]); }
+};
+template <>
+struct DFT<4> {
+  ESTL_HD static void run(cf32* x) { dft4(x[0], x[1], x[2], x[3]); }
+};
+template <>
+struct DFT<8> {
+  // decimation in frequency: a_r = x_r + x_{r+4}, b_r = (x_r - x_{r+4}) w8^r,
+  // X[2k] = DFT4(a)[k], X[2k+1] = DFT4(b)[k].
+  ESTL_HD static void run(cf32* x) {
+    cf32 a0 = cadd(x[0], x[4]), a1 = cadd(x[1], x[5]), a2 = cadd(x[2], x[6]), a3 = cadd(x[3], x[7]);
+    cf32 b0 = csub(x[0], x[4]);
+    cf32 b1 = mul_w8_1(csub(x[1], x[5]));
+    cf32 b2 = mul_mi(csub(x[2], x[6]));
+    cf32 b3 = mul_w8_3(csub(x[3], x[7]));
+    dft4(a0, a1, a2, a3);
+    dft4(b0, b1, b2, b3);
+    x[0] = a0; x[2] = a1; x[4] = a2; x[6] = a3;
+    x[1] = b0; x[3] = b1; x[5] = b2; x[7] = b3;
+  }
+};
+template <>
+struct DFT<16> {
+  // 4 x 4: n = n2 + 4 n1, k = k1 + 4 k2.
+  //   A[n2][k1] = DFT4_n1(x[n2 + 4 n1]) * w16^(n2 k1);  X[k1 + 4 k2] = DFT4_n2(A[n2][k1]).
+  ESTL_HD static void run(cf32* x) {
+    dft4(x[0], x[4], x[8], x[12]);
+    dft4(x[1], x[5], x[9], x[13]);
+    dft4(x[2], x[6], x[10], x[14]);
+    dft4(x[3], x[7], x[11], x[15]);
+    // now x[n2 + 4 k1] = A[n2][k1]
+    x[5] = cmulc(x[5], kC16, -kS16);   // w^1
+    x[9] = mul_w8_1(x[9]);             // w^2
+    x[13] = cmulc(x[13], kS16, -kC16); // w^3
+    x[6] = mul_w8_1(x[6]);             // w^2
+    x[10] = mul_mi(x[10]);             // w^4
+    x[14] = mul_w8_3(x[14]);           // w^6
+    x[7] = cmulc(x[7], kS16, -kC16);   // w^3
+    x[11] = mul_w8_3(x[11]);           // w^6
+    x[15] = cmulc(x[15], -kC16, kS16); // w^9
+    dft4(x[0], x[1], x[2], x[3]);      // k1 = 0 -> X[0], X[4], X[8], X[12]
+    dft4(x[4], x[5], x[6], x[7]);      // k1 = 1
+    dft4(x[8], x[9], x[10], x[11]);    // k1 = 2
+    dft4(x[12], x[13], x[14], x[15]);  // k1 = 3
+    // x[4 k1 + k2] = X[k1 + 4 k2]: transpose the 4x4 block in registers
+    cf32 t;
+    t = x[1]; x[1] = x[4]; x[4] = t;
+    t = x[2]; x[2] = x[8]; x[8] = t;
+    t = x[3]; x[3] = x[12]; x[12] = t;
+    t = x[6]; x[6] = x[9]; x[9] = t;
+    t = x[7]; x[7] = x[13]; x[13] = t;
+    t = x[11]; x[11] = x[14]; x[14] = t;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Twiddle bank: one device table holding w_{2^k}^j for every k <= kBankLog
+// at index 2^k + j, followed by 4096-entry "low" tables for 2^(kBankLog+1)..2^kMaxLog
+// so that w_N^a = lo_N[a mod 4096] * w_{N/4096}^{a div 4096} for large N.
+// Generated on the device from FP64 sincospi and rounded once to FP32.
+// ---------------------------------------------------------------------------
+constexpr int kBankLog = 18;
+constexpr int kMaxLog = 26;
+constexpr int kLoLog = 12;
+constexpr long long kBankDirect = 1LL << (kBankLog + 1);
+constexpr long long kBankSize = kBankDirect + (long long)(kMaxLog - kBankLog) * (1LL << kLoLog);
+ESTL_CX long long bank_lo_offset(int logn) { return kBankDirect + (long long)(logn - kBankLog - 1) * (1LL << kLoLog); }
+
+// w_N^a for 0 <= a < N, N = 2^logn.
+ESTL_HD cf32 twiddle_n(const Ptr<const cf32>& bank, int logn, int a) {
+  if (logn <= kBankLog) return ldg(bank, (1 << logn) + a);
+  cf32 lo = ldg(bank, (int)bank_lo_offset(logn) + (a & ((1 << kLoLog) - 1)));
+  cf32 hi = ldg(bank, (1 << (logn - kLoLog)) + (a >> kLoLog));
+  return cmul(lo, hi);
+}
+
+// x_r *= w_M^{r u} for r = 1..R-1 with w_M^{u}, w_M^{2u}, w_M^{4u}, w_M^{8u}
+// loaded from the table (tw points at w_M^0) and the other powers formed by at
+// most three products.
+template <int R>
+ESTL_HD void twiddle_apply(cf32* x, const Ptr<const cf32>& tw, int u) {
+  if constexpr (R == 2) {
+    x[1] = cmul(x[1], ldg(tw, u));
+  } else if constexpr (R == 4) {
+    cf32 w1 = ldg(tw, u), w2 = ldg(tw, 2 * u);
+    x[1] = cmul(x[1], w1);
+    x[2] = cmul(x[2], w2);
+    x[3] = cmul(x[3], cmul(w1, w2));
+  } else if constexpr (R == 8) {
+    cf32 w1 = ldg(tw, u), w2 = ldg(tw, 2 * u), w4 = ldg(tw, 4 * u);
+    cf32 w3 = cmul(w1, w2);
+    x[1] = cmul(x[1], w1);
+    x[2] = cmul(x[2], w2);
+    x[3] = cmul(x[3], w3);
+    x[4] = cmul(x[4], w4);
+    x[5] = cmul(x[5], cmul(w1, w4));
+    x[6] = cmul(x[6], cmul(w2, w4));
+    x[7] = cmul(x[7], cmul(w3, w4));
+  } else if constexpr (R == 16) {
+    cf32 w1 = ldg(tw, u), w2 = ldg(tw, 2 * u), w4 = ldg(tw, 4 * u), w8 = ldg(tw, 8 * u);
+    cf32 w3 = cmul(w1, w2), w5 = cmul(w1, w4), w6 = cmul(w2, w4), w7 = cmul(w3, w4);
+    x[1] = cmul(x[1], w1);
+    x[2] = cmul(x[2], w2);
+    x[3] = cmul(x[3], w3);
+    x[4] = cmul(x[4], w4);
+    x[5] = cmul(x[5], w5);
+    x[6] = cmul(x[6], w6);
+    x[7] = cmul(x[7], w7);
+    x[8] = cmul(x[8], w8);
+    x[9] = cmul(x[9], cmul(w1, w8));
+    x[10] = cmul(x[10], cmul(w2, w8));
+    x[11] = cmul(x[11], cmul(w3, w8));
+    x[12] = cmul(x[12], cmul(w4, w8));
+    x[13] = cmul(x[13], cmul(w5, w8));
+    x[14] = cmul(x[14], cmul(w6, w8));
+    x[15] = cmul(x[15], cmul(w7, w8));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Radix schedule of an M = 2^LOGM point tile FFT: full passes of radix
+// 2^LOGR, then one remainder pass.  Mirrors the reference plan
+// BGs = [16]*floor(log2 N / 4) (+ 2^(log2 N mod 4)) (FFT_OpenCL_Contiguous.h:54-61)
+// with its prefix products A_q / N_q (OpenCLFFTAlgorithm.h:9-12).
+// ---------------------------------------------------------------------------
+template <int LOGM, int LOGE, int LOGR>
+struct Tile {
+  static_assert(LOGE >= LOGR || LOGE >= LOGM, "elements per thread must cover a radix");
+  static constexpr int M = 1 << LOGM;
+  static constexpr int LR_FULL = (LOGR < LOGM) ? LOGR : LOGM;
+  static constexpr int E = 1 << LOGE;
+  static constexpr int LOGT = LOGM - LOGE;
+  static constexpr int T = 1 << LOGT;
+  static constexpr int NFULL = LOGM / LR_FULL;
+  static constexpr int LREM = LOGM % LR_FULL;
+  static constexpr int P = NFULL + (LREM ? 1 : 0);
+  static_assert(LOGM >= LOGE, "tile smaller than a thread's register block");
+
+  ESTL_CX static int lr(int p) { return p < NFULL ? LR_FULL : LREM; }
+  ESTL_CX static int lns(int p) { return p * LR_FULL; }
+
+  // Compute pass p in registers: v[j] holds position t + T*j on entry and
+  // output y_r of butterfly i (slot j = i + r*E/R) on exit.
+  template <int p>
+  ESTL_HD static void compute(cf32 (&v)[E], int t, const Ptr<const cf32>& tw) {
+    constexpr int LR = lr(p), R = 1 << LR, LNS = lns(p), NS = 1 << LNS, G = E / R;
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      cf32 x[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) x[r] = v[i + r * G];
+      if constexpr (NS > 1) {
+        int b = t + T * i;
+        int k = b & (NS - 1);
+        int u = k << (LOGM - LNS - LR);  // k * M / (Ns * R)
+        twiddle_apply<R>(x, tw, u);
+      }
+      DFT<R>::run(x);
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[i + r * G] = x[r];
+    }
+  }
+
+  // Output position of slot j after pass p.
+  template <int p>
+  ESTL_HD static int out_pos(int t, int j) {
+    constexpr int LR = lr(p), R = 1 << LR, LNS = lns(p), NS = 1 << LNS, G = E / R;
+    int i = j & (G - 1), r = j / G;
+    int b = t + T * i;
+    int k = b & (NS - 1);
+    return ((b - k) << LR) + k + (r << LNS);
+  }
+
+  // Shared-memory row padding: one spare slot per 16 elements keeps the
+  // scattered pass stores free of bank conflicts.
+  ESTL_CX static int pad(int m) { return m + (m >> 4); }
+  static constexpr int MP = M + (M >> 4);
+};
+
+// Runs passes p..P-1 over the tile.  Between passes each thread writes its
+// outputs to shared memory at their Stockham positions and re-reads its next
+// inputs at t + T*j.  SIDX maps (column c, position m) to a shared index.
+template <class TL, int p, class SIDX>
+ESTL_HD void run_passes(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw,
+                        SIDX sidx) {
+  if constexpr (p < TL::P) {
+    TL::template compute<p>(v, t, tw);
+    if constexpr (p + 1 < TL::P) {
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) sm[sidx(c, TL::template out_pos<p>(t, j))] = v[j];
+      ESTL_SYNC();
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = sm[sidx(c, t + TL::T * j)];
+      ESTL_SYNC();
+    }
+    run_passes<TL, p + 1>(v, t, c, sm, tw, sidx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch parameters shared by all tile kernels.
+// ---------------------------------------------------------------------------
+struct TileArgs {
+  Ptr<const cf32> in;
+  Ptr<cf32> out;
+  Ptr<const cf32> bank;
+  long long rows;  // single: number of transforms
+  int logn;        // log2 of the full transform length
+  int logn1;       // four-step: log2 N1 (N = N1 * N2)
+  float sgn;       // +1 forward; -1 = backward via conj(FFT(conj(x)))
+};
+
+ESTL_HD cf32 conj_if(cf32 v, float sgn) { return {v.x, v.y * sgn}; }
+
+// Whole transforms of length M = 2^LOGM, C transforms per CTA.  Thread
+// (c, t) = (tid >> LOGT, tid & (T-1)): unit-stride rows for loads and stores.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct SingleKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = (TL::MP | 1);  // odd row stride
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static_assert(NT <= 1024, "too many threads");
+
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const long long row = cta * C + c;
+    const bool valid = row < a.rows;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    cf32 v[TL::E];
+    if (valid) {
+      const Ptr<const cf32> in = a.in.sub(row * TL::M, TL::M);
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, t + TL::T * j), a.sgn);
+    } else {
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    if (valid) {
+      const Ptr<cf32> out = a.out.sub(row * TL::M, TL::M);
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) stcs(out, t + TL::T * j, conj_if(v[j], a.sgn));
+    }
+  }
+};
+
+// Four-step column pass: N = N1 * N2, x[n1 + N1 n2].  A CTA owns C adjacent
+// columns n1 of one transform and runs their N2-point DFTs (M = N2), then
+// multiplies by w_N^{n1 k2} and writes S[k2 * N1 + n1].  Thread mapping is
+// column-fastest so both the loads and the stores move runs of C elements.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ColKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
+  static_assert(NT <= 1024, "too many threads");
+
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
+  };
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int c = tid & (C - 1);
+    const int t = tid >> LOGC;
+    const int logn1 = a.logn - LOGM;
+    const int N = 1 << a.logn, N1 = 1 << logn1;
+    const int nblk = N1 >> LOGC;
+    const long long f = cta / nblk;
+    const int n1 = (int)(cta - f * nblk) * C + c;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<const cf32> in = a.in.sub(f * N, N);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, n1 + ((t + TL::T * j) << logn1)), a.sgn);
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    const Ptr<cf32> out = a.out.sub(f * N, N);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k2 = t + TL::T * j;
+      cf32 w = twiddle_n(a.bank, a.logn, n1 * k2);
+      out[(k2 << logn1) + n1] = cmul(v[j], w);
+    }
+  }
+};
+
+// Four-step row pass: reads S[k2 * N1 + n1] (C contiguous rows of N1 = M),
+// runs the N1-point DFTs and writes X[k2 + N2 k1].  The rows are loaded
+// unit-stride; the results are staged in shared memory and stored
+// column-fastest so that every store moves a run of C elements.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct RowKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = (TL::MP | 1);
+  static constexpr int SMEM_ELEMS = C * CS;
+  static_assert(NT <= 1024, "too many threads");
+  static_assert(NT % C == 0 && (NT / C) * TL::E >= TL::M, "store remap must cover the tile");
+
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int N = 1 << a.logn;
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = cta / nblk;
+    const int k2_0 = (int)(cta - f * nblk) * C;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Sidx sidx{};
+    cf32 v[TL::E];
+    const Ptr<const cf32> in = a.in.sub(f * N + (long long)(k2_0 + c) * TL::M, TL::M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = in[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    constexpr int T2 = NT / C;  // == TL::T
+    const Ptr<cf32> out = a.out.sub(f * N, N);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k1 = t2 + T2 * j;
+      stcs(out, k2_0 + c2 + (k1 << logn2), conj_if(sm[sidx(c2, k1)], a.sgn));
+    }
+  }
+};
+
+}  // namespace estl

@@ -1,0 +1,41 @@
+// kernels.cuh — __global__ wrappers and the kernel registry entries for the
+// tile FFT kernels of fft_core.cuh.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fft_core.cuh"
+
+namespace estl {
+
+enum KernelKind { KIND_SINGLE = 0, KIND_COL = 1, KIND_ROW = 2 };
+
+struct KernelDesc {
+  int kind;
+  int logm, loge, logr, logc;
+  int nthreads;
+  int smem_bytes;
+  const void* fn;
+};
+
+template <class K>
+__global__ void __launch_bounds__(K::NT) tile_kernel(TileArgs a) {
+  extern __shared__ float2 estl_smem[];
+  K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
+}
+
+template <class K>
+KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc) {
+  return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
+                    reinterpret_cast<const void*>(&tile_kernel<K>)};
+}
+
+#define ESTL_SINGLE(M, E, R, C) make_desc<SingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C)
+#define ESTL_COL(M, E, R, C) make_desc<ColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
+#define ESTL_ROW(M, E, R, C) make_desc<RowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C)
+
+// Per translation unit tables (kernels_*.cu).
+int registry_single(const KernelDesc** out);
+int registry_col(const KernelDesc** out);
+int registry_row(const KernelDesc** out);
+
+}  // namespace estl

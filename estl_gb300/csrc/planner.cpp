@@ -1,0 +1,237 @@
+// planner.cpp — see planner.h.
+#include "planner.h"
+
+#include <algorithm>
+#include <cstdio>
+
+#include "fft_core.cuh"
+
+namespace estl {
+
+namespace {
+
+template <class K>
+TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc) {
+  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32))};
+}
+
+std::vector<TileCfg> build_configs() {
+  std::vector<TileCfg> v;
+#define ESTL_X_SINGLE(M, E, R, C) v.push_back(cfg_of<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
+#define ESTL_X_COL(M, E, R, C) v.push_back(cfg_of<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
+#define ESTL_X_ROW(M, E, R, C) v.push_back(cfg_of<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
+#include "kernel_list.inc"
+  return v;
+}
+
+// Planner defaults: the configuration used before any autotuning.
+// Single kernel: elements/thread 16, about 256 threads per CTA.
+// Four-step: N2 = 2^floor(log2 N / 2) column DFTs, the widest column/row
+// chunk whose CTA still fits 512 threads.
+const TileCfg* default_single(int logm) {
+  const TileCfg* best = nullptr;
+  for (const TileCfg& c : tile_configs()) {
+    if (c.kind != STEP_SINGLE || c.logm != logm) continue;
+    if (c.loge != std::min(4, logm)) continue;
+    if (!best || std::abs(c.nthreads - 256) < std::abs(best->nthreads - 256)) best = &c;
+  }
+  return best;
+}
+
+const TileCfg* default_pass(int kind, int logm, int max_logc) {
+  const TileCfg* best = nullptr;
+  for (const TileCfg& c : tile_configs()) {
+    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > max_logc) continue;
+    if (c.nthreads > 512) continue;
+    if (!best || c.logc > best->logc) best = &c;
+  }
+  if (!best)
+    for (const TileCfg& c : tile_configs()) {
+      if (c.kind != kind || c.logm != logm || c.logc > max_logc) continue;
+      if (!best || c.nthreads < best->nthreads) best = &c;
+    }
+  return best;
+}
+
+}  // namespace
+
+const std::vector<TileCfg>& tile_configs() {
+  static const std::vector<TileCfg> v = build_configs();
+  return v;
+}
+
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc) {
+  for (const TileCfg& c : tile_configs())
+    if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc) return &c;
+  return nullptr;
+}
+
+int ilog2_exact(long long n) {
+  if (n < 1) return -1;
+  int l = 0;
+  while ((1LL << l) < n) l++;
+  return ((1LL << l) == n) ? l : -1;
+}
+
+static void set_err(std::string* err, const char* msg, long long a = 0, long long b = 0) {
+  if (!err) return;
+  char buf[256];
+  std::snprintf(buf, sizeof buf, msg, a, b);
+  *err = buf;
+}
+
+bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* out, std::string* err) {
+  int logn = ilog2_exact(n);
+  if (logn < 0) {
+    set_err(err, "transform length %lld is not a power of two", n);
+    return false;
+  }
+  if (logn > kMaxLogN) {
+    set_err(err, "transform length 2^%lld exceeds the supported maximum 2^%lld", logn, kMaxLogN);
+    return false;
+  }
+  if (batch < 1) {
+    set_err(err, "batch must be >= 1 (got %lld)", batch);
+    return false;
+  }
+  Plan1D p;
+  p.n = n;
+  p.batch = batch;
+  p.logn = logn;
+  p.choice = choice;
+  const long long total = n * batch;
+
+  if (logn == 0) {
+    Step s{STEP_COPY, 0, 0, 0, 0, 1, BUF_IN, BUF_OUT, 0, total, 0, total, total, 0};
+    p.steps.push_back(s);
+    p.hbm_passes = 1;
+    *out = p;
+    return true;
+  }
+
+  int mode = choice.mode;
+  if (mode == 0) mode = (logn <= kSingleMaxLog) ? 1 : 2;
+
+  if (mode == 1) {
+    if (logn > kSingleMaxLog) {
+      set_err(err, "single-kernel plan needs log2 n <= %lld (got %lld)", kSingleMaxLog, logn);
+      return false;
+    }
+    const TileCfg* c = nullptr;
+    if (choice.single_loge >= 0)
+      c = find_tile(STEP_SINGLE, logn, choice.single_loge, 4, choice.single_logc);
+    else
+      c = default_single(logn);
+    if (!c) {
+      set_err(err, "no single-kernel tile instantiated for log2 n = %lld", logn);
+      return false;
+    }
+    const long long per = 1LL << c->logc;
+    Step s{STEP_SINGLE, c->logm, c->loge, c->logr, c->logc, (batch + per - 1) / per, BUF_IN, BUF_OUT,
+           0, total, 0, total, batch, logn};
+    p.steps.push_back(s);
+    p.hbm_passes = 1;
+    *out = p;
+    return true;
+  }
+
+  // four-step
+  int logn2 = choice.logn2 >= 0 ? choice.logn2 : logn / 2;
+  int logn1 = logn - logn2;
+  const TileCfg* col = nullptr;
+  const TileCfg* row = nullptr;
+  if (choice.col_loge >= 0)
+    col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
+  else
+    col = default_pass(STEP_COL, logn2, logn1);
+  if (choice.row_loge >= 0)
+    row = find_tile(STEP_ROW, logn1, choice.row_loge, 4, choice.row_logc);
+  else
+    row = default_pass(STEP_ROW, logn1, logn2);
+  if (!col || !row) {
+    set_err(err, "no four-step tiles instantiated for N1 = 2^%lld, N2 = 2^%lld", logn1, logn2);
+    return false;
+  }
+  if (col->logc > logn1 || row->logc > logn2) {
+    set_err(err, "four-step chunk wider than the transform (N1 = 2^%lld, N2 = 2^%lld)", logn1, logn2);
+    return false;
+  }
+  long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (256LL << 20) / (8 * n));
+  chunk = std::min(chunk, batch);
+  p.scratch_elems = chunk * n;
+  for (long long b0 = 0; b0 < batch; b0 += chunk) {
+    long long cnt = std::min(chunk, batch - b0);
+    Step a{STEP_COL, col->logm, col->loge, col->logr, col->logc, cnt << (logn1 - col->logc), BUF_IN, BUF_SCRATCH,
+           b0 * n, cnt * n, 0, cnt * n, cnt, logn};
+    Step b{STEP_ROW, row->logm, row->loge, row->logr, row->logc, cnt << (logn2 - row->logc), BUF_SCRATCH, BUF_OUT,
+           0, cnt * n, b0 * n, cnt * n, cnt, logn};
+    p.steps.push_back(a);
+    p.steps.push_back(b);
+  }
+  p.hbm_passes = 2;
+  *out = p;
+  return true;
+}
+
+std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
+  std::vector<PlanChoice> out;
+  int logn = ilog2_exact(n);
+  if (logn < 0 || logn > kMaxLogN) return out;
+  out.push_back(PlanChoice{});
+  if (logn == 0) return out;
+  if (logn <= kSingleMaxLog) {
+    for (const TileCfg& c : tile_configs()) {
+      if (c.kind != STEP_SINGLE || c.logm != logn) continue;
+      PlanChoice ch;
+      ch.mode = 1;
+      ch.single_loge = c.loge;
+      ch.single_logc = c.logc;
+      out.push_back(ch);
+    }
+  }
+  if (logn >= 14) {
+    for (int logn2 = 7; logn2 <= 12; ++logn2) {
+      int logn1 = logn - logn2;
+      if (logn1 < 7 || logn1 > 12) continue;
+      for (const TileCfg& c : tile_configs()) {
+        if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1) continue;
+        for (const TileCfg& r : tile_configs()) {
+          if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2) continue;
+          for (long long chunk : {0LL, 4LL << 20, 16LL << 20, 64LL << 20}) {
+            PlanChoice ch;
+            ch.mode = 2;
+            ch.logn2 = logn2;
+            ch.col_loge = c.loge;
+            ch.col_logc = c.logc;
+            ch.row_loge = r.loge;
+            ch.row_logc = r.logc;
+            ch.chunk = chunk == 0 ? 0 : std::max(1LL, chunk / n);
+            out.push_back(ch);
+          }
+        }
+      }
+    }
+  }
+  (void)batch;
+  return out;
+}
+
+std::string Plan1D::describe() const {
+  std::string s;
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "{\"n\": %lld, \"batch\": %lld, \"hbm_passes\": %d, \"launches\": %zu, \"scratch_bytes\": %lld, \"kernels\": [",
+                n, batch, hbm_passes, steps.size(), scratch_elems * 8);
+  s += buf;
+  const char* names[] = {"single", "col", "row", "copy"};
+  int shown = 0;
+  for (size_t i = 0; i < steps.size() && shown < 2; ++i, ++shown) {
+    const Step& st = steps[i];
+    std::snprintf(buf, sizeof buf, "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"grid\": %lld}",
+                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid);
+    s += buf;
+  }
+  s += "]}";
+  return s;
+}
+
+}  // namespace estl

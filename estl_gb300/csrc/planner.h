@@ -1,0 +1,77 @@
+// planner.h — host-side FFT plan: which tile kernels run, on which buffers,
+// in which order.  Pure C++ (no CUDA calls) so that the CPU index emulator
+// executes exactly the launch list the GPU executor runs.
+//
+// Reference counterpart: the constructor of FFT_OpenCL_Contiguous
+// (FFT_OpenCL_Contiguous.h:46-71), which fixes the radix list BGs and builds
+// one kernel per radix-16 pass, and OpenCLFFTAlgorithm::computeParameters
+// (OpenCLFFTAlgorithm.h:9-12).  Here the plan groups passes into tile kernels:
+//   log2 N <= 14 : one launch (all passes of a transform in one CTA)
+//   log2 N >  14 : four-step N = N1 * N2, a column launch then a row launch
+//                  per chunk of transforms (two HBM round trips)
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace estl {
+
+enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3 };
+enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_SCRATCH = 2 };
+
+struct TileCfg {
+  int kind;  // STEP_SINGLE / STEP_COL / STEP_ROW
+  int logm, loge, logr, logc;
+  int nthreads;
+  int smem_bytes;
+};
+
+// All instantiated tile kernels (kernel_list.inc).
+const std::vector<TileCfg>& tile_configs();
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc);
+
+struct Step {
+  int kind;
+  int logm, loge, logr, logc;
+  long long grid;
+  int src, dst;
+  long long src_off, src_len;  // complex elements
+  long long dst_off, dst_len;
+  long long rows;  // STEP_SINGLE: transforms; STEP_COPY: elements
+  int logn;
+};
+
+// Tunable plan parameters (what the autotuner searches).  Zero / -1 fields
+// mean "planner default".
+struct PlanChoice {
+  int mode = 0;  // 0 default, 1 single kernel, 2 four-step
+  int single_loge = -1, single_logc = -1;
+  int logn2 = -1;  // four-step: log2 N2 (column DFT length)
+  int col_loge = -1, col_logc = -1;
+  int row_loge = -1, row_logc = -1;
+  long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
+};
+
+struct Plan1D {
+  long long n = 0, batch = 0;
+  int logn = 0;
+  PlanChoice choice;
+  std::vector<Step> steps;
+  long long scratch_elems = 0;
+  int hbm_passes = 0;
+  std::string describe() const;  // one-line JSON
+};
+
+constexpr int kSingleMaxLog = 14;
+constexpr int kMaxLogN = 24;
+
+// Returns false (with *err set) when n is not a power of two in [1, 2^24] or
+// the choice names no instantiated kernel.
+bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* out, std::string* err);
+
+// Candidate choices for (n, batch), default first (autotuner search space).
+std::vector<PlanChoice> plan_candidates(long long n, long long batch);
+
+int ilog2_exact(long long n);
+
+}  // namespace estl

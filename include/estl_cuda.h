@@ -1,0 +1,140 @@
+/* estl_cuda.h — C ABI of the GB300 FFT engine (libestl_cuda.so).
+ *
+ * This is the boundary the ESTL plugin layer binds: plain C types, device
+ * and host pointers, no exceptions, every call returns an estl_status and
+ * estl_last_error() gives the message of the last failure on the calling
+ * thread.  The C++ plugin FFT_CUDA<D> (FFT_CUDA.h) is written on top of it.
+ *
+ * Data layout: interleaved complex64 (re, im as float pairs), transform b of
+ * a batch at element offset b*n — the layout FFT_FFTW3 plans on
+ * (FFT_FFTW3.h:24-28, SplitInterleavedDataInterface(n*batch, false),
+ * DataInterface.h:37-45).  Transforms are unnormalised in both directions
+ * (FFTW_FORWARD = exp(-2 pi i jk/n), FFTW_BACKWARD = exp(+2 pi i jk/n)).
+ */
+#ifndef ESTL_CUDA_H
+#define ESTL_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Replaces the reference's exception paths: CLException via
+ * xCLErr (uOpenCL.h:21-55) and the printed-only capacity failure
+ * (FFT_OpenCL_Contiguous.h:49). */
+typedef enum estl_status {
+  ESTL_OK = 0,
+  ESTL_INVALID_ARG = 1,
+  ESTL_UNSUPPORTED_SIZE = 2,
+  ESTL_OUT_OF_MEMORY = 3,
+  ESTL_ADMISSION_REJECTED = 4,
+  ESTL_DEVICE_ERROR = 5,
+  ESTL_TIMEOUT = 6,
+  ESTL_NOT_INITIALIZED = 7
+} estl_status;
+
+/* Direction, FFTW sign convention (FFT_FFTW3.h:28: forward ? FFTW_FORWARD : FFTW_BACKWARD). */
+#define ESTL_FORWARD (-1)
+#define ESTL_BACKWARD (+1)
+
+/* Arithmetic of a plan.  FP32 is the plain path. */
+#define ESTL_PREC_FP32 0
+
+typedef struct estl_plan_s* estl_plan;
+
+/* Select the CUDA device, allocate the twiddle bank and set the HBM budget
+ * (bytes; 0 = 90% of the memory free at init).  Replaces OpenCLAlgorithm's
+ * constructor (uOpenCL.h:284-321: platform/device/context/queue set-up).
+ * Idempotent for the same device. */
+estl_status estl_init(int device, size_t hbm_budget_bytes);
+
+/* Release every plan and the twiddle bank. */
+estl_status estl_shutdown(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* estl_last_error(void);
+
+/* Name of a status code. */
+const char* estl_status_string(estl_status status);
+
+/* Largest batch of n-point transforms the HBM budget admits for a plan with
+ * its own input, output and scratch buffers; clamped to INT32_MAX.
+ * Replaces FFT_OpenCL_Contiguous::getMaxBatchSize (FFT_OpenCL_Contiguous.h:43-44),
+ * computed in 64 bits instead of the int that overflows above 2 GiB
+ * (uOpenCL.h:323-332).  Returns 0 before estl_init or for unsupported n. */
+int64_t estl_max_batch(int64_t n);
+
+/* Plan `batch` transforms of length n (power of two, 1 <= n <= 2^24).
+ * direction: ESTL_FORWARD / ESTL_BACKWARD; precision: ESTL_PREC_FP32.
+ * Replaces the FFT_OpenCL_Contiguous constructor (FFT_OpenCL_Contiguous.h:46-71):
+ * radix plan, kernels (precompiled, no runtime compile) and device scratch.
+ * Uses an autotuned configuration when the tuning cache holds one for
+ * (n, batch). */
+estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precision, estl_plan* plan);
+
+/* Free the plan and its device buffers (FFT_OpenCL_Contiguous.h:186-191). */
+estl_status estl_plan_destroy(estl_plan plan);
+
+/* One-line JSON description of the plan: launches, HBM passes, tile kernels,
+ * scratch bytes.  Writes at most len bytes including the terminator. */
+estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len);
+
+/* Number of kernel launches (and device copies) one execute issues. */
+int64_t estl_plan_launches(estl_plan plan);
+
+/* Device-resident execute, stream ordered (stream: a cudaStream_t, NULL =
+ * legacy default stream).  d_in / d_out: n*batch complex64 elements each,
+ * 8-byte aligned, out-of-place (d_in is not modified; d_in == d_out is
+ * rejected).  Replaces the kernel loop of FFT_OpenCL_Contiguous::execute
+ * (FFT_OpenCL_Contiguous.h:107-124) without its host copies; backward
+ * transforms are computed for every transform of the batch (the reference
+ * conjugates only batch 0, FFT_OpenCL_Contiguous.h:100-102,134-136).
+ * Successive executes of one plan are serialised on the device (they share
+ * the plan's scratch); use separate plans for concurrent streams. */
+estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* stream);
+
+/* Host-to-host execute with the semantics of FFT<D>::execute (FFT.h:35,
+ * FFT_OpenCL_Contiguous.h:97-142): copies h_in to the device, transforms,
+ * copies the result to h_out and returns when h_out is complete.  The copy
+ * in, the transform and the copy out run pipelined over chunks of the batch
+ * on three streams.  h_in/h_out should be pinned (estl_host_register) for
+ * full bandwidth; pageable memory works but is slower. */
+estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out);
+
+/* Per-launch device timing, the counterpart of OpenCLAlgorithm's
+ * kernelTimers / timerComputation (uOpenCL.h:281-282) that
+ * FFT_OpenCL_Contiguous::execute fills from event profiling
+ * (FFT_OpenCL_Contiguous.h:129-131).  While enabled, every launch of an
+ * execute is bracketed by CUDA events on the execute's stream; enabling or
+ * disabling resets the statistics. */
+estl_status estl_plan_set_profiling(estl_plan plan, int enable);
+
+/* Per kernel kind (index 0 single-tile, 1 column pass, 2 row pass, 3 device
+ * copy): launches, summed device milliseconds and summed algorithmic bytes
+ * (16 bytes per complex element read and written).  Waits for the profiled
+ * launches to finish.  Arrays have 4 entries; any may be NULL. */
+estl_status estl_plan_kernel_stats(estl_plan plan, int64_t* launches, double* total_ms, double* bytes);
+
+/* Page-lock / unlock host memory for estl_execute_host. */
+estl_status estl_host_register(void* ptr, size_t bytes);
+estl_status estl_host_unregister(void* ptr);
+
+/* Time every candidate plan for (n, batch) on the device (iters executes
+ * each, after two warm-up executes), store the fastest in the tuning cache
+ * ($ESTL_TUNE_CACHE, else ~/.cache/estl_gb300/tune.jsonl) and use it for
+ * later estl_plan_create calls with the same n and log2(batch).  Writes a
+ * JSON summary to result_json (may be NULL).  The reference has no tuner: its
+ * radix is fixed at 16 (FFT_OpenCL_Contiguous.h:55). */
+estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* result_json, size_t len);
+
+/* Bytes currently held by the engine on the device (plans, scratch, staging,
+ * twiddle bank) and the budget set at init. */
+estl_status estl_memory_usage(size_t* used_bytes, size_t* budget_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ESTL_CUDA_H */

@@ -1,0 +1,227 @@
+/* oracle.c — TEST INFRASTRUCTURE ONLY (the checker, never the product).
+ *
+ * CPU FP64 restatement of the transform the reference's CPU backend computes:
+ *   FFT_FFTW3.h:23-31  fftwf_plan_many_dft(rank 1, n = size, howmany = batch,
+ *                      stride 1, dist = size, out-of-place, interleaved complex,
+ *                      FFTW_FORWARD = exp(-2 pi i jk/N) / FFTW_BACKWARD = exp(+2 pi i jk/N),
+ *                      unnormalised in both directions)
+ *   FFT.h:32-33        flattened element index batch*size + index
+ *   DataInterface.h:37-45 + Complex.h:177-180  interleaved (re, im) layout
+ * FFTW 3 itself (the reference links -lfftw3f, ESTL.pro:10, version not pinned)
+ * is not available here; its published definition of the DFT is restated.
+ *
+ * Pinned by: the known-answer test of tests/Test.cpp:60-77 (cosine -> two
+ * spikes of M/2, forward sign), a long-double direct DFT (oracle_dft_ld) and
+ * numpy.fft (tests/test_oracle.py).
+ *
+ * Also here: linear convolution by FFT and directly (Convolution.h:95-148
+ * restated in 1D), used to check the CUDA convolution path.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+typedef struct {
+  double re, im;
+} c64;
+
+/* ---- twiddle tables w_N^j = exp(-2 pi i j / N), j < N/2, cached per log2 N ---- */
+static c64* g_tw[40];
+static pthread_mutex_t g_tw_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static int ilog2_exact(int64_t n) {
+  int l = 0;
+  while (((int64_t)1 << l) < n) l++;
+  return (((int64_t)1 << l) == n) ? l : -1;
+}
+
+/* cos/sin of 2 pi j / N from the first octant only, so every table entry
+ * carries the error of one libm call on an argument in [0, pi/4]. */
+static void octant_cs(int64_t j, int64_t n, double* c, double* s) {
+  int64_t q = n / 8;
+  if (n < 8) {
+    double a = 2.0 * M_PI * (double)j / (double)n;
+    *c = cos(a);
+    *s = sin(a);
+    if (4 * j == n) *c = 0.0;
+    if (2 * j == n) *s = 0.0;
+    return;
+  }
+  if (j <= q) {
+    double a = 2.0 * M_PI * (double)j / (double)n;
+    *c = cos(a);
+    *s = sin(a);
+  } else if (j <= 2 * q) {
+    double a = 2.0 * M_PI * (double)(2 * q - j) / (double)n;
+    *c = sin(a);
+    *s = cos(a);
+  } else if (j <= 3 * q) {
+    double a = 2.0 * M_PI * (double)(j - 2 * q) / (double)n;
+    *c = -sin(a);
+    *s = cos(a);
+  } else {
+    double a = 2.0 * M_PI * (double)(4 * q - j) / (double)n;
+    *c = -cos(a);
+    *s = sin(a);
+  }
+}
+
+static const c64* twiddles(int logn) {
+  pthread_mutex_lock(&g_tw_lock);
+  if (!g_tw[logn]) {
+    int64_t n = (int64_t)1 << logn, h = n / 2 > 0 ? n / 2 : 1;
+    c64* t = (c64*)malloc(sizeof(c64) * (size_t)h);
+    for (int64_t j = 0; j < h; j++) {
+      double c, s;
+      octant_cs(j, n, &c, &s);
+      t[j].re = c;
+      t[j].im = -s;
+    }
+    g_tw[logn] = t;
+  }
+  const c64* r = g_tw[logn];
+  pthread_mutex_unlock(&g_tw_lock);
+  return r;
+}
+
+/* One radix-2 Stockham FFT (natural order in and out).  sign = -1 forward,
+ * +1 backward.  x is overwritten with the result; w is work space of n. */
+static void fft1(c64* x, c64* w, int logn, int sign) {
+  int64_t n = (int64_t)1 << logn, h = n / 2;
+  const c64* tw = twiddles(logn);
+  c64 *src = x, *dst = w;
+  for (int64_t ns = 1; ns < n; ns *= 2) {
+    int64_t step = n / (2 * ns);
+    for (int64_t j = 0; j < h; j++) {
+      int64_t k = j & (ns - 1);
+      c64 wk = tw[k * step];
+      if (sign > 0) wk.im = -wk.im;
+      c64 a = src[j], b = src[j + h];
+      c64 bw = {b.re * wk.re - b.im * wk.im, b.re * wk.im + b.im * wk.re};
+      int64_t o = (j - k) * 2 + k;
+      dst[o].re = a.re + bw.re;
+      dst[o].im = a.im + bw.im;
+      dst[o + ns].re = a.re - bw.re;
+      dst[o + ns].im = a.im - bw.im;
+    }
+    c64* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (src != x) memcpy(x, src, sizeof(c64) * (size_t)n);
+}
+
+typedef struct {
+  const double* in;
+  double* out;
+  int64_t n, b0, b1;
+  int logn, sign;
+} job_t;
+
+static void* fft_worker(void* arg) {
+  job_t* jb = (job_t*)arg;
+  c64* w = (c64*)malloc(sizeof(c64) * (size_t)jb->n);
+  for (int64_t b = jb->b0; b < jb->b1; b++) {
+    c64* o = (c64*)(jb->out + 2 * b * jb->n);
+    if ((const double*)o != jb->in + 2 * b * jb->n) memcpy(o, jb->in + 2 * b * jb->n, sizeof(c64) * (size_t)jb->n);
+    fft1(o, w, jb->logn, jb->sign);
+  }
+  free(w);
+  return NULL;
+}
+
+/* Batched FP64 FFT with the plan semantics of FFT_FFTW3.h:26-28.
+ * in/out: interleaved complex128, batch*n elements.  Returns 0, or -1 when n
+ * is not a power of two (the reference plan rounds every size up to 2^k,
+ * SimpleMath.h:7-11, FFT_OpenCL_Contiguous.h:56). */
+int oracle_fft(const double* in, double* out, int64_t n, int64_t batch, int sign, int nthreads) {
+  int logn = ilog2_exact(n);
+  if (logn < 0 || batch < 0) return -1;
+  if (n == 1) {
+    memmove(out, in, sizeof(double) * 2 * (size_t)batch);
+    return 0;
+  }
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > batch) nthreads = (int)(batch > 0 ? batch : 1);
+  pthread_t th[256];
+  job_t jobs[256];
+  if (nthreads > 256) nthreads = 256;
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].in = in;
+    jobs[t].out = out;
+    jobs[t].n = n;
+    jobs[t].b0 = batch * t / nthreads;
+    jobs[t].b1 = batch * (t + 1) / nthreads;
+    jobs[t].logn = logn;
+    jobs[t].sign = sign;
+  }
+  if (nthreads == 1) {
+    fft_worker(&jobs[0]);
+    return 0;
+  }
+  for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, fft_worker, &jobs[t]);
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  return 0;
+}
+
+/* Long-double direct O(n^2) DFT of one transform (independent check of
+ * oracle_fft for small n).  The phase index jk mod n is reduced exactly. */
+void oracle_dft_ld(const double* in, double* out, int64_t n, int sign) {
+  for (int64_t k = 0; k < n; k++) {
+    long double sr = 0.0L, si = 0.0L;
+    for (int64_t j = 0; j < n; j++) {
+      int64_t m = (j * k) % n;
+      long double a = 2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)n;
+      long double c = cosl(a), s = sign * sinl(a);
+      long double xr = in[2 * j], xi = in[2 * j + 1];
+      sr += xr * c - xi * s;
+      si += xr * s + xi * c;
+    }
+    out[2 * k] = (double)sr;
+    out[2 * k + 1] = (double)si;
+  }
+}
+
+/* Direct linear convolution (and correlation) of real sequences in long
+ * double: out[m] = sum_i a[i] b[m - i], length la + lb - 1. */
+void oracle_conv_direct(const double* a, int64_t la, const double* b, int64_t lb, double* out) {
+  for (int64_t m = 0; m < la + lb - 1; m++) {
+    long double s = 0.0L;
+    int64_t i0 = m - (lb - 1) > 0 ? m - (lb - 1) : 0;
+    int64_t i1 = m < la - 1 ? m : la - 1;
+    for (int64_t i = i0; i <= i1; i++) s += (long double)a[i] * (long double)b[m - i];
+    out[m] = (double)s;
+  }
+}
+
+/* FP64 FFT linear convolution of real sequences: zero-pad both to
+ * n = nextPow2(la + lb - 1) (Convolution.h:89-97), forward FFT, pointwise
+ * product (Convolution.h:132-136; conj(B) when correlate, :125-130), inverse
+ * FFT, scale 1/n, keep the real part of the first la + lb - 1 samples. */
+int oracle_conv_fft(const double* a, int64_t la, const double* b, int64_t lb, double* out, int correlate) {
+  int64_t len = la + lb - 1, n = 1;
+  while (n < len) n *= 2;
+  c64* A = (c64*)calloc((size_t)n, sizeof(c64));
+  c64* B = (c64*)calloc((size_t)n, sizeof(c64));
+  for (int64_t i = 0; i < la; i++) A[i].re = a[i];
+  for (int64_t i = 0; i < lb; i++) B[i].re = b[i];
+  oracle_fft((double*)A, (double*)A, n, 1, -1, 1);
+  oracle_fft((double*)B, (double*)B, n, 1, -1, 1);
+  for (int64_t i = 0; i < n; i++) {
+    double br = B[i].re, bi = correlate ? -B[i].im : B[i].im;
+    double r = A[i].re * br - A[i].im * bi, im = A[i].re * bi + A[i].im * br;
+    A[i].re = r;
+    A[i].im = im;
+  }
+  oracle_fft((double*)A, (double*)A, n, 1, +1, 1);
+  for (int64_t i = 0; i < len; i++) out[i] = A[i].re / (double)n;
+  free(A);
+  free(B);
+  return 0;
+}

@@ -1,0 +1,253 @@
+// emu.cpp — host emulator of the tile FFT kernels (test infrastructure).
+//
+// Runs the planner's launch list (estl_gb300/csrc/planner.cpp) through the
+// same kernel bodies the GPU runs (estl_gb300/csrc/fft_core.cuh, compiled with
+// ESTL_EMU): every emulated GPU thread is a host thread, __syncthreads is a
+// std::barrier, and every global / shared / twiddle access is bounds checked.
+// A CPU test can therefore prove that a kernel configuration stays in bounds
+// and computes the right transform before it is launched on a GPU.
+#include <barrier>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fft_core.cuh"
+#include "planner.h"
+
+using namespace estl;
+
+namespace {
+thread_local std::barrier<>* tl_bar = nullptr;
+std::mutex g_msg_mu;
+std::string g_msg;
+
+struct EmuFault : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+}  // namespace
+
+void estl_emu_sync() { tl_bar->arrive_and_wait(); }
+
+void estl_emu_fail(const char* what, long long idx, long long n) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: index %lld outside [0, %lld)", what, idx, n);
+  {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    if (g_msg.empty()) g_msg = buf;
+  }
+  throw EmuFault(buf);
+}
+
+namespace {
+
+using RunFn = void (*)(const TileArgs&, long long, int, cf32*);
+struct EmuKernel {
+  int kind, logm, loge, logr, logc, nt;
+  long long smem;
+  RunFn fn;
+};
+
+template <class K>
+EmuKernel mk(int kind, int m, int e, int r, int c) {
+  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run};
+}
+
+const std::vector<EmuKernel>& emu_kernels() {
+  static const std::vector<EmuKernel> v = [] {
+    std::vector<EmuKernel> k;
+#define ESTL_X_SINGLE(M, E, R, C) k.push_back(mk<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
+#define ESTL_X_COL(M, E, R, C) k.push_back(mk<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
+#define ESTL_X_ROW(M, E, R, C) k.push_back(mk<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
+#include "kernel_list.inc"
+    return k;
+  }();
+  return v;
+}
+
+const std::vector<cf32>& host_bank() {
+  static const std::vector<cf32> b = [] {
+    std::vector<cf32> v((size_t)kBankSize);
+    for (long long idx = 0; idx < kBankSize; ++idx) {
+      long double x;
+      if (idx < kBankDirect) {
+        if (idx < 2) {
+          v[idx] = cf32{1.f, 0.f};
+          continue;
+        }
+        int k = 0;
+        while ((2LL << k) <= idx) k++;
+        long long j = idx - (1LL << k);
+        x = -(long double)j / (long double)(1LL << (k - 1));
+      } else {
+        long long r = idx - kBankDirect;
+        int n = kBankLog + 1 + (int)(r >> kLoLog);
+        long long j = r & ((1LL << kLoLog) - 1);
+        x = -(long double)j / (long double)(1LL << (n - 1));
+      }
+      const long double pi = 3.14159265358979323846264338327950288L;
+      v[idx] = cf32{(float)cosl(pi * x), (float)sinl(pi * x)};
+    }
+    return v;
+  }();
+  return b;
+}
+
+bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
+  std::barrier<> bar(k.nt);
+  std::vector<cf32> smem((size_t)std::max<long long>(k.smem, 1));
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  for (auto& e : smem) e = cf32{nan, nan};
+  std::atomic<bool> failed{false};
+  std::vector<std::thread> th;
+  th.reserve(k.nt);
+  for (int tid = 0; tid < k.nt; ++tid) {
+    th.emplace_back([&, tid] {
+      tl_bar = &bar;
+      try {
+        for (long long cta = 0; cta < grid; ++cta) {
+          k.fn(a, cta, tid, smem.data());
+          estl_emu_sync();
+          // poison shared memory between CTAs so that a read of a slot the
+          // current CTA never wrote shows up as NaN in the output
+          if (tid == 0)
+            for (auto& e : smem) e = cf32{nan, nan};
+          estl_emu_sync();
+        }
+      } catch (const EmuFault&) {
+        failed = true;
+        bar.arrive_and_drop();
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  return !failed;
+}
+
+void set_err(char* err, int len, const std::string& s) {
+  if (err && len > 0) std::snprintf(err, (size_t)len, "%s", s.c_str());
+}
+
+PlanChoice choice_from(const int* f) {
+  PlanChoice c;
+  if (!f) return c;
+  c.mode = f[0];
+  c.single_loge = f[1];
+  c.single_logc = f[2];
+  c.logn2 = f[3];
+  c.col_loge = f[4];
+  c.col_logc = f[5];
+  c.row_loge = f[6];
+  c.row_logc = f[7];
+  c.chunk = f[8];
+  return c;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Runs the plan for (n, batch) on interleaved complex64 host data.
+// choice: 9 ints (PlanChoice fields) or NULL for the planner default.
+// sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
+// 2 plan error, 3 missing kernel.
+int emu_plan_run(long long n, long long batch, const int* choice, int sign, const float* in, float* out, char* err,
+                 int errlen) {
+  Plan1D p;
+  std::string e;
+  if (!make_plan(n, batch, choice_from(choice), &p, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    g_msg.clear();
+  }
+  const long long total = n * batch;
+  std::vector<cf32> scratch((size_t)std::max<long long>(p.scratch_elems, 1),
+                            cf32{std::numeric_limits<float>::quiet_NaN(), 0.f});
+  const cf32* cin = reinterpret_cast<const cf32*>(in);
+  cf32* cout = reinterpret_cast<cf32*>(out);
+  for (const Step& st : p.steps) {
+    const cf32* src = st.src == BUF_IN ? cin : (st.src == BUF_SCRATCH ? scratch.data() : cout);
+    long long src_cap = st.src == BUF_SCRATCH ? (long long)scratch.size() : total;
+    cf32* dst = st.dst == BUF_OUT ? cout : scratch.data();
+    long long dst_cap = st.dst == BUF_SCRATCH ? (long long)scratch.size() : total;
+    if (st.src_off < 0 || st.src_off + st.src_len > src_cap || st.dst_off < 0 || st.dst_off + st.dst_len > dst_cap) {
+      set_err(err, errlen, "step buffer range outside its allocation");
+      return 1;
+    }
+    if (st.kind == STEP_COPY) {
+      std::memcpy(dst + st.dst_off, src + st.src_off, (size_t)st.rows * sizeof(cf32));
+      continue;
+    }
+    const EmuKernel* k = nullptr;
+    for (const EmuKernel& c : emu_kernels())
+      if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc) k = &c;
+    if (!k) {
+      set_err(err, errlen, "no emulated kernel for a plan step");
+      return 3;
+    }
+    TileArgs a;
+    a.in = Ptr<const cf32>{src + st.src_off, st.src_len};
+    a.out = Ptr<cf32>{dst + st.dst_off, st.dst_len};
+    a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
+    a.rows = st.rows;
+    a.logn = st.logn;
+    a.logn1 = 0;
+    a.sgn = sign < 0 ? 1.f : -1.f;
+    if (!run_kernel(*k, a, st.grid)) {
+      std::lock_guard<std::mutex> g(g_msg_mu);
+      set_err(err, errlen, g_msg);
+      return 1;
+    }
+  }
+  return 0;
+}
+
+// Plan description (JSON) for (n, batch, choice); returns 0 or 2.
+int emu_plan_describe(long long n, long long batch, const int* choice, char* buf, int len) {
+  Plan1D p;
+  std::string e;
+  if (!make_plan(n, batch, choice_from(choice), &p, &e)) {
+    set_err(buf, len, e);
+    return 2;
+  }
+  set_err(buf, len, p.describe());
+  return 0;
+}
+
+// Candidate choices of the autotuner for (n, batch): writes up to max rows
+// of 9 ints, returns the number of candidates.
+int emu_plan_candidates(long long n, long long batch, int* out, int max) {
+  std::vector<PlanChoice> c = plan_candidates(n, batch);
+  int k = 0;
+  for (const PlanChoice& ch : c) {
+    if (k >= max) break;
+    int* f = out + 9 * k++;
+    f[0] = ch.mode;
+    f[1] = ch.single_loge;
+    f[2] = ch.single_logc;
+    f[3] = ch.logn2;
+    f[4] = ch.col_loge;
+    f[5] = ch.col_logc;
+    f[6] = ch.row_loge;
+    f[7] = ch.row_logc;
+    f[8] = (int)ch.chunk;
+  }
+  return (int)c.size();
+}
+
+// Copies the host twiddle bank (kBankSize complex64) into out (if not NULL);
+// returns kBankSize.
+long long emu_bank(float* out) {
+  if (out) std::memcpy(out, host_bank().data(), sizeof(cf32) * (size_t)kBankSize);
+  return kBankSize;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+"""Every tile kernel configuration and every plan shape, run through the host
+emulator (tests/emu/emu.cpp): the kernel bodies of estl_gb300/csrc/fft_core.cuh
+with bounds-checked global/shared/twiddle accesses and real barriers.
+
+This is the pre-flight check for GPU launches: a configuration that reads or
+writes outside its buffers, or reads shared memory it never wrote, fails here
+on the CPU (poisoned shared memory shows up as NaN in the output).
+"""
+import ctypes
+import json
+
+import numpy as np
+import pytest
+
+import oracle
+
+TOL = 2e-6  # rel-L2 bound for FP32 results, N <= 2^20
+
+
+def rand_c64(shape, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)).astype(np.complex64)
+
+
+def emu_run(emu, n, batch, x, sign=-1, choice=None):
+    y = np.full((batch, n), np.nan + 1j * np.nan, dtype=np.complex64)
+    err = ctypes.create_string_buffer(512)
+    ch = None
+    if choice is not None:
+        ch = (ctypes.c_int * 9)(*choice)
+    rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
+    return rc, err.value.decode(), y
+
+
+def candidates(emu, n, batch):
+    buf = (ctypes.c_int * (9 * 4096))()
+    k = emu.emu_plan_candidates(n, batch, buf, 4096)
+    return [list(buf[9 * i: 9 * i + 9]) for i in range(min(k, 4096))]
+
+
+def describe(emu, n, batch, choice=None):
+    buf = ctypes.create_string_buffer(2048)
+    ch = (ctypes.c_int * 9)(*choice) if choice is not None else None
+    rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
+    assert rc == 0, buf.value
+    return json.loads(buf.value.decode())
+
+
+@pytest.mark.parametrize("logn", range(0, 15))
+def test_default_plans_small(emu, logn):
+    n = 1 << logn
+    for batch in (1, 3):
+        x = rand_c64((batch, n), logn * 10 + batch)
+        for sign in (-1, +1):
+            rc, msg, y = emu_run(emu, n, batch, x, sign)
+            assert rc == 0, msg
+            assert np.all(np.isfinite(y))
+            assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL
+
+
+@pytest.mark.parametrize("logn", range(1, 15))
+def test_every_single_kernel_config(emu, logn):
+    """All instantiated single-kernel tiles, with a ragged last CTA."""
+    n = 1 << logn
+    cands = [c for c in candidates(emu, n, 5) if c[0] == 1]
+    assert cands, "no single-kernel candidates"
+    for c in cands:
+        per_cta = 1 << c[2]
+        batch = per_cta + 1 if per_cta < 64 else 3
+        x = rand_c64((batch, n), 7 + logn)
+        rc, msg, y = emu_run(emu, n, batch, x, -1, c)
+        assert rc == 0, (c, msg)
+        assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < TOL, c
+
+
+@pytest.mark.parametrize("logn", [14, 15, 16, 17])
+def test_every_four_step_config(emu, logn):
+    """All column/row tile pairs the autotuner may pick, with chunking."""
+    n = 1 << logn
+    cands = [c for c in candidates(emu, n, 2) if c[0] == 2]
+    assert cands
+    x = rand_c64((3, n), logn)
+    ref = oracle.fft(x, +1)
+    seen = set()
+    for c in cands:
+        key = tuple(c[:8])
+        if key in seen:
+            continue
+        seen.add(key)
+        c = list(c)
+        c[8] = 2  # chunk of two transforms: exercises the chunk loop with a tail
+        rc, msg, y = emu_run(emu, n, 3, x, +1, c)
+        assert rc == 0, (c, msg)
+        assert oracle.rel_l2(y, ref).max() < TOL, c
+
+
+@pytest.mark.parametrize("logn", [18, 20])
+def test_four_step_large(emu, logn):
+    n = 1 << logn
+    x = rand_c64((1, n), logn)
+    rc, msg, y = emu_run(emu, n, 1, x, -1)
+    assert rc == 0, msg
+    assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < TOL
+
+
+def test_plan_shapes(emu):
+    assert describe(emu, 1, 7)["kernels"][0]["kind"] == "copy"
+    d = describe(emu, 4096, 256)
+    assert d["hbm_passes"] == 1 and d["launches"] == 1 and d["kernels"][0]["kind"] == "single"
+    d = describe(emu, 1 << 20, 128)
+    assert d["hbm_passes"] == 2 and d["kernels"][0]["kind"] == "col" and d["kernels"][1]["kind"] == "row"
+    assert d["scratch_bytes"] <= 256 << 20
+    d = describe(emu, 1 << 24, 8)
+    assert d["launches"] == 8  # 256 MiB scratch = two 2^24-point transforms per chunk, 2 launches per chunk
+
+
+def test_rejects_bad_sizes(emu):
+    x = np.zeros((1, 16), np.complex64)
+    for n in (3, 12, 1 << 25, 0):
+        rc, msg, _ = emu_run(emu, n, 1, np.zeros((1, max(n, 1)), np.complex64))
+        assert rc == 2 and msg
+    rc, msg, _ = emu_run(emu, 16, 0, x)
+    assert rc == 2
+
+
+def test_twiddle_bank_accuracy(emu):
+    """The bank holds w_{2^k}^j rounded once from higher precision."""
+    size = emu.emu_bank(None)
+    bank = np.empty(size, np.complex64)
+    emu.emu_bank(bank.ctypes.data)
+    for k in (1, 4, 12, 18):
+        j = np.arange(1 << k)
+        exact = np.exp(-2j * np.pi * j / (1 << k))
+        got = bank[(1 << k) + j]
+        assert np.abs(got - exact).max() < 6e-8

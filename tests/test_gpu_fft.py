@@ -1,0 +1,158 @@
+"""GPU parity of the batched C2C FP32 FFT against the FP64 oracle, through the
+C ABI (libestl_cuda.so via ctypes).
+
+Tolerances (relative L2 per transform, the metric of OpenCL_FFT/main.cpp:333-359
+without the division by FLT_EPSILON): 2e-6 for N <= 2^20 and
+c * log2(N) * 2^-24 with c = 2 beyond.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(n):
+    return 2e-6 if n <= (1 << 20) else 2.0 * math.log2(n) * 2.0 ** -24
+
+
+def uniform_c64(shape, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)).astype(np.complex64)
+
+
+def run(engine, x_np, direction):
+    import torch
+    batch, n = x_np.shape
+    p = engine.Plan(n, batch, direction)
+    xd = torch.from_numpy(x_np).cuda()
+    yd = p.execute(xd)
+    torch.cuda.synchronize()
+    return yd.cpu().numpy(), p
+
+
+@pytest.mark.parametrize("logn", range(0, 25))
+def test_parity_every_size(engine, logn):
+    n = 1 << logn
+    batch = max(1, min(5, (1 << 22) // n))
+    x = uniform_c64((batch, n), 1000 + logn)
+    for direction in (-1, +1):
+        y, _ = run(engine, x, direction)
+        e = oracle.rel_l2(y, oracle.fft(x, direction))
+        assert e.max() < tol(n), (n, direction, e.max())
+
+
+def test_config1_plain_4096x256(engine):
+    """N = 4096, batch = 256, uniform[-1,1) seed 1: every transform vs the oracle."""
+    x = uniform_c64((256, 4096), 1)
+    y, p = run(engine, x, -1)
+    e = oracle.rel_l2(y, oracle.fft(x, -1))
+    assert e.max() < 2e-6
+    assert p.describe()["hbm_passes"] == 1
+
+
+def test_known_answer_like_reference(engine):
+    """tests/Test.cpp:60-77 through the engine: cosine -> spikes of M/2."""
+    for m in (4, 10, 12, 16):
+        M = 1 << m
+        B = 8
+        q = np.arange(M)
+        x = np.empty((B, M), np.complex64)
+        expect = np.zeros((B, M), np.complex128)
+        for b in range(B):
+            eff = ((1 + b) % (M // 2 - 1)) + 1
+            x[b] = np.cos(2 * np.pi * (eff * q) / M).astype(np.float32)
+            expect[b, eff] += M / 2
+            expect[b, M - eff] += M / 2
+        y, _ = run(engine, x, -1)
+        assert (np.abs(y - expect) ** 2).max() < 1e-3 * M
+
+
+@pytest.mark.parametrize("logn", [10, 12, 14, 16, 20, 24])
+def test_full_size_sweep_properties(engine, logn):
+    """Sweep configuration (N * batch = 2^27, 1 GiB): round trip, Parseval and
+    oracle spot checks of the first and last transform."""
+    import torch
+    n = 1 << logn
+    batch = (1 << 27) // n
+    g = torch.Generator(device="cuda").manual_seed(2)
+    x = (torch.rand((batch, n, 2), device="cuda", generator=g) * 2 - 1).contiguous()
+    xc = torch.view_as_complex(x)
+    fwd = engine.Plan(n, batch, -1)
+    bwd = engine.Plan(n, batch, +1)
+    y = fwd.execute(xc)
+    z = bwd.execute(y)
+    torch.cuda.synchronize()
+    rt = ((z / n - xc).abs().double() ** 2).sum(-1).sqrt() / (xc.abs().double() ** 2).sum(-1).sqrt()
+    assert rt.max().item() < 2 * tol(n)
+    px = (xc.abs().double() ** 2).sum(-1) * n
+    py = (y.abs().double() ** 2).sum(-1)
+    assert ((py - px).abs() / px).max().item() < 1e-5
+    for b in (0, batch - 1):
+        xb = xc[b].cpu().numpy()[None, :]
+        assert oracle.rel_l2(y[b].cpu().numpy()[None, :], oracle.fft(xb, -1)).max() < tol(n)
+    del x, xc, y, z
+
+
+def test_execute_host_matches_device(engine):
+    import torch
+    for n, batch in ((4096, 64), (1 << 16, 40), (1 << 20, 3)):
+        x = uniform_c64((batch, n), n)
+        p = engine.Plan(n, batch, -1)
+        yd = p.execute(torch.from_numpy(x).cuda()).cpu().numpy()
+        xh = torch.from_numpy(x).pin_memory().numpy()
+        yh = torch.empty((batch, n), dtype=torch.complex64).pin_memory().numpy()
+        p.execute_host(xh, yh)
+        assert np.array_equal(yh, yd)
+        yp = np.zeros_like(x)  # pageable output
+        p.execute_host(x, yp)
+        assert np.array_equal(yp, yd)
+
+
+def test_non_default_stream(engine):
+    import torch
+    x = uniform_c64((16, 1 << 15), 3)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        xd = torch.from_numpy(x).cuda()
+        p = engine.Plan(1 << 15, 16, -1)
+        yd = p.execute(xd, stream=s)
+    s.synchronize()
+    assert oracle.rel_l2(yd.cpu().numpy(), oracle.fft(x, -1)).max() < 2e-6
+
+
+def test_errors(engine):
+    import torch
+    from estl_gb300 import EstlError
+    with pytest.raises(EstlError) as e:
+        engine.Plan(12, 1)
+    assert e.value.name == "ESTL_UNSUPPORTED_SIZE"
+    with pytest.raises(EstlError) as e:
+        engine.Plan(1 << 25, 1)
+    assert e.value.name == "ESTL_UNSUPPORTED_SIZE"
+    with pytest.raises(EstlError) as e:
+        engine.Plan(16, 0)
+    assert e.value.name == "ESTL_INVALID_ARG"
+    p = engine.Plan(16, 4)
+    x = torch.zeros(64, dtype=torch.complex64, device="cuda")
+    with pytest.raises(EstlError):
+        p.execute_ptr(x.data_ptr(), x.data_ptr())  # in-place
+    with pytest.raises(EstlError):
+        p.execute_ptr(x.data_ptr() + 4, x.data_ptr() + 256)  # misaligned
+    assert engine.max_batch(4096) > 1000
+
+
+def test_autotune_keeps_results(engine, tmp_path, monkeypatch):
+    import torch
+    monkeypatch.setenv("ESTL_TUNE_CACHE", str(tmp_path / "tune.jsonl"))
+    n, batch = 1 << 16, 64
+    res = engine.autotune(n, batch, iters=3)
+    assert res["candidates"] > 1 and res["best_ms"] > 0
+    assert (tmp_path / "tune.jsonl").exists()
+    x = uniform_c64((batch, n), 5)
+    y = engine.Plan(n, batch, -1).execute(torch.from_numpy(x).cuda()).cpu().numpy()
+    assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < 2e-6
