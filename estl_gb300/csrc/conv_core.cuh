@@ -1,0 +1,321 @@
+// conv_core.cuh — FFT convolution tile kernels (real signal * real filter).
+//
+// Reference: Convolution2D_FFT::convolve (Convolution.h:95-154): zero-pad both
+// operands to nextPowerOf2(W + K - 1) (:89-97), forward FFT of both (:122-123),
+// pointwise product (or product with the conjugate for correlation,
+// :125-137), inverse FFT (:139), scale 1/(W*H*K^[0]) and crop (:141-148).
+// Restated here in 1D for a batch of independent requests, with
+//  * the filter spectrum computed once per filter and pre-scaled by 1/N
+//    (plain linear convolution) or 1/(N * sum h) with the kernel-centring
+//    shift (reference-compatible mode), conjugated for correlation;
+//  * the inverse transform taken as conj(FFT(conj(Y))) so that it reuses the
+//    forward register layout, and the real part of conj(z) is Re(z), so the
+//    final conjugation disappears;
+//  * N <= 2^14: one kernel per tile of requests: load padded real signal,
+//    forward FFT, multiply, second FFT, store real part — one HBM read of the
+//    signal and of the spectrum, one HBM write of the output;
+//  * N > 2^14: four-step with the spectrum kept in the row-pass order
+//    Hp[k2*N1 + k1] = H[k2 + N2*k1] so that the multiply, the inverse row DFT
+//    and the forward row DFT fuse into one kernel (3 kernels in total).
+#pragma once
+#include "fft_core.cuh"
+
+namespace estl {
+
+// One request (or one filter) inside a launch.  Offsets are element offsets
+// into the packed arrays of the launch.
+struct ConvRow {
+  long long sig_off;   // real input (signal, or filter for the spectrum kernels)
+  long long spec_off;  // complex filter spectrum (read by conv kernels, written by spectrum kernels)
+  long long out_off;   // real output
+  int sig_len;         // valid input samples; the rest of the N-point row is zero
+  int out_len;         // output samples written
+  int out_shift;       // first sample of the circular result that is written
+  float scale;         // spectrum kernels: multiplies the spectrum (1/N, or 1/(N*sum h))
+  float conj;          // spectrum kernels: -1 stores conj(H) (correlation), +1 H
+  int dc_norm;         // conv kernels: divide the output by N * spectrum[0] (= sum of the
+                       // filter): the 1/K^[0] normalisation of Convolution.h:141-143
+};
+
+struct ConvArgs {
+  Ptr<const ConvRow> rows;
+  long long nrows;
+  Ptr<const float> sig;
+  Ptr<const cf32> spec;
+  Ptr<cf32> spec_out;
+  Ptr<float> out;
+  Ptr<cf32> s1;        // four-step scratch: N per row
+  Ptr<cf32> s2;        // four-step scratch: N per row
+  Ptr<const cf32> bank;
+  int logn;
+};
+
+ESTL_HD cf32 cconj(cf32 v) { return {v.x, -v.y}; }
+
+// 1 / (N * spectrum DC) when the row asks for the reference's DC
+// normalisation, else 1 (the stored spectrum already carries 1/N).
+ESTL_HD float dc_factor(const ConvArgs& a, const ConvRow& r) {
+  if (!r.dc_norm) return 1.f;
+  const float dc = ldg(a.spec, r.spec_off).x;
+  return 1.f / ((float)(1 << a.logn) * dc);
+}
+
+// ---------------------------------------------------------------------------
+// N <= 2^14: whole requests in one CTA (C requests per CTA)
+// ---------------------------------------------------------------------------
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvSingleKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static_assert(NT <= 1024, "too many threads");
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+
+  ESTL_HD static void load_real(cf32 (&v)[TL::E], const ConvArgs& a, const ConvRow& r, int t) {
+    const Ptr<const float> s = a.sig.sub(r.sig_off, r.sig_len);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int pos = t + TL::T * j;
+      v[j] = cf32{pos < r.sig_len ? s[pos] : 0.f, 0.f};
+    }
+  }
+
+  // mode 0: convolution (signal -> real output); mode 1: filter -> spectrum
+  template <int MODE>
+  ESTL_HD static void run_mode(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const long long ri = cta * C + c;
+    const bool valid = ri < a.nrows;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    ConvRow r{};
+    if (valid) r = a.rows[ri];
+    cf32 v[TL::E];
+    if (valid) {
+      load_real(v, a, r, t);
+    } else {
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    if constexpr (MODE == 1) {
+      if (valid) {
+        const Ptr<cf32> o = a.spec_out.sub(r.spec_off, TL::M);
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) o[t + TL::T * j] = cf32{v[j].x * r.scale, v[j].y * r.scale * r.conj};
+      }
+    } else {
+      if (valid) {
+        const Ptr<const cf32> h = a.spec.sub(r.spec_off, TL::M);
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
+      }
+      run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+      if (valid) {
+        const Ptr<float> o = a.out.sub(r.out_off, r.out_len);
+        const float g = dc_factor(a, r);
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) {
+          const int m = t + TL::T * j - r.out_shift;
+          if (m >= 0 && m < r.out_len) o[m] = v[j].x * g;
+        }
+      }
+    }
+  }
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) { run_mode<0>(a, cta, tid, sm); }
+};
+
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC> {
+  using B = ConvSingleKernel<LOGM, LOGE, LOGR, LOGC>;
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) {
+    B::template run_mode<1>(a, cta, tid, sm);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// N > 2^14: four-step, N = N1 * N2, x[n1 + N1 n2]
+// ---------------------------------------------------------------------------
+// A: column pass over the zero-padded real input of row f: C adjacent
+// columns n1, N2-point DFTs, times w_N^{n1 k2}, to s1[f*N + k2*N1 + n1].
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvColKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
+  static_assert(NT <= 1024, "too many threads");
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int c = tid & (C - 1);
+    const int t = tid >> LOGC;
+    const int logn1 = a.logn - LOGM;
+    const int N = 1 << a.logn, N1 = 1 << logn1;
+    const int nblk = N1 >> LOGC;
+    const long long f = cta / nblk;
+    const int n1 = (int)(cta - f * nblk) * C + c;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<const float> s = a.sig.sub(r.sig_off, r.sig_len);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n = n1 + ((t + TL::T * j) << logn1);
+      v[j] = cf32{n < r.sig_len ? s[n] : 0.f, 0.f};
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    const Ptr<cf32> o = a.s1.sub(f * N, N);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k2 = t + TL::T * j;
+      o[(k2 << logn1) + n1] = cmul(v[j], twiddle_n(a.bank, a.logn, n1 * k2));
+    }
+  }
+};
+
+// B (spectrum): row pass of the filter: row k2 of s1 -> N1-point DFT ->
+// Hp[k2*N1 + k1] = scale * H[k2 + N2 k1] (conjugated for correlation), stored
+// unit-stride in the permuted order the convolution kernels read.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct SpecRowKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static_assert(NT <= 1024, "too many threads");
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int N = 1 << a.logn;
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = cta / nblk;
+    const int k2 = (int)(cta - f * nblk) * C + c;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> s1 = a.s1.sub(f * N + (long long)k2 * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    const Ptr<cf32> o = a.spec_out.sub(r.spec_off + (long long)k2 * TL::M, TL::M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) o[t + TL::T * j] = cf32{v[j].x * r.scale, v[j].y * r.scale * r.conj};
+  }
+};
+
+// B (convolution): row k2 of s1 -> N1-point DFT (X[k2 + N2 k1]) -> times
+// Hp -> conj -> N1-point DFT over k1 (V[k2][n1]) -> times w_N^{k2 n1} ->
+// s2[f*N + n1*N2 + k2], stored through shared memory in runs of C rows.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvMidKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, C);
+  static constexpr int SMEM_ELEMS = C * CS;
+  static_assert(NT <= 1024, "too many threads");
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int N = 1 << a.logn;
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = cta / nblk;
+    const int k2_0 = (int)(cta - f * nblk) * C;
+    const int k2 = k2_0 + c;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Sidx sidx{};
+    const Ptr<cf32> s1 = a.s1.sub(f * N + (long long)k2 * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    const Ptr<const cf32> h = a.spec.sub(r.spec_off + (long long)k2 * TL::M, TL::M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t + TL::T * j;
+      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logn, k2 * n1));
+    }
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const Ptr<cf32> o = a.s2.sub(f * N, N);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t2 + TL::T * j;
+      o[(n1 << logn2) + k2_0 + c2] = sm[sidx(c2, n1)];
+    }
+  }
+};
+
+// C: row n1 of s2 (N2 contiguous values over k2) -> N2-point DFT over k2 ->
+// conj(result)[n1 + N1 n2] -> real part, staged through shared memory and
+// stored in runs of C columns, cropped to [out_shift, out_shift + out_len).
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvOutKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, C);
+  static constexpr int SMEM_ELEMS = C * CS;
+  static_assert(NT <= 1024, "too many threads");
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int N = 1 << a.logn;
+    const int logn1 = a.logn - LOGM;
+    const int nblk = 1 << (logn1 - LOGC);
+    const long long f = cta / nblk;
+    const int n1_0 = (int)(cta - f * nblk) * C;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Sidx sidx{};
+    const Ptr<cf32> s2 = a.s2.sub(f * N + (long long)(n1_0 + c) * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s2[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const Ptr<float> o = a.out.sub(r.out_off, r.out_len);
+    const float g = dc_factor(a, r);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n2 = t2 + TL::T * j;
+      const int m = n1_0 + c2 + (n2 << logn1) - r.out_shift;
+      const float val = sm[sidx(c2, n2)].x;
+      if (m >= 0 && m < r.out_len) o[m] = val * g;
+    }
+  }
+};
+
+}  // namespace estl

@@ -1,0 +1,126 @@
+// conv_plan.cpp — see conv_plan.h.
+#include "conv_plan.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <map>
+
+namespace estl {
+
+namespace {
+
+// Rows/columns per CTA of the instantiated convolution kernels (conv_list.inc).
+int single_logc(int logm) {
+  static const int c[15] = {0, 8, 8, 8, 8, 7, 6, 5, 4, 3, 2, 1, 0, 0, 0};
+  return c[logm];
+}
+int four_step_logc(int logm) {
+  switch (logm) {
+    case 7: return 5;
+    case 8: return 4;
+    case 9: return 3;
+    case 10: return 3;
+    default: return 2;
+  }
+}
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int conv_logn(long long signal_len, long long filter_len) {
+  long long len = signal_len + filter_len - 1;
+  int l = 1;  // N >= 2 keeps every request on a tile kernel
+  while ((1LL << l) < len) l++;
+  return l;
+}
+
+long long conv_out_len(long long signal_len, long long filter_len, int flags) {
+  return (flags & CONV_REFERENCE_COMPAT) ? signal_len : signal_len + filter_len - 1;
+}
+
+bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err) {
+  ConvLayout L;
+  if (count < 0 || (count > 0 && !reqs)) {
+    if (err) *err = "invalid request array";
+    return false;
+  }
+  std::map<int, std::vector<int>> buckets;  // log2 N -> request indices
+  for (int i = 0; i < count; ++i) {
+    const ConvReq& q = reqs[i];
+    if (q.signal_len < 1 || q.filter_len < 1 || q.sig_off < 0 || q.filt_off < 0 || q.out_off < 0) {
+      if (err) *err = "request " + std::to_string(i) + ": lengths must be >= 1 and offsets >= 0";
+      return false;
+    }
+    int logn = conv_logn(q.signal_len, q.filter_len);
+    if (logn > kConvMaxLogN) {
+      if (err) *err = "request " + std::to_string(i) + ": padded length exceeds 2^" + std::to_string(kConvMaxLogN);
+      return false;
+    }
+    buckets[logn].push_back(i);
+    L.out_elems = std::max(L.out_elems, q.out_off + conv_out_len(q.signal_len, q.filter_len, flags));
+  }
+  long long spec = 0, scratch = 0;
+  for (auto& kv : buckets) {
+    const int logn = kv.first;
+    const long long N = 1LL << logn;
+    const long long rb = (long long)L.sig_rows.size();
+    const long long cnt = (long long)kv.second.size();
+    for (int i : kv.second) {
+      const ConvReq& q = reqs[i];
+      ConvRow f{}, s{};
+      f.sig_off = q.filt_off;
+      f.sig_len = (int)q.filter_len;
+      f.spec_off = spec;
+      f.scale = 1.0f / (float)N;
+      f.conj = (flags & CONV_CORRELATE) ? -1.f : 1.f;
+      s.sig_off = q.sig_off;
+      s.sig_len = (int)q.signal_len;
+      s.spec_off = spec;
+      s.out_off = q.out_off;
+      s.out_len = (int)conv_out_len(q.signal_len, q.filter_len, flags);
+      s.out_shift = (flags & CONV_REFERENCE_COMPAT) ? (int)((q.filter_len + 1) / 2) : 0;
+      s.dc_norm = (flags & CONV_REFERENCE_COMPAT) ? 1 : 0;
+      s.scale = 1.f;
+      s.conj = 1.f;
+      L.filt_rows.push_back(f);
+      L.sig_rows.push_back(s);
+      spec += N;
+    }
+    if (logn <= kSingleMaxLog) {
+      const int lc = single_logc(logn), le = std::min(4, logn);
+      const long long grid = (cnt + (1LL << lc) - 1) >> lc;
+      L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
+      L.launches.push_back(ConvLaunch{CK_CONV_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
+    } else {
+      const int logn2 = logn / 2, logn1 = logn - logn2;
+      const int cc = four_step_logc(logn2), cr = four_step_logc(logn1);
+      const long long s_off = scratch;
+      L.launches.push_back(ConvLaunch{CK_COL_FILTER, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_SPEC_ROW, logn1, 4, 4, cr, cnt << (logn2 - cr), logn, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_COL_SIGNAL, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_MID, logn1, 4, 4, cr, cnt << (logn2 - cr), logn, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_OUT, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
+      scratch += cnt * N;
+    }
+  }
+  L.buckets = (int)buckets.size();
+  L.spec_elems = spec;
+  L.scratch_elems = scratch;
+  size_t off = 0;
+  L.off_filt_rows = off;
+  off = align256(off + L.filt_rows.size() * sizeof(ConvRow));
+  L.off_sig_rows = off;
+  off = align256(off + L.sig_rows.size() * sizeof(ConvRow));
+  L.off_spec = off;
+  off = align256(off + (size_t)spec * sizeof(cf32));
+  L.off_s1 = off;
+  off = align256(off + (size_t)scratch * sizeof(cf32));
+  L.off_s2 = off;
+  off = align256(off + (size_t)scratch * sizeof(cf32));
+  L.workspace_bytes = off;
+  *out = std::move(L);
+  return true;
+}
+
+}  // namespace estl

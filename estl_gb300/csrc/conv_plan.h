@@ -1,0 +1,63 @@
+// conv_plan.h — host-side layout of a batch of FFT convolutions: size
+// buckets, per-request descriptors, workspace offsets and the launch list.
+// Pure C++ so that the host emulator runs the same launch list as the GPU.
+//
+// Reference: Convolution2D_FFT::convolve (Convolution.h:95-154), restated in
+// 1D for many independent requests.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "conv_core.cuh"
+
+namespace estl {
+
+enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2 };
+
+// One convolution request: offsets (in floats) into the caller's packed
+// signal / filter / output arrays.
+struct ConvReq {
+  long long signal_len, filter_len;
+  long long sig_off, filt_off, out_off;
+};
+
+enum ConvLaunchKind {
+  CK_SPEC_SINGLE = 0,  // filter -> spectrum, N <= 2^14
+  CK_CONV_SINGLE = 1,  // signal -> output, N <= 2^14 (fused)
+  CK_COL_FILTER = 2,   // four-step column pass of the filters
+  CK_SPEC_ROW = 3,     // four-step row pass of the filters -> permuted spectrum
+  CK_COL_SIGNAL = 4,   // four-step column pass of the signals
+  CK_MID = 5,          // row DFT, multiply, row DFT, twiddle
+  CK_OUT = 6,          // column DFT -> real output
+};
+
+struct ConvLaunch {
+  int kind;
+  int logm, loge, logr, logc;
+  long long grid;
+  int logn;
+  long long row_begin, row_count;  // rows in the filter (CK_SPEC_*, CK_COL_FILTER) or signal row array
+  long long s_off;                 // element offset of this bucket's scratch in s1 / s2
+};
+
+struct ConvLayout {
+  std::vector<ConvRow> filt_rows, sig_rows;
+  std::vector<ConvLaunch> launches;
+  long long spec_elems = 0;     // complex
+  long long scratch_elems = 0;  // complex, each of s1 and s2
+  long long out_elems = 0;      // floats written (max out_off + out_len)
+  // workspace byte offsets (256-byte aligned regions)
+  size_t off_filt_rows = 0, off_sig_rows = 0, off_spec = 0, off_s1 = 0, off_s2 = 0, workspace_bytes = 0;
+  int buckets = 0;
+};
+
+constexpr int kConvMaxLogN = 22;
+
+// Output length of one request (signal_len + filter_len - 1, or signal_len
+// in reference-compatible mode).
+long long conv_out_len(long long signal_len, long long filter_len, int flags);
+int conv_logn(long long signal_len, long long filter_len);
+
+bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err);
+
+}  // namespace estl

@@ -329,6 +329,13 @@ struct Tile {
   static constexpr int MP = M + (M >> 4);
 };
 
+// Stride (in complex elements) between the shared-memory rows of a tile of
+// C rows.  A half-warp of 8-byte accesses covers all 32 banks once when its
+// 16 lanes hit distinct 16-element residues.  Row-major accesses by T >= 16
+// lanes per row never span rows; the column-fastest store remap (lanes c
+// fastest, then 16/C positions per row) needs stride = 16/C (mod 16).
+ESTL_CX int row_stride(int mp, int c) { return c >= 16 ? (mp | 1) : ((mp + 15) / 16) * 16 + 16 / c; }
+
 // Runs passes p..P-1 over the tile.  Between passes each thread writes its
 // outputs to shared memory at their Stockham positions and re-reads its next
 // inputs at t + T*j.  SIDX maps (column c, position m) to a shared index.
@@ -350,6 +357,19 @@ ESTL_HD void run_passes(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, con
 }
 
 // ---------------------------------------------------------------------------
+// Blocks per SM requested from the compiler: 16 elements per thread are built
+// for 1024 resident threads per SM (64 registers), 32 elements per thread for
+// 512 (128 registers).
+ESTL_CX int min_blocks(int nt, int e) { return nt * e >= 16384 ? 1 : 16384 / (nt * e); }
+
+// Keeps the compiler from hoisting every iteration's table loads to the top
+// of an unrolled epilogue (which costs 2 registers per load in flight).
+ESTL_HD void schedule_fence() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("" ::: "memory");
+#endif
+}
+
 // Launch parameters shared by all tile kernels.
 // ---------------------------------------------------------------------------
 struct TileArgs {
@@ -371,7 +391,7 @@ struct SingleKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = (TL::MP | 1);  // odd row stride
+  static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
   static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
   static_assert(NT <= 1024, "too many threads");
 
@@ -441,6 +461,7 @@ struct ColKernel {
       const int k2 = t + TL::T * j;
       cf32 w = twiddle_n(a.bank, a.logn, n1 * k2);
       out[(k2 << logn1) + n1] = cmul(v[j], w);
+      if ((j & 3) == 3) schedule_fence();
     }
   }
 };
@@ -454,7 +475,7 @@ struct RowKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = (TL::MP | 1);
+  static constexpr int CS = row_stride(TL::MP, C);
   static constexpr int SMEM_ELEMS = C * CS;
   static_assert(NT <= 1024, "too many threads");
   static_assert(NT % C == 0 && (NT / C) * TL::E >= TL::M, "store remap must cover the tile");

@@ -18,7 +18,7 @@ struct KernelDesc {
 };
 
 template <class K>
-__global__ void __launch_bounds__(K::NT) tile_kernel(TileArgs a) {
+__global__ void __launch_bounds__(K::NT, min_blocks(K::NT, K::TL::E)) tile_kernel(TileArgs a) {
   extern __shared__ float2 estl_smem[];
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
 }

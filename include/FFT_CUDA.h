@@ -1,0 +1,180 @@
+/* FFT_CUDA.h — ESTL backend plugin for the GB300 FFT engine.
+ *
+ * FFT_CUDA<D> is an FFT<D> (FFT.h:19-36) like FFT_FFTW3<D> (FFT_FFTW3.h:16-34)
+ * and FFT_OpenCL_Contiguous<D> (FFT_OpenCL_Contiguous.h:26-192), so it drops
+ * into every place the reference creates a backend through a factory:
+ *
+ *   factories.push_back(new FFTFactorySpecific<FFT_CUDA<T> >());   // tests/Test.cpp:196-200
+ *   FFTFactory<S>* f = new FFTFactorySpecific<FFT_CUDA<S> >();      // Convolution.h:101
+ *
+ * It uses the interleaved host layout of FFT_FFTW3
+ * (SplitInterleavedDataInterface(n*batch, false), FFT_FFTW3.h:24), pins those
+ * host arrays once, and executes through the C ABI (estl_cuda.h): copy in,
+ * all passes on the device, copy out, with the copies and the transform
+ * pipelined.  Backward transforms are exact for every transform of the batch.
+ *
+ * The per-kernel timers keep the member names of OpenCLAlgorithm
+ * (uOpenCL.h:281-282, 339-340) on the GpuAlgorithm mix-in, so a driver written
+ * like tests/Test.cpp:56,86-99 reads them after dynamic_cast<GpuAlgorithm*>.
+ *
+ * Errors: C ABI status codes become EstlException (the reference throws
+ * CLException from xCLErr, uOpenCL.h:21-55).
+ *
+ * Include after ESTL's FFT.h (or an interface-compatible copy of it).
+ */
+#ifndef FFT_CUDA_H
+#define FFT_CUDA_H
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "FFT.h"
+#include "estl_cuda.h"
+
+class EstlException : public std::exception {
+ public:
+  EstlException(estl_status s, const std::string& where)
+      : status(s), msg(std::string("[") + estl_status_string(s) + "] " + where + ": " + estl_last_error()) {}
+  virtual const char* what() const throw() { return msg.c_str(); }
+  virtual ~EstlException() throw() {}
+  estl_status status;
+
+ private:
+  std::string msg;
+};
+
+inline void estlCheck(estl_status s, const char* where) {
+  if (s != ESTL_OK) throw EstlException(s, where);
+}
+
+/* Default timer with the interface of ESTL's Timer (tests/Timer.h:47-116);
+ * ESTL's own Timer is used instead when tests/Timer.h was included first. */
+class EstlHostTimer {
+ public:
+  EstlHostTimer() : totalTime(0), runs(0) {}
+  void addRun(double t) {
+    totalTime += t;
+    runs++;
+  }
+  double getTotalTime() { return totalTime; }
+  double getAverageTime() { return runs ? totalTime / runs : 0; }
+  int getRuns() { return runs; }
+
+ private:
+  double totalTime;
+  int runs;
+};
+
+#ifdef TIMER_H
+typedef Timer EstlTimerType;
+#else
+typedef EstlHostTimer EstlTimerType;
+#endif
+
+/* Instrumentation contract of OpenCLAlgorithm (uOpenCL.h:275-348). */
+class GpuAlgorithm {
+ public:
+  EstlTimerType *timerComputation, *timerTotal;
+  std::vector<EstlTimerType> kernelTimers;
+  GpuAlgorithm() : timerComputation(NULL), timerTotal(NULL) {}
+  virtual double getTotalComputationFlops(int kernel) { return 0; }
+  virtual std::string getKernelInfo(int kernel) { return ""; }
+  virtual ~GpuAlgorithm() {}
+
+  static void ensureInit() {
+    const char* dev = getenv("ESTL_DEVICE");
+    estlCheck(estl_init(dev ? atoi(dev) : 0, 0), "estl_init");
+  }
+};
+
+template <class D>
+class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
+ public:
+  typedef SplitInterleavedDataInterface<D> DataInterfaceType;
+
+  static streng getName() { return "GB300 CUDA FFT"; }
+
+  /* FFT_OpenCL_Contiguous::getMaxBatchSize (FFT_OpenCL_Contiguous.h:43-44) against the HBM budget. */
+  static int getMaxBatchSize(int n) {
+    ensureInit();
+    int64_t b = estl_max_batch(n);
+    return b > 2147483647 ? 2147483647 : (int)b;
+  }
+
+  FFT_CUDA(int n, bool forward = true, int iBatchCount = 1)
+      : FFT<D>(n, iBatchCount), plan(NULL), registered(false) {
+    typedef char only_float_is_supported[(sizeof(D) == sizeof(float)) ? 1 : -1];
+    (void)sizeof(only_float_is_supported);
+    this->dataInterface = arrays = new DataInterfaceType(this->batchCount * this->size, false);
+    ensureInit();
+    estlCheck(estl_plan_create(n, iBatchCount, forward ? ESTL_FORWARD : ESTL_BACKWARD, ESTL_PREC_FP32, &plan),
+              "estl_plan_create");
+    estlCheck(estl_plan_set_profiling(plan, 1), "estl_plan_set_profiling");
+    char desc[1024];
+    estl_plan_describe(plan, desc, sizeof desc);
+    describe = desc;
+    kinds.clear();
+    if (describe.find("\"single\"") != std::string::npos) kinds.push_back(0);
+    if (describe.find("\"col\"") != std::string::npos) kinds.push_back(1);
+    if (describe.find("\"row\"") != std::string::npos) kinds.push_back(2);
+    if (describe.find("\"copy\"") != std::string::npos) kinds.push_back(3);
+    kernelTimers.resize(kinds.size());
+    const size_t bytes = sizeof(D) * 2 * (size_t)this->size * this->batchCount;
+    registered = estl_host_register(arrays->in->getData(), bytes) == ESTL_OK &&
+                 estl_host_register(arrays->out->getData(), bytes) == ESTL_OK;
+    for (int k = 0; k < 4; ++k) lastMs[k] = 0;
+  }
+
+  virtual double getTotalComputationFlops(int kernel) {
+    double lg = log((double)this->size) / log(2.0), part = lg;
+    int logn = (int)(lg + 0.5);
+    if (kinds.size() == 2) part = (kernel == 0) ? (double)(logn / 2) : (double)(logn - logn / 2);
+    return 5.0 * this->size * part * this->batchCount;
+  }
+
+  virtual std::string getKernelInfo(int kernel) {
+    static const char* names[] = {"tile", "column", "row", "copy"};
+    return (kernel >= 0 && kernel < (int)kinds.size()) ? names[kinds[kernel]] : "";
+  }
+
+  /* FFT<D>::execute: the result is in the data interface's output array. */
+  virtual void execute() {
+    estlCheck(estl_execute_host(plan, arrays->in->getData(), arrays->out->getData()), "estl_execute_host");
+    int64_t launches[4];
+    double ms[4], bytes[4];
+    estlCheck(estl_plan_kernel_stats(plan, launches, ms, bytes), "estl_plan_kernel_stats");
+    double total = 0;
+    for (size_t i = 0; i < kinds.size(); ++i) {
+      double d = ms[kinds[i]] - lastMs[kinds[i]];
+      kernelTimers[i].addRun(1e-3 * d);
+      total += d;
+    }
+    for (int k = 0; k < 4; ++k) lastMs[k] = ms[k];
+    if (timerComputation) timerComputation->addRun(1e-3 * total);
+  }
+
+  const std::string& planDescription() const { return describe; }
+
+  virtual ~FFT_CUDA() {
+    if (registered) {
+      estl_host_unregister(arrays->in->getData());
+      estl_host_unregister(arrays->out->getData());
+    }
+    if (plan) estl_plan_destroy(plan);
+  }
+
+ private:
+  DataInterfaceType* arrays;
+  estl_plan plan;
+  bool registered;
+  std::string describe;
+  std::vector<int> kinds;
+  double lastMs[4];
+};
+
+#endif  // FFT_CUDA_H
