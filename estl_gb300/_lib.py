@@ -60,6 +60,7 @@ SIGNATURES = {
     "estl_host_unregister": (_INT, [_P]),
     "estl_autotune": (_INT, [_I64, _I64, _INT, ctypes.c_char_p, _SZ]),
     "estl_memory_usage": (_INT, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
+    "estl_execute_noalloc": (_INT, [_I64, _I64, _INT, _P, _P, _P]),
 }
 
 

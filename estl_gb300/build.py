@@ -22,6 +22,7 @@ SOURCES = [
     "planner.cpp",
     "tuner.cu",
     "api.cu",
+    "noalloc.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -129,6 +129,30 @@ estl_status estl_host_unregister(void* ptr);
  * radix is fixed at 16 (FFT_OpenCL_Contiguous.h:55). */
 estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* result_json, size_t len);
 
+/* Allocation-free FFT for callers that cannot allocate device memory: plugins
+ * whose host owns all device memory through its own allocator or pool,
+ * latency-critical loops where cudaMalloc/cudaFree would synchronise the
+ * device, and hosts that forbid device allocation in plugin calls.  This
+ * entry point has no counterpart in the reference.
+ *
+ * Runs `batch` transforms of length n with the four-step column and row
+ * kernels of estl_execute, but keeps their scratch in one fixed device array
+ * of 2^22 complex64 (32 MiB) and uses its own 4.4 MB twiddle table; every GPU
+ * that loads this library holds both until the process exits.  Needs neither
+ * estl_init nor a plan and allocates nothing (no cudaMalloc, cudaFree or
+ * allocating library call); the caller passes the input and output buffers
+ * (n*batch complex64 each, distinct, 8-byte aligned) and a stream.
+ *  - n must be a power of two in [2^14, 2^22]; other sizes are rejected with
+ *    ESTL_UNSUPPORTED_SIZE (estl_execute handles them).
+ *  - The first call on a device resolves the arrays' device addresses and
+ *    fills the twiddle table, synchronising `stream`; make that first call
+ *    before any stream capture.
+ *  - All calls share the array and leave their last contents in it; nothing
+ *    in it needs to start at zero.  Calls whose work overlaps on the GPU
+ *    (unordered streams, or several threads) race on it: order them. */
+estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direction, const void* d_in, void* d_out,
+                                 void* stream);
+
 /* Bytes currently held by the engine on the device (plans, scratch, staging,
  * twiddle bank) and the budget set at init. */
 estl_status estl_memory_usage(size_t* used_bytes, size_t* budget_bytes);
