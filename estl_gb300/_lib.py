@@ -61,7 +61,30 @@ SIGNATURES = {
     "estl_autotune": (_INT, [_I64, _I64, _INT, ctypes.c_char_p, _SZ]),
     "estl_memory_usage": (_INT, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
     "estl_execute_noalloc": (_INT, [_I64, _I64, _INT, _P, _P, _P]),
+    "estl_conv_output_length": (_I64, [_I64, _I64, _INT]),
+    "estl_conv_workspace_size": (_INT, [_P, _I64, _INT, ctypes.POINTER(_SZ)]),
+    "estl_conv_execute": (_INT, [_P, _I64, _INT, _P, _P, _P, _P, _SZ, _P]),
+    "estl_conv_plan_create": (_INT, [_I64, _I64, _I64, _INT, ctypes.POINTER(_P)]),
+    "estl_conv_plan_set_filter": (_INT, [_P, _P, _P]),
+    "estl_conv_plan_execute": (_INT, [_P, _P, _P, _P]),
+    "estl_conv_plan_launches": (_I64, [_P]),
+    "estl_conv_plan_destroy": (_INT, [_P]),
+    "estl_packed_plan_create": (_INT, [_P, _P, _I64, _INT, _INT, ctypes.POINTER(_P)]),
+    "estl_packed_execute": (_INT, [_P, _P, _P, _P]),
+    "estl_packed_check": (_INT, [_P]),
+    "estl_packed_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
+    "estl_packed_plan_destroy": (_INT, [_P]),
 }
+
+
+class ConvRequest(ctypes.Structure):
+    """estl_conv_request: lengths and float offsets of one convolution."""
+    _fields_ = [("signal_len", ctypes.c_int64), ("filter_len", ctypes.c_int64), ("signal_offset", ctypes.c_int64),
+                ("filter_offset", ctypes.c_int64), ("output_offset", ctypes.c_int64)]
+
+
+CONV_CORRELATE = 1
+CONV_REFERENCE_COMPAT = 2
 
 
 def lib():

@@ -23,6 +23,10 @@ SOURCES = [
     "tuner.cu",
     "api.cu",
     "noalloc.cu",
+    "conv_plan.cpp",
+    "conv.cu",
+    "packed_plan.cpp",
+    "packed.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

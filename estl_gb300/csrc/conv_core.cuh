@@ -71,6 +71,7 @@ struct ConvSingleKernel {
   static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
   static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
   static_assert(NT <= 1024, "too many threads");
+  static constexpr int MINB = min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -150,6 +151,7 @@ struct ConvColKernel {
   static constexpr int NT = TL::T * C;
   static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
   static_assert(NT <= 1024, "too many threads");
+  static constexpr int MINB = min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
@@ -192,6 +194,7 @@ struct SpecRowKernel {
   static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
   static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
   static_assert(NT <= 1024, "too many threads");
+  static constexpr int MINB = min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -228,6 +231,8 @@ struct ConvMidKernel {
   static constexpr int CS = row_stride(TL::MP, C);
   static constexpr int SMEM_ELEMS = C * CS;
   static_assert(NT <= 1024, "too many threads");
+  // two DFTs, the spectrum multiply and the twiddle epilogue: allow 128 registers
+  static constexpr int MINB = 1;
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -281,6 +286,7 @@ struct ConvOutKernel {
   static constexpr int CS = row_stride(TL::MP, C);
   static constexpr int SMEM_ELEMS = C * CS;
   static_assert(NT <= 1024, "too many threads");
+  static constexpr int MINB = min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };

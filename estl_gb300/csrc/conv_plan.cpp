@@ -1,6 +1,8 @@
 // conv_plan.cpp — see conv_plan.h.
 #include "conv_plan.h"
 
+#include "planner.h"
+
 #include <algorithm>
 #include <cstdio>
 #include <map>
@@ -39,7 +41,18 @@ long long conv_out_len(long long signal_len, long long filter_len, int flags) {
   return (flags & CONV_REFERENCE_COMPAT) ? signal_len : signal_len + filter_len - 1;
 }
 
-bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err) {
+void conv_extents(const ConvReq* reqs, int count, long long* sig_elems, long long* filt_elems) {
+  long long s = 0, f = 0;
+  for (int i = 0; i < count; ++i) {
+    s = std::max(s, reqs[i].sig_off + reqs[i].signal_len);
+    f = std::max(f, reqs[i].filt_off + reqs[i].filter_len);
+  }
+  *sig_elems = s;
+  *filt_elems = f;
+}
+
+bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err,
+                       bool shared_filter) {
   ConvLayout L;
   if (count < 0 || (count > 0 && !reqs)) {
     if (err) *err = "invalid request array";
@@ -58,6 +71,11 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       return false;
     }
     buckets[logn].push_back(i);
+    if (shared_filter && (q.filter_len != reqs[0].filter_len || q.filt_off != reqs[0].filt_off ||
+                          logn != conv_logn(reqs[0].signal_len, reqs[0].filter_len))) {
+      if (err) *err = "shared-filter batch: every request must use filter 0 and pad to the same length";
+      return false;
+    }
     L.out_elems = std::max(L.out_elems, q.out_off + conv_out_len(q.signal_len, q.filter_len, flags));
   }
   long long spec = 0, scratch = 0;
@@ -66,8 +84,10 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
     const long long N = 1LL << logn;
     const long long rb = (long long)L.sig_rows.size();
     const long long cnt = (long long)kv.second.size();
+    const long long fb = (long long)L.filt_rows.size();
     for (int i : kv.second) {
       const ConvReq& q = reqs[i];
+      const bool new_spectrum = !shared_filter || L.filt_rows.empty();
       ConvRow f{}, s{};
       f.sig_off = q.filt_off;
       f.sig_len = (int)q.filter_len;
@@ -76,28 +96,34 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       f.conj = (flags & CONV_CORRELATE) ? -1.f : 1.f;
       s.sig_off = q.sig_off;
       s.sig_len = (int)q.signal_len;
-      s.spec_off = spec;
+      s.spec_off = new_spectrum ? spec : L.filt_rows[0].spec_off;
       s.out_off = q.out_off;
       s.out_len = (int)conv_out_len(q.signal_len, q.filter_len, flags);
       s.out_shift = (flags & CONV_REFERENCE_COMPAT) ? (int)((q.filter_len + 1) / 2) : 0;
       s.dc_norm = (flags & CONV_REFERENCE_COMPAT) ? 1 : 0;
       s.scale = 1.f;
       s.conj = 1.f;
-      L.filt_rows.push_back(f);
+      if (new_spectrum) {
+        L.filt_rows.push_back(f);
+        spec += N;
+      }
       L.sig_rows.push_back(s);
-      spec += N;
     }
+    const long long fcnt = (long long)L.filt_rows.size() - fb;
     if (logn <= kSingleMaxLog) {
       const int lc = single_logc(logn), le = std::min(4, logn);
       const long long grid = (cnt + (1LL << lc) - 1) >> lc;
-      L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
+      const long long fgrid = (fcnt + (1LL << lc) - 1) >> lc;
+      if (fcnt) L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, fgrid, logn, fb, fcnt, 0});
       L.launches.push_back(ConvLaunch{CK_CONV_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
     } else {
       const int logn2 = logn / 2, logn1 = logn - logn2;
       const int cc = four_step_logc(logn2), cr = four_step_logc(logn1);
       const long long s_off = scratch;
-      L.launches.push_back(ConvLaunch{CK_COL_FILTER, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
-      L.launches.push_back(ConvLaunch{CK_SPEC_ROW, logn1, 4, 4, cr, cnt << (logn2 - cr), logn, rb, cnt, s_off});
+      if (fcnt) {
+        L.launches.push_back(ConvLaunch{CK_COL_FILTER, logn2, 4, 4, cc, fcnt << (logn1 - cc), logn, fb, fcnt, s_off});
+        L.launches.push_back(ConvLaunch{CK_SPEC_ROW, logn1, 4, 4, cr, fcnt << (logn2 - cr), logn, fb, fcnt, s_off});
+      }
       L.launches.push_back(ConvLaunch{CK_COL_SIGNAL, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
       L.launches.push_back(ConvLaunch{CK_MID, logn1, 4, 4, cr, cnt << (logn2 - cr), logn, rb, cnt, s_off});
       L.launches.push_back(ConvLaunch{CK_OUT, logn2, 4, 4, cc, cnt << (logn1 - cc), logn, rb, cnt, s_off});
@@ -105,6 +131,8 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
     }
   }
   L.buckets = (int)buckets.size();
+  for (const ConvLaunch& l : L.launches)
+    L.is_spectrum_launch.push_back(l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW);
   L.spec_elems = spec;
   L.scratch_elems = scratch;
   size_t off = 0;

@@ -49,6 +49,9 @@ struct ConvLayout {
   // workspace byte offsets (256-byte aligned regions)
   size_t off_filt_rows = 0, off_sig_rows = 0, off_spec = 0, off_s1 = 0, off_s2 = 0, workspace_bytes = 0;
   int buckets = 0;
+  // launches that compute spectra come first in each bucket; these counts let
+  // a caller run the spectrum launches once and the convolution launches often
+  std::vector<char> is_spectrum_launch;
 };
 
 constexpr int kConvMaxLogN = 22;
@@ -58,6 +61,12 @@ constexpr int kConvMaxLogN = 22;
 long long conv_out_len(long long signal_len, long long filter_len, int flags);
 int conv_logn(long long signal_len, long long filter_len);
 
-bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err);
+// shared_filter: every request uses the filter of request 0 (one spectrum,
+// computed once); all requests must then pad to the same N.
+bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* out, std::string* err,
+                       bool shared_filter = false);
+
+// Extents (in floats) of the packed signal / filter arrays the requests use.
+void conv_extents(const ConvReq* reqs, int count, long long* sig_elems, long long* filt_elems);
 
 }  // namespace estl

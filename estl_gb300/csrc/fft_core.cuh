@@ -100,6 +100,18 @@ ESTL_HD cf32 ldcs(const Ptr<const cf32>& q, long long i) {
   return q.p[i];
 #endif
 }
+// Load that bypasses L1: data another CTA of the same launch may have
+// written (four-step scratch in the persistent packed kernel).
+ESTL_HD cf32 ldcg(const Ptr<cf32>& q, long long i) {
+  ESTL_CHECK(i, q.n, "global load");
+#if defined(__CUDA_ARCH__)
+  float2 v = __ldcg(reinterpret_cast<const float2*>(q.p) + i);
+  return {v.x, v.y};
+#else
+  return q.p[i];
+#endif
+}
+
 ESTL_HD void stcs(const Ptr<cf32>& q, long long i, cf32 v) {
   ESTL_CHECK(i, q.n, "global store");
 #if defined(__CUDA_ARCH__)
@@ -399,28 +411,36 @@ struct SingleKernel {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
 
-  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+  // One tile: row c of the tile is transform `in` -> `out` (length M each);
+  // rows with valid == false only take part in the barriers.
+  ESTL_HD static void body(const Ptr<const cf32>& in, const Ptr<cf32>& out, bool valid, int tid, cf32* smraw,
+                           const Ptr<const cf32>& bank, float sgn) {
     const int t = tid & (TL::T - 1);
     const int c = tid >> TL::LOGT;
-    const long long row = cta * C + c;
-    const bool valid = row < a.rows;
-    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
     cf32 v[TL::E];
     if (valid) {
-      const Ptr<const cf32> in = a.in.sub(row * TL::M, TL::M);
 #pragma unroll
-      for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, t + TL::T * j), a.sgn);
+      for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, t + TL::T * j), sgn);
     } else {
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
     }
     run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     if (valid) {
-      const Ptr<cf32> out = a.out.sub(row * TL::M, TL::M);
 #pragma unroll
-      for (int j = 0; j < TL::E; ++j) stcs(out, t + TL::T * j, conj_if(v[j], a.sgn));
+      for (int j = 0; j < TL::E; ++j) stcs(out, t + TL::T * j, conj_if(v[j], sgn));
     }
+  }
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int c = tid >> TL::LOGT;
+    const long long row = cta * C + c;
+    const bool valid = row < a.rows;
+    const Ptr<const cf32> in = valid ? a.in.sub(row * TL::M, TL::M) : Ptr<const cf32>{a.in.p, 0};
+    const Ptr<cf32> out = valid ? a.out.sub(row * TL::M, TL::M) : Ptr<cf32>{a.out.p, 0};
+    body(in, out, valid, tid, smraw, a.bank, a.sgn);
   }
 };
 
@@ -440,29 +460,36 @@ struct ColKernel {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
 
-  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+  // Columns n1_0 .. n1_0 + C - 1 of one transform: in = the transform
+  // (N elements), out = its scratch (N elements, S[k2*N1 + n1]).
+  ESTL_HD static void body(const Ptr<const cf32>& in, const Ptr<cf32>& out, int n1_0, int logn, int tid,
+                           cf32* smraw, const Ptr<const cf32>& bank, float sgn) {
     const int c = tid & (C - 1);
     const int t = tid >> LOGC;
-    const int logn1 = a.logn - LOGM;
-    const int N = 1 << a.logn, N1 = 1 << logn1;
-    const int nblk = N1 >> LOGC;
-    const long long f = cta / nblk;
-    const int n1 = (int)(cta - f * nblk) * C + c;
-    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const int logn1 = logn - LOGM;
+    const int n1 = n1_0 + c;
+    const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
-    const Ptr<const cf32> in = a.in.sub(f * N, N);
     cf32 v[TL::E];
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, n1 + ((t + TL::T * j) << logn1)), a.sgn);
+    for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, n1 + ((t + TL::T * j) << logn1)), sgn);
     run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
-    const Ptr<cf32> out = a.out.sub(f * N, N);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int k2 = t + TL::T * j;
-      cf32 w = twiddle_n(a.bank, a.logn, n1 * k2);
+      cf32 w = twiddle_n(bank, logn, n1 * k2);
       out[(k2 << logn1) + n1] = cmul(v[j], w);
       if ((j & 3) == 3) schedule_fence();
     }
+  }
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int logn1 = a.logn - LOGM;
+    const int N = 1 << a.logn;
+    const int nblk = (1 << logn1) >> LOGC;
+    const long long f = cta / nblk;
+    const int n1_0 = (int)(cta - f * nblk) * C;
+    body(a.in.sub(f * N, N), a.out.sub(f * N, N), n1_0, a.logn, tid, smraw, a.bank, a.sgn);
   }
 };
 
@@ -484,21 +511,20 @@ struct RowKernel {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
 
-  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+  // Rows k2_0 .. k2_0 + C - 1 of one transform's scratch `in` (N elements)
+  // -> the transform's output `out` (N elements, X[k2 + N2 k1]).
+  ESTL_HD static void body(const Ptr<cf32>& in, const Ptr<cf32>& out, int k2_0, int logn, int tid, cf32* smraw,
+                           const Ptr<const cf32>& bank, float sgn) {
     const int t = tid & (TL::T - 1);
     const int c = tid >> TL::LOGT;
-    const int N = 1 << a.logn;
-    const int logn2 = a.logn - LOGM;
-    const int nblk = 1 << (logn2 - LOGC);
-    const long long f = cta / nblk;
-    const int k2_0 = (int)(cta - f * nblk) * C;
-    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const int logn2 = logn - LOGM;
+    const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
     const Sidx sidx{};
     cf32 v[TL::E];
-    const Ptr<const cf32> in = a.in.sub(f * N + (long long)(k2_0 + c) * TL::M, TL::M);
+    const Ptr<cf32> row = in.sub((long long)(k2_0 + c) * TL::M, TL::M);
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) v[j] = in[t + TL::T * j];
+    for (int j = 0; j < TL::E; ++j) v[j] = ldcg(row, t + TL::T * j);
     run_passes<TL, 0>(v, t, c, sm, tw, sidx);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
@@ -506,12 +532,23 @@ struct RowKernel {
     const int c2 = tid & (C - 1);
     const int t2 = tid >> LOGC;
     constexpr int T2 = NT / C;  // == TL::T
-    const Ptr<cf32> out = a.out.sub(f * N, N);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int k1 = t2 + T2 * j;
-      stcs(out, k2_0 + c2 + (k1 << logn2), conj_if(sm[sidx(c2, k1)], a.sgn));
+      stcs(out, k2_0 + c2 + (k1 << logn2), conj_if(sm[sidx(c2, k1)], sgn));
     }
+  }
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const int N = 1 << a.logn;
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = cta / nblk;
+    const int k2_0 = (int)(cta - f * nblk) * C;
+    // the scratch written by the column pass is read-only here
+    const Ptr<cf32> in{const_cast<cf32*>(a.in.p) + f * N, N};
+    ESTL_CHECK(f * N + N, a.in.n + 1, "row pass input range");
+    body(in, a.out.sub(f * N, N), k2_0, a.logn, tid, smraw, a.bank, a.sgn);
   }
 };
 

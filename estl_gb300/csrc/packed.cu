@@ -1,0 +1,237 @@
+// packed.cu — uneven batches (packed transforms of mixed lengths): the
+// persistent work-queue kernel, its CUDA graph, and the C ABI.
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "engine.h"
+#include "packed_core.cuh"
+
+namespace estl {
+
+__global__ void __launch_bounds__(kPackedThreads, 3) packed_kernel(PackedArgs a) {
+  extern __shared__ float2 estl_packed_smem[];
+  __shared__ int slot[2];
+  packed_run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_packed_smem), slot);
+}
+
+}  // namespace estl
+
+using namespace estl;
+
+struct estl_packed_plan_s {
+  PackedLayout layout;
+  int direction = ESTL_FORWARD;
+  // device workspace
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  PackedItem* items = nullptr;
+  int* class_list = nullptr;
+  long long* offsets = nullptr;
+  long long* scratch_off = nullptr;
+  int* ncol = nullptr;
+  unsigned int* counters = nullptr;  // [0] work counter, [1..] done per transform
+  int* error = nullptr;
+  cf32* scratch = nullptr;
+  size_t counter_bytes = 0;
+  int grid = 0;  // persistent grid (CTAs)
+  size_t smem = 0;
+  // graph (captured per (in, out) pair)
+  std::mutex mu;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* g_in = nullptr;
+  void* g_out = nullptr;
+  cudaStream_t cap_stream = nullptr;
+};
+
+static size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out, cudaStream_t st) {
+  Engine& E = engine();
+  const PackedLayout& L = p->layout;
+  estl_status s = check_cuda(cudaMemsetAsync(p->counters, 0, p->counter_bytes, st), "cudaMemsetAsync(counters)");
+  if (s != ESTL_OK) return s;
+  for (size_t k = 0; k < L.launch_begin.size(); ++k) {
+    PackedArgs a;
+    a.items = Ptr<const PackedItem>{p->items, (long long)L.items.size()};
+    a.item_base = L.launch_begin[k];
+    a.nitems = L.launch_count[k];
+    a.class_list = Ptr<const int>{p->class_list, (long long)L.class_list.size()};
+    a.offsets = Ptr<const long long>{p->offsets, (long long)L.offsets.size()};
+    a.scratch_off = Ptr<const long long>{p->scratch_off, (long long)L.scratch_off.size()};
+    a.ncol = Ptr<const int>{p->ncol, (long long)L.ncol.size()};
+    a.in = Ptr<const cf32>{in, L.total_elems};
+    a.out = Ptr<cf32>{out, L.total_elems};
+    a.scratch = Ptr<cf32>{p->scratch, L.scratch_elems};
+    a.bank = Ptr<const cf32>{E.bank, kBankSize};
+    a.next = p->counters;
+    a.done = p->counters + 1;
+    a.error = p->error;
+    a.sgn = p->direction == ESTL_FORWARD ? 1.f : -1.f;
+    a.persistent = L.persistent ? 1 : 0;
+    const long long grid = L.persistent ? std::min<long long>(p->grid, L.launch_count[k]) : L.launch_count[k];
+    if (grid < 1 || grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "packed grid of %lld CTAs", grid);
+    packed_kernel<<<(unsigned)grid, kPackedThreads, p->smem, st>>>(a);
+    s = check_cuda(cudaGetLastError(), "packed_kernel launch");
+    if (s != ESTL_OK) return s;
+  }
+  return ESTL_OK;
+}
+
+static void packed_release(estl_packed_plan p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  dev_free(p->ws, p->ws_bytes);
+  delete p;
+}
+
+extern "C" {
+
+estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                    int mode, estl_packed_plan* plan) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan pointer");
+  *plan = nullptr;
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  if (direction != ESTL_FORWARD && direction != ESTL_BACKWARD) return fail(ESTL_INVALID_ARG, "bad direction %d", direction);
+  if (mode != ESTL_PACKED_PERSISTENT && mode != ESTL_PACKED_PER_SIZE) return fail(ESTL_INVALID_ARG, "bad mode %d", mode);
+  std::unique_ptr<estl_packed_plan_s> p(new estl_packed_plan_s);
+  std::string err;
+  if (!build_packed_layout(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
+                           count, mode == ESTL_PACKED_PERSISTENT, &p->layout, &err))
+    return fail(ESTL_INVALID_ARG, "%s", err.c_str());
+  p->direction = direction;
+  const PackedLayout& L = p->layout;
+  // workspace: items | class list | offsets | scratch offsets | ncol | counters | error | scratch
+  size_t off = 0;
+  const size_t o_items = off;
+  off = up256(off + L.items.size() * sizeof(PackedItem));
+  const size_t o_cls = off;
+  off = up256(off + std::max<size_t>(L.class_list.size(), 1) * sizeof(int));
+  const size_t o_off = off;
+  off = up256(off + L.offsets.size() * sizeof(long long));
+  const size_t o_soff = off;
+  off = up256(off + L.scratch_off.size() * sizeof(long long));
+  const size_t o_ncol = off;
+  off = up256(off + L.ncol.size() * sizeof(int));
+  const size_t o_cnt = off;
+  p->counter_bytes = (1 + L.offsets.size()) * sizeof(unsigned int);
+  off = up256(off + p->counter_bytes);
+  const size_t o_err = off;
+  off = up256(off + sizeof(int));
+  const size_t o_scr = off;
+  off = up256(off + (size_t)L.scratch_elems * sizeof(cf32));
+  p->ws_bytes = off;
+  s = dev_alloc(&p->ws, p->ws_bytes, "packed plan workspace");
+  if (s != ESTL_OK) return s;
+  char* w = static_cast<char*>(p->ws);
+  p->items = reinterpret_cast<PackedItem*>(w + o_items);
+  p->class_list = reinterpret_cast<int*>(w + o_cls);
+  p->offsets = reinterpret_cast<long long*>(w + o_off);
+  p->scratch_off = reinterpret_cast<long long*>(w + o_soff);
+  p->ncol = reinterpret_cast<int*>(w + o_ncol);
+  p->counters = reinterpret_cast<unsigned int*>(w + o_cnt);
+  p->error = reinterpret_cast<int*>(w + o_err);
+  p->scratch = reinterpret_cast<cf32*>(w + o_scr);
+  struct Up {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  } ups[] = {{p->items, L.items.data(), L.items.size() * sizeof(PackedItem)},
+             {p->class_list, L.class_list.data(), L.class_list.size() * sizeof(int)},
+             {p->offsets, L.offsets.data(), L.offsets.size() * sizeof(long long)},
+             {p->scratch_off, L.scratch_off.data(), L.scratch_off.size() * sizeof(long long)},
+             {p->ncol, L.ncol.data(), L.ncol.size() * sizeof(int)}};
+  for (const Up& u : ups) {
+    if (!u.bytes) continue;
+    s = check_cuda(cudaMemcpy(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice), "cudaMemcpy(packed tables)");
+    if (s != ESTL_OK) {
+      packed_release(p.release());
+      return s;
+    }
+  }
+  cudaMemset(p->error, 0, sizeof(int));
+  p->smem = (size_t)kPackedSmemElems * sizeof(cf32);
+  s = check_cuda(cudaFuncSetAttribute(packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem),
+                 "cudaFuncSetAttribute(packed)");
+  int per_sm = 0;
+  if (s == ESTL_OK)
+    s = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, packed_kernel, kPackedThreads, p->smem),
+                   "occupancy");
+  if (s == ESTL_OK)
+    s = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (s != ESTL_OK) {
+    packed_release(p.release());
+    return s;
+  }
+  p->grid = std::max(1, per_sm) * engine().num_sms;
+  *plan = p.release();
+  return ESTL_OK;
+}
+
+estl_status estl_packed_execute(estl_packed_plan p, const void* d_in, void* d_out, void* stream) {
+  if (!p || !d_in || !d_out) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
+  if (d_in == d_out) return fail(ESTL_INVALID_ARG, "in-place execution is not supported");
+  if (((uintptr_t)d_in & 7) || ((uintptr_t)d_out & 7)) return fail(ESTL_INVALID_ARG, "buffers must be 8-byte aligned");
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  std::lock_guard<std::mutex> g(p->mu);
+  if (!p->exec || p->g_in != d_in || p->g_out != d_out) {
+    // capture the launch sequence once per (input, output) pair
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->exec = nullptr;
+    p->graph = nullptr;
+    s = check_cuda(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    if (s != ESTL_OK) return s;
+    estl_status s2 = packed_enqueue(p, static_cast<const cf32*>(d_in), static_cast<cf32*>(d_out), p->cap_stream);
+    s = check_cuda(cudaStreamEndCapture(p->cap_stream, &p->graph), "cudaStreamEndCapture");
+    if (s2 != ESTL_OK) return s2;
+    if (s != ESTL_OK) return s;
+    s = check_cuda(cudaGraphInstantiate(&p->exec, p->graph, 0), "cudaGraphInstantiate");
+    if (s != ESTL_OK) return s;
+    p->g_in = d_in;
+    p->g_out = d_out;
+  }
+  return check_cuda(cudaGraphLaunch(p->exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+estl_status estl_packed_check(estl_packed_plan p) {
+  if (!p) return fail(ESTL_INVALID_ARG, "NULL plan");
+  estl_status s = check_cuda(cudaDeviceSynchronize(), "packed execute");
+  if (s != ESTL_OK) return s;
+  int e = 0;
+  s = check_cuda(cudaMemcpy(&e, p->error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  if (s != ESTL_OK) return s;
+  if (e) {
+    cudaMemset(p->error, 0, sizeof(int));
+    return fail(ESTL_TIMEOUT, "a row item gave up waiting for its column items");
+  }
+  return ESTL_OK;
+}
+
+estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len) {
+  if (!p || !buf || !len) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
+  const PackedLayout& L = p->layout;
+  std::snprintf(buf, len,
+                "{\"transforms\": %zu, \"items\": %zu, \"launches\": %zu, \"persistent\": %s, \"grid\": %d, "
+                "\"elements\": %lld, \"flops\": %.6g, \"scratch_bytes\": %lld, \"smem_bytes\": %zu}",
+                L.offsets.size(), L.items.size(), L.launch_begin.size(), L.persistent ? "true" : "false",
+                L.persistent ? p->grid : 0, L.elements, L.flops, L.scratch_elems * 8, p->smem);
+  return ESTL_OK;
+}
+
+estl_status estl_packed_plan_destroy(estl_packed_plan p) {
+  if (!p) return ESTL_OK;
+  cudaDeviceSynchronize();
+  packed_release(p);
+  return ESTL_OK;
+}
+
+}  // extern "C"

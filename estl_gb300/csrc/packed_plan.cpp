@@ -1,0 +1,136 @@
+// packed_plan.cpp — see packed_plan.h.
+#include "packed_plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace estl {
+
+int packed_single_logc(int logn) {
+  // 256 threads: 16 elements per thread for n >= 16, n elements (one thread) below
+  static const int c[13] = {0, 8, 8, 8, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+  return c[logn];
+}
+int packed_logn2(int logn) { return logn / 2; }
+static int logc_for_m(int logm) { return 12 - logm; }  // 256 threads = (2^logm / 16) * C
+int packed_col_logc(int logn) { return logc_for_m(packed_logn2(logn)); }
+int packed_row_logc(int logn) { return logc_for_m(logn - packed_logn2(logn)); }
+
+bool build_packed_layout(const long long* offsets, const long long* sizes, long long count, bool persistent,
+                         PackedLayout* out, std::string* err) {
+  PackedLayout L;
+  L.persistent = persistent;
+  if (count < 1 || !offsets || !sizes) {
+    if (err) *err = "need at least one transform";
+    return false;
+  }
+  if (count > (1LL << 30)) {
+    if (err) *err = "too many transforms";
+    return false;
+  }
+  L.offsets.assign(offsets, offsets + count);
+  L.lognv.resize(count);
+  L.scratch_off.assign(count, -1);
+  L.ncol.assign(count, 0);
+  for (long long i = 0; i < count; ++i) {
+    const long long n = sizes[i];
+    int l = 0;
+    while ((1LL << l) < n) l++;
+    if (n < 2 || (1LL << l) != n || l > kPackedMaxLog) {
+      if (err) *err = "transform " + std::to_string(i) + ": length " + std::to_string(n) +
+                      " is not a power of two in [2, 2^" + std::to_string(kPackedMaxLog) + "]";
+      return false;
+    }
+    if (offsets[i] < 0) {
+      if (err) *err = "transform " + std::to_string(i) + ": negative offset";
+      return false;
+    }
+    L.lognv[i] = l;
+    L.total_elems = std::max(L.total_elems, offsets[i] + n);
+    L.elements += n;
+    L.flops += 5.0 * (double)n * l;
+  }
+  // overlapping transforms would write the same output elements
+  std::vector<long long> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](long long a, long long b) { return offsets[a] < offsets[b]; });
+  for (long long k = 1; k < count; ++k) {
+    const long long a = order[k - 1], b = order[k];
+    if (offsets[a] + sizes[a] > offsets[b]) {
+      if (err) *err = "transforms " + std::to_string(a) + " and " + std::to_string(b) + " overlap";
+      return false;
+    }
+  }
+  // class lists, smallest class first
+  std::vector<std::vector<int>> cls(kPackedMaxLog + 1);
+  for (long long i = 0; i < count; ++i) cls[L.lognv[i]].push_back((int)i);
+  std::vector<PackedItem> single_items, col_items, row_items;
+  std::vector<std::vector<PackedItem>> per_class(kPackedMaxLog + 1);
+  std::vector<std::vector<PackedItem>> per_class_row(kPackedMaxLog + 1);
+  for (int l = kPackedMinLog; l <= kPackedMaxLog; ++l) {
+    if (cls[l].empty()) continue;
+    if (l <= kPackedSingleMaxLog) {
+      const int per = 1 << packed_single_logc(l);
+      const int base = (int)L.class_list.size();
+      L.class_list.insert(L.class_list.end(), cls[l].begin(), cls[l].end());
+      for (int k = 0; k < (int)cls[l].size(); k += per) {
+        PackedItem it{PK_SINGLE, l, base + k, std::min(per, (int)cls[l].size() - k)};
+        single_items.push_back(it);
+        per_class[l].push_back(it);
+      }
+    } else {
+      const int l2 = packed_logn2(l), l1 = l - l2;
+      const int cc = packed_col_logc(l), rc = packed_row_logc(l);
+      for (int id : cls[l]) {
+        L.scratch_off[id] = L.scratch_elems;
+        L.scratch_elems += 1LL << l;
+        L.ncol[id] = 1 << (l1 - cc);
+        for (int b = 0; b < (1 << (l1 - cc)); ++b) {
+          PackedItem it{PK_COL, l, id, b << cc};
+          col_items.push_back(it);
+          per_class[l].push_back(it);
+        }
+        for (int b = 0; b < (1 << (l2 - rc)); ++b) {
+          PackedItem it{PK_ROW, l, id, b << rc};
+          row_items.push_back(it);
+          per_class_row[l].push_back(it);
+        }
+      }
+    }
+  }
+  if (persistent) {
+    // Column items of the largest transforms first, then whole small
+    // transforms (they keep the SMs busy while the column items finish), then
+    // the row items in the same transform order: a row item is only taken
+    // after every column item has been taken by a running CTA, so its
+    // dependency wait ends.
+    auto by_size_desc = [](const PackedItem& a, const PackedItem& b) { return a.logn > b.logn; };
+    std::stable_sort(col_items.begin(), col_items.end(), by_size_desc);
+    std::stable_sort(row_items.begin(), row_items.end(), by_size_desc);
+    std::stable_sort(single_items.begin(), single_items.end(), by_size_desc);
+    L.items = col_items;
+    L.items.insert(L.items.end(), single_items.begin(), single_items.end());
+    L.items.insert(L.items.end(), row_items.begin(), row_items.end());
+    L.launch_begin.push_back(0);
+    L.launch_count.push_back((int)L.items.size());
+  } else {
+    // one launch per size class (two for four-step classes: columns, then rows)
+    for (int l = kPackedMinLog; l <= kPackedMaxLog; ++l) {
+      if (!per_class[l].empty()) {
+        L.launch_begin.push_back((int)L.items.size());
+        L.launch_count.push_back((int)per_class[l].size());
+        L.items.insert(L.items.end(), per_class[l].begin(), per_class[l].end());
+      }
+      if (!per_class_row[l].empty()) {
+        L.launch_begin.push_back((int)L.items.size());
+        L.launch_count.push_back((int)per_class_row[l].size());
+        L.items.insert(L.items.end(), per_class_row[l].begin(), per_class_row[l].end());
+      }
+    }
+  }
+  *out = std::move(L);
+  return true;
+}
+
+}  // namespace estl

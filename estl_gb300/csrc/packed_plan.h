@@ -1,0 +1,57 @@
+// packed_plan.h — uneven batches: many independent transforms of different
+// power-of-two lengths, packed in one buffer with an offsets array, run as a
+// list of work items by one persistent launch (or one launch per size class).
+//
+// The reference runs one FFT object per size (tests/Test.cpp:45-60 creates a
+// plan per (M, B)); there is no uneven batch.  Work items reuse the tile
+// bodies of fft_core.cuh with a fixed CTA of 256 threads:
+//   n <= 2^12           one item = C whole transforms of one size
+//   2^13 <= n <= 2^18   four-step: column items then row items per transform
+#pragma once
+#include <string>
+#include <vector>
+
+namespace estl {
+
+enum PackedItemKind { PK_SINGLE = 0, PK_COL = 1, PK_ROW = 2 };
+
+struct PackedItem {
+  int kind;   // PackedItemKind
+  int logn;   // transform length class
+  int tf;     // PK_SINGLE: first position in class_list; PK_COL/PK_ROW: transform index
+  int blk;    // PK_SINGLE: transforms in the item; PK_COL: first column n1; PK_ROW: first row k2
+};
+
+constexpr int kPackedThreads = 256;
+constexpr int kPackedMinLog = 1;
+constexpr int kPackedMaxLog = 18;
+constexpr int kPackedSingleMaxLog = 12;
+
+// Tile shape of a size class: log2 rows (single) or columns/rows (four-step) per item.
+int packed_single_logc(int logn);
+int packed_logn2(int logn);  // four-step column DFT length
+int packed_col_logc(int logn);
+int packed_row_logc(int logn);
+
+struct PackedLayout {
+  std::vector<PackedItem> items;
+  std::vector<int> class_list;          // transform indices grouped by size class
+  std::vector<long long> offsets;       // element offset of each transform (input and output)
+  std::vector<int> lognv;               // log2 length of each transform
+  std::vector<long long> scratch_off;   // four-step transforms: element offset in the scratch
+  std::vector<int> ncol;                // four-step transforms: column items (row-item dependency)
+  std::vector<int> launch_begin, launch_count;  // per-size mode: item ranges, one launch each
+  long long scratch_elems = 0;
+  long long total_elems = 0;  // max(offset + length)
+  long long elements = 0;     // sum of lengths
+  double flops = 0;           // sum of 5 n log2 n
+  bool persistent = true;
+};
+
+// offsets / sizes: count transforms.  Returns false with *err on a size that
+// is not a power of two in [2^1, 2^18], a negative offset, or overlapping
+// transforms.
+bool build_packed_layout(const long long* offsets, const long long* sizes, long long count, bool persistent,
+                         PackedLayout* out, std::string* err);
+
+}  // namespace estl

@@ -153,6 +153,74 @@ estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* result_json
 estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direction, const void* d_in, void* d_out,
                                  void* stream);
 
+/* ---- FFT convolution (Convolution2D_FFT, Convolution.h:95-154, in 1D) ----
+ * Real signal x (length L) with real filter h (length K): both zero-padded to
+ * n = nextPow2(L + K - 1) (Convolution.h:89-97), forward FFTs, pointwise
+ * product (conj(H) for correlation, :125-137), inverse FFT, scaled by 1/n.
+ * Default output: the full linear convolution, L + K - 1 samples.
+ * ESTL_CONV_REFERENCE_COMPAT reproduces Convolution.h's normalisation and crop
+ * instead: kernel centred by (K + 1)/2 (:113-120), result divided by n * H[0]
+ * (:141-143), L samples kept (:146-148).  n may be at most 2^22. */
+#define ESTL_CONV_CORRELATE 1
+#define ESTL_CONV_REFERENCE_COMPAT 2
+
+/* One request of a batched convolution.  Offsets are in floats into the
+ * caller's packed signal / filter / output arrays. */
+typedef struct estl_conv_request {
+  int64_t signal_len, filter_len;
+  int64_t signal_offset, filter_offset, output_offset;
+} estl_conv_request;
+
+/* Output samples of one request: L + K - 1, or L with REFERENCE_COMPAT. */
+int64_t estl_conv_output_length(int64_t signal_len, int64_t filter_len, int flags);
+
+/* Device workspace (bytes) estl_conv_execute needs for these requests. */
+estl_status estl_conv_workspace_size(const estl_conv_request* reqs, int64_t count, int flags, size_t* bytes);
+
+/* Batched convolution of requests with their own filters and lengths.
+ * Requests are grouped by padded length; each group runs a spectrum launch
+ * and a fused convolution launch (n <= 2^14), or five four-step launches.
+ * Blocking: returns when the outputs are written. */
+estl_status estl_conv_execute(const estl_conv_request* reqs, int64_t count, int flags, const float* d_signals,
+                              const float* d_filters, float* d_out, void* d_workspace, size_t workspace_bytes,
+                              void* stream);
+
+/* A convolution plan: `count` signals of signal_len samples, packed
+ * back-to-back, all with one filter whose spectrum is computed once
+ * (estl_conv_plan_set_filter) and cached on the device; outputs are packed
+ * back-to-back with estl_conv_output_length samples each.  Stream ordered. */
+typedef struct estl_conv_plan_s* estl_conv_plan;
+estl_status estl_conv_plan_create(int64_t signal_len, int64_t filter_len, int64_t count, int flags,
+                                  estl_conv_plan* plan);
+estl_status estl_conv_plan_set_filter(estl_conv_plan plan, const float* d_filter, void* stream);
+estl_status estl_conv_plan_execute(estl_conv_plan plan, const float* d_signals, float* d_out, void* stream);
+int64_t estl_conv_plan_launches(estl_conv_plan plan);
+estl_status estl_conv_plan_destroy(estl_conv_plan plan);
+
+/* ---- Uneven batches: packed transforms of mixed lengths ----
+ * count transforms, transform i of length sizes[i] (a power of two in
+ * [2, 2^18]) at complex-element offset offsets[i] of both the input and the
+ * output buffer (transforms must not overlap).  The reference has one FFT
+ * object per size (tests/Test.cpp:45-60) and no uneven batch.
+ * ESTL_PACKED_PERSISTENT: one persistent launch; CTAs take work items (whole
+ *   small transforms, four-step column and row tiles of large ones) from a
+ *   device queue, largest first; a row tile waits (bounded) for its column
+ *   tiles.  ESTL_PACKED_PER_SIZE: one launch per size class (two for
+ *   four-step classes).  Either way the launch sequence is captured once per
+ *   (d_in, d_out) pair in a CUDA graph and replayed. */
+#define ESTL_PACKED_PERSISTENT 0
+#define ESTL_PACKED_PER_SIZE 1
+typedef struct estl_packed_plan_s* estl_packed_plan;
+estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                    int mode, estl_packed_plan* plan);
+estl_status estl_packed_execute(estl_packed_plan plan, const void* d_in, void* d_out, void* stream);
+/* Waits for the device and returns ESTL_TIMEOUT if a dependency wait of the
+ * persistent kernel gave up since the last check (its outputs are then
+ * incomplete), else ESTL_OK. */
+estl_status estl_packed_check(estl_packed_plan plan);
+estl_status estl_packed_plan_describe(estl_packed_plan plan, char* buf, size_t len);
+estl_status estl_packed_plan_destroy(estl_packed_plan plan);
+
 /* Bytes currently held by the engine on the device (plans, scratch, staging,
  * twiddle bank) and the budget set at init. */
 estl_status estl_memory_usage(size_t* used_bytes, size_t* budget_bytes);

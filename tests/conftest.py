@@ -20,14 +20,16 @@ EMU_LIB = os.path.join(EMU_DIR, "_build", "libestl_emu.so")
 
 def build_emulator():
     """Compile the host emulator of the tile kernels (g++, C++20)."""
-    srcs = [os.path.join(EMU_DIR, "emu.cpp"), os.path.join(ROOT, "estl_gb300", "csrc", "planner.cpp")]
+    srcs = [os.path.join(EMU_DIR, "emu.cpp"), os.path.join(ROOT, "estl_gb300", "csrc", "planner.cpp"),
+            os.path.join(ROOT, "estl_gb300", "csrc", "conv_plan.cpp"),
+            os.path.join(ROOT, "estl_gb300", "csrc", "packed_plan.cpp")]
     deps = srcs + [os.path.join(ROOT, "estl_gb300", "csrc", f) for f in os.listdir(os.path.join(ROOT, "estl_gb300", "csrc"))]
     if os.path.exists(EMU_LIB) and os.path.getmtime(EMU_LIB) >= max(os.path.getmtime(d) for d in deps):
         return EMU_LIB
     os.makedirs(os.path.dirname(EMU_LIB), exist_ok=True)
     cmd = ["g++", "-std=c++20", "-O2", "-DESTL_EMU", "-fPIC", "-shared", "-pthread",
            "-I", os.path.join(ROOT, "estl_gb300", "csrc"), "-I", os.path.join(ROOT, "include"),
-           "-x", "c++", srcs[0], "-x", "c++", srcs[1], "-o", EMU_LIB]
+           "-x", "c++"] + srcs + ["-o", EMU_LIB]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return EMU_LIB
 
@@ -40,6 +42,11 @@ def emu():
     lib.emu_plan_run.restype = ctypes.c_int
     lib.emu_plan_describe.argtypes = [ctypes.c_longlong, ctypes.c_longlong, P, ctypes.c_char_p, ctypes.c_int]
     lib.emu_plan_candidates.argtypes = [ctypes.c_longlong, ctypes.c_longlong, P, ctypes.c_int]
+    lib.emu_conv_run.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, ctypes.c_char_p, ctypes.c_int]
+    lib.emu_conv_run.restype = ctypes.c_int
+    lib.emu_packed_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_char_p,
+                                   ctypes.c_int]
+    lib.emu_packed_run.restype = ctypes.c_int
     lib.emu_bank.argtypes = [P]
     lib.emu_bank.restype = ctypes.c_longlong
     return lib

@@ -17,7 +17,9 @@
 #include <thread>
 #include <vector>
 
+#include "conv_plan.h"
 #include "fft_core.cuh"
+#include "packed_core.cuh"
 #include "planner.h"
 
 using namespace estl;
@@ -115,6 +117,68 @@ bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
           estl_emu_sync();
           // poison shared memory between CTAs so that a read of a slot the
           // current CTA never wrote shows up as NaN in the output
+          if (tid == 0)
+            for (auto& e : smem) e = cf32{nan, nan};
+          estl_emu_sync();
+        }
+      } catch (const EmuFault&) {
+        failed = true;
+        bar.arrive_and_drop();
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  return !failed;
+}
+
+// ---- convolution kernels ----
+using ConvFn = void (*)(const ConvArgs&, long long, int, cf32*);
+struct EmuConvKernel {
+  int kind, logm, loge, logr, logc, nt;
+  long long smem;
+  ConvFn fn;
+};
+
+template <class K>
+EmuConvKernel mkc(int kind, int m, int e, int r, int c) {
+  return EmuConvKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run};
+}
+
+const std::vector<EmuConvKernel>& emu_conv_kernels() {
+  static const std::vector<EmuConvKernel> v = [] {
+    std::vector<EmuConvKernel> k;
+#define ESTL_XC_SINGLE(M, E, R, C)                                      \
+  k.push_back(mkc<SpecSingleKernel<M, E, R, C>>(CK_SPEC_SINGLE, M, E, R, C)); \
+  k.push_back(mkc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C));
+#define ESTL_XC_COL(M, E, R, C)                                       \
+  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C)); \
+  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));
+#define ESTL_XC_ROW(M, E, R, C)                                     \
+  k.push_back(mkc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C)); \
+  k.push_back(mkc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));
+#define ESTL_XC_OUT(M, E, R, C) k.push_back(mkc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C));
+#include "conv_list.inc"
+    return k;
+  }();
+  return v;
+}
+
+template <class Fn, class Args>
+bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
+  std::barrier<> bar(nt);
+  std::vector<cf32> smem((size_t)std::max<long long>(smem_elems, 1));
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  for (auto& e : smem) e = cf32{nan, nan};
+  std::atomic<bool> failed{false};
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int tid = 0; tid < nt; ++tid) {
+    th.emplace_back([&, tid] {
+      tl_bar = &bar;
+      try {
+        for (long long cta = 0; cta < grid; ++cta) {
+          fn(a, cta, tid, smem.data());
+          estl_emu_sync();
           if (tid == 0)
             for (auto& e : smem) e = cf32{nan, nan};
           estl_emu_sync();
@@ -241,6 +305,118 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[8] = (int)ch.chunk;
   }
   return (int)c.size();
+}
+
+// Batched FFT convolution of real data.  reqs: count x 5 int64
+// (signal_len, filter_len, sig_off, filt_off, out_off).  shared: one filter
+// (request 0) for all.  Returns 0 ok, 1 out-of-bounds access, 2 layout error,
+// 3 missing kernel.
+int emu_conv_run(const long long* reqs, int count, int flags, int shared, const float* sig, const float* filt,
+                 float* out, char* err, int errlen) {
+  ConvLayout L;
+  std::string e;
+  if (!build_conv_layout(reinterpret_cast<const ConvReq*>(reqs), count, flags, &L, &e, shared != 0)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    g_msg.clear();
+  }
+  long long se, fe;
+  conv_extents(reinterpret_cast<const ConvReq*>(reqs), count, &se, &fe);
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  std::vector<cf32> spec((size_t)std::max<long long>(L.spec_elems, 1), cf32{nan, nan});
+  std::vector<cf32> s1((size_t)std::max<long long>(L.scratch_elems, 1), cf32{nan, nan});
+  std::vector<cf32> s2((size_t)std::max<long long>(L.scratch_elems, 1), cf32{nan, nan});
+  for (const ConvLaunch& l : L.launches) {
+    const EmuConvKernel* k = nullptr;
+    for (const EmuConvKernel& c : emu_conv_kernels())
+      if (c.kind == l.kind && c.logm == l.logm && c.loge == l.loge && c.logr == l.logr && c.logc == l.logc) k = &c;
+    if (!k) {
+      set_err(err, errlen, "no emulated convolution kernel for a launch");
+      return 3;
+    }
+    const long long N = 1LL << l.logn;
+    const bool f = l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW;
+    if (l.s_off + l.row_count * N > (long long)s1.size() && (l.kind >= CK_COL_FILTER)) {
+      set_err(err, errlen, "launch scratch range outside the scratch buffer");
+      return 1;
+    }
+    ConvArgs a;
+    const std::vector<ConvRow>& rows = f ? L.filt_rows : L.sig_rows;
+    a.rows = Ptr<const ConvRow>{rows.data() + l.row_begin, l.row_count};
+    a.nrows = l.row_count;
+    a.sig = f ? Ptr<const float>{filt, fe} : Ptr<const float>{sig, se};
+    a.spec = Ptr<const cf32>{spec.data(), L.spec_elems};
+    a.spec_out = Ptr<cf32>{spec.data(), L.spec_elems};
+    a.out = Ptr<float>{out, L.out_elems};
+    a.s1 = Ptr<cf32>{s1.data() + (l.kind >= CK_COL_FILTER ? l.s_off : 0), l.kind >= CK_COL_FILTER ? l.row_count * N : 0};
+    a.s2 = Ptr<cf32>{s2.data() + (l.kind >= CK_COL_FILTER ? l.s_off : 0), l.kind >= CK_COL_FILTER ? l.row_count * N : 0};
+    a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
+    a.logn = l.logn;
+    if (!run_generic(k->nt, k->smem, k->fn, a, l.grid)) {
+      std::lock_guard<std::mutex> g(g_msg_mu);
+      set_err(err, errlen, g_msg);
+      return 1;
+    }
+  }
+  return 0;
+}
+
+// Uneven batch: count transforms of lengths sizes[i] at offsets[i] (complex
+// elements).  persistent: the work-queue kernel run as one CTA (items in
+// queue order); else one CTA per item, launch by launch.  Returns 0 ok,
+// 1 out-of-bounds access, 2 layout error, 4 a dependency wait gave up.
+int emu_packed_run(const long long* offsets, const long long* sizes, long long count, int persistent, int sign,
+                   const float* in, float* out, char* err, int errlen) {
+  PackedLayout L;
+  std::string e;
+  if (!build_packed_layout(offsets, sizes, count, persistent != 0, &L, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    g_msg.clear();
+  }
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  std::vector<cf32> scratch((size_t)std::max<long long>(L.scratch_elems, 1), cf32{nan, nan});
+  std::vector<unsigned int> counters(1 + L.offsets.size(), 0u);
+  int error = 0;
+  for (size_t k = 0; k < L.launch_begin.size(); ++k) {
+    PackedArgs a;
+    a.items = Ptr<const PackedItem>{L.items.data(), (long long)L.items.size()};
+    a.item_base = L.launch_begin[k];
+    a.nitems = L.launch_count[k];
+    a.class_list = Ptr<const int>{L.class_list.data(), (long long)L.class_list.size()};
+    a.offsets = Ptr<const long long>{L.offsets.data(), (long long)L.offsets.size()};
+    a.scratch_off = Ptr<const long long>{L.scratch_off.data(), (long long)L.scratch_off.size()};
+    a.ncol = Ptr<const int>{L.ncol.data(), (long long)L.ncol.size()};
+    a.in = Ptr<const cf32>{reinterpret_cast<const cf32*>(in), L.total_elems};
+    a.out = Ptr<cf32>{reinterpret_cast<cf32*>(out), L.total_elems};
+    a.scratch = Ptr<cf32>{scratch.data(), L.scratch_elems};
+    a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
+    a.next = counters.data();
+    a.done = counters.data() + 1;
+    a.error = &error;
+    a.sgn = sign < 0 ? 1.f : -1.f;
+    a.persistent = persistent ? 1 : 0;
+    counters[0] = 0;
+    int slot[2] = {0, 0};
+    auto fn = [&slot](const PackedArgs& args, long long cta, int tid, cf32* sm) { packed_run(args, cta, tid, sm, slot); };
+    const long long grid = persistent ? 1 : a.nitems;
+    if (!run_generic(kPackedThreads, kPackedSmemElems, fn, a, grid)) {
+      std::lock_guard<std::mutex> g(g_msg_mu);
+      set_err(err, errlen, g_msg);
+      return 1;
+    }
+  }
+  if (error) {
+    set_err(err, errlen, "dependency wait gave up");
+    return 4;
+  }
+  return 0;
 }
 
 // Copies the host twiddle bank (kBankSize complex64) into out (if not NULL);

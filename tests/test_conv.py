@@ -1,0 +1,186 @@
+"""FFT convolution (Convolution2D_FFT, Convolution.h:95-154, in 1D and batched).
+
+* emulator (CPU): every size class through the host emulator of the
+  convolution kernels, with bounds checks, against the FP64 oracle;
+* GPU: the C ABI (estl_conv_execute, estl_conv_plan_*) against the oracle.
+
+Tolerance: rel-L2 of the output vector <= 1e-6 against the FP64 FFT
+convolution (itself checked against a long-double direct convolution in
+tests/test_oracle.py).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+
+TOL = 1e-6
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
+
+
+def make_requests(shapes, seed):
+    """Packed signals / filters / outputs for (L, K) pairs."""
+    rng = np.random.default_rng(seed)
+    reqs, sigs, filts = [], [], []
+    so = fo = oo = 0
+    for L, K in shapes:
+        s = rng.standard_normal(L).astype(np.float32)
+        f = rng.standard_normal(K).astype(np.float32)
+        reqs.append((L, K, so, fo, oo))
+        sigs.append(s)
+        filts.append(f)
+        so += L
+        fo += K
+        oo += L + K - 1
+    return reqs, np.concatenate(sigs), np.concatenate(filts), oo
+
+
+def compat_reference(s, f):
+    """Convolution.h's normalisation and crop in 1D: centre the kernel by
+    (K+1)/2 (:113-120), divide by sum(h) (= K^[0], :141-143), keep L samples."""
+    L, K = len(s), len(f)
+    full = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))
+    sh = (K + 1) // 2
+    return full[sh: sh + L] / np.sum(f.astype(np.float64))
+
+
+def emu_conv(emu, reqs, sig, filt, out_len, flags=0, shared=False):
+    arr = np.array(reqs, dtype=np.int64).ravel()
+    out = np.full(out_len, np.nan, np.float32)
+    err = ctypes.create_string_buffer(512)
+    rc = emu.emu_conv_run(arr.ctypes.data, len(reqs), flags, int(shared), sig.ctypes.data, filt.ctypes.data,
+                          out.ctypes.data, err, len(err))
+    assert rc == 0, err.value
+    return out
+
+
+SHAPES_EMU = [(1, 1), (3, 2), (5, 4), (16, 16), (100, 17), (256, 16), (1000, 64), (2000, 100), (4096, 300),
+              (9000, 700), (13000, 3000), (20000, 4096)]
+
+
+def test_emulated_batch_all_size_classes(emu):
+    reqs, sig, filt, olen = make_requests(SHAPES_EMU, 1)
+    out = emu_conv(emu, reqs, sig, filt, olen)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < TOL, (L, K)
+
+
+def test_emulated_correlation_and_compat(emu):
+    shapes = [(300, 40), (5000, 33), (20000, 257)]
+    reqs, sig, filt, olen = make_requests(shapes, 2)
+    out = emu_conv(emu, reqs, sig, filt, olen, flags=1)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64), correlate=True)
+        assert rel(out[oo:oo + L + K - 1], ref) < TOL
+    # reference-compatible mode writes L samples per request
+    creqs = []
+    oo = 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L
+    # positive filters keep sum(h) away from zero
+    filt_pos = np.abs(filt) + 0.1
+    out = emu_conv(emu, creqs, sig, filt_pos, oo, flags=2)
+    for L, K, so, fo, oo in creqs:
+        ref = compat_reference(sig[so:so + L], filt_pos[fo:fo + K])
+        assert rel(out[oo:oo + L], ref) < TOL
+
+
+def test_emulated_shared_filter(emu):
+    L, K, n = 3000, 100, 7
+    rng = np.random.default_rng(3)
+    sig = rng.standard_normal(L * n).astype(np.float32)
+    filt = rng.standard_normal(K).astype(np.float32)
+    reqs = [(L, K, i * L, 0, i * (L + K - 1)) for i in range(n)]
+    out = emu_conv(emu, reqs, sig, filt, n * (L + K - 1), shared=True)
+    for i in range(n):
+        ref = oracle.conv_fft(sig[i * L:(i + 1) * L].astype(np.float64), filt.astype(np.float64))
+        assert rel(out[i * (L + K - 1):(i + 1) * (L + K - 1)], ref) < TOL
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def gpu_conv_batch(engine, reqs, sig, filt, out_len, flags=0):
+    import torch
+
+    from estl_gb300._lib import ConvRequest, check, lib
+    L = lib()
+    arr = (ConvRequest * len(reqs))(*[ConvRequest(*r) for r in reqs])
+    ws = ctypes.c_size_t()
+    check(L.estl_conv_workspace_size(arr, len(reqs), flags, ctypes.byref(ws)))
+    d_sig = torch.from_numpy(sig).cuda()
+    d_filt = torch.from_numpy(filt).cuda()
+    d_out = torch.full((out_len,), float("nan"), device="cuda")
+    d_ws = torch.empty(ws.value + 256, dtype=torch.uint8, device="cuda")
+    base = (d_ws.data_ptr() + 255) // 256 * 256
+    st = torch.cuda.current_stream().cuda_stream
+    check(L.estl_conv_execute(arr, len(reqs), flags, ctypes.c_void_p(d_sig.data_ptr()),
+                              ctypes.c_void_p(d_filt.data_ptr()), ctypes.c_void_p(d_out.data_ptr()),
+                              ctypes.c_void_p(base), ws.value, ctypes.c_void_p(st)))
+    return d_out.cpu().numpy()
+
+
+@pytest.mark.gpu
+def test_gpu_batch_mixed_sizes(engine):
+    shapes = SHAPES_EMU + [(1 << 16, 4096), (1 << 18, 1000), ((1 << 20) - 7, 4096), (1 << 20, 4096)]
+    reqs, sig, filt, olen = make_requests(shapes, 4)
+    out = gpu_conv_batch(engine, reqs, sig, filt, olen)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < TOL, (L, K)
+
+
+@pytest.mark.gpu
+def test_gpu_correlation_and_compat(engine):
+    shapes = [(300, 40), (5000, 33), (20000, 257), (300000, 2049)]
+    reqs, sig, filt, olen = make_requests(shapes, 5)
+    out = gpu_conv_batch(engine, reqs, sig, filt, olen, flags=1)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64), correlate=True)
+        assert rel(out[oo:oo + L + K - 1], ref) < TOL
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L
+    filt_pos = np.abs(filt) + 0.1
+    out = gpu_conv_batch(engine, creqs, sig, filt_pos, oo, flags=2)
+    for L, K, so, fo, oo in creqs:
+        assert rel(out[oo:oo + L], compat_reference(sig[so:so + L], filt_pos[fo:fo + K])) < TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,K,count", [(1000, 31, 64), (50000, 1000, 8), (1 << 20, 4096, 2)])
+def test_gpu_conv_plan(engine, L, K, count):
+    import torch
+
+    from estl_gb300._lib import check, lib
+    Lb = lib()
+    plan = ctypes.c_void_p()
+    check(Lb.estl_conv_plan_create(L, K, count, 0, ctypes.byref(plan)))
+    try:
+        rng = np.random.default_rng(L + K)
+        sig = rng.standard_normal(L * count).astype(np.float32)
+        filt = rng.standard_normal(K).astype(np.float32)
+        olen = int(Lb.estl_conv_output_length(L, K, 0))
+        st = torch.cuda.current_stream().cuda_stream
+        d_filt = torch.from_numpy(filt).cuda()
+        check(Lb.estl_conv_plan_set_filter(plan, ctypes.c_void_p(d_filt.data_ptr()), ctypes.c_void_p(st)))
+        d_sig = torch.from_numpy(sig).cuda()
+        d_out = torch.full((olen * count,), float("nan"), device="cuda")
+        for _ in range(2):  # cached spectrum reused
+            check(Lb.estl_conv_plan_execute(plan, ctypes.c_void_p(d_sig.data_ptr()),
+                                            ctypes.c_void_p(d_out.data_ptr()), ctypes.c_void_p(st)))
+        out = d_out.cpu().numpy()
+        for i in range(count):
+            ref = oracle.conv_fft(sig[i * L:(i + 1) * L].astype(np.float64), filt.astype(np.float64))
+            assert rel(out[i * olen:(i + 1) * olen], ref) < TOL
+    finally:
+        Lb.estl_conv_plan_destroy(plan)

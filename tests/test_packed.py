@@ -1,0 +1,132 @@
+"""Uneven batches: packed transforms of mixed power-of-two lengths with an
+offsets array (the uneven-batch configuration: 8192 transforms, lengths
+log-uniform over 2^6..2^16, complex N(0,1), seed 3).
+
+* emulator (CPU): both execution modes of the packed kernel (persistent work
+  queue; one launch per size) through the bounds-checked host emulator;
+* GPU: the C ABI at the full configuration, both modes, against the oracle.
+"""
+import ctypes
+import json
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def tol(n):
+    return 2e-6
+
+
+def make_batch(count, lo, hi, seed, gap=0):
+    rng = np.random.default_rng(seed)
+    e = rng.integers(lo, hi + 1, count)
+    sizes = (1 << e).astype(np.int64)
+    offsets = np.zeros(count, np.int64)
+    if count > 1:
+        offsets[1:] = np.cumsum(sizes[:-1] + gap)
+    total = int(offsets[-1] + sizes[-1])
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    return offsets, sizes, x
+
+
+def check_against_oracle(offsets, sizes, x, y, sign, every=1):
+    for i in range(0, len(sizes), every):
+        o, n = int(offsets[i]), int(sizes[i])
+        ref = oracle.fft(x[o:o + n][None, :], sign)
+        e = oracle.rel_l2(y[o:o + n][None, :], ref)[0]
+        assert e < tol(n), (i, n, e)
+
+
+def emu_packed(emu, offsets, sizes, x, persistent, sign):
+    y = np.full_like(x, np.nan + 1j * np.nan)
+    err = ctypes.create_string_buffer(512)
+    rc = emu.emu_packed_run(offsets.ctypes.data, sizes.ctypes.data, len(sizes), int(persistent), sign,
+                            x.ctypes.data, y.ctypes.data, err, len(err))
+    return rc, err.value.decode(), y
+
+
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_emulated_mixed_sizes(emu, persistent):
+    offsets, sizes, x = make_batch(40, 1, 15, 11, gap=3)
+    for sign in (-1, +1):
+        rc, msg, y = emu_packed(emu, offsets, sizes, x, persistent, sign)
+        assert rc == 0, msg
+        check_against_oracle(offsets, sizes, x, y, sign)
+
+
+def test_emulated_largest_classes(emu):
+    offsets = np.array([0, 1 << 16, (1 << 16) + (1 << 17)], np.int64)
+    sizes = np.array([1 << 16, 1 << 17, 1 << 18], np.int64)
+    rng = np.random.default_rng(5)
+    total = int(offsets[-1] + sizes[-1])
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    rc, msg, y = emu_packed(emu, offsets, sizes, x, 1, -1)
+    assert rc == 0, msg
+    check_against_oracle(offsets, sizes, x, y, -1)
+
+
+def test_layout_validation(emu):
+    x = np.zeros(64, np.complex64)
+    bad = [
+        (np.array([0, 8], np.int64), np.array([16, 16], np.int64)),   # overlap
+        (np.array([0], np.int64), np.array([12], np.int64)),          # not a power of two
+        (np.array([0], np.int64), np.array([1 << 19], np.int64)),     # too long
+        (np.array([-4], np.int64), np.array([4], np.int64)),          # negative offset
+    ]
+    for off, sz in bad:
+        rc, msg, _ = emu_packed(emu, off, sz, x, 1, -1)
+        assert rc == 2 and msg
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def gpu_packed(offsets, sizes, x_dev, mode, direction):
+    import torch
+
+    from estl_gb300._lib import check, lib
+    L = lib()
+    plan = ctypes.c_void_p()
+    check(L.estl_packed_plan_create(offsets.ctypes.data, sizes.ctypes.data, len(sizes), direction, mode,
+                                    ctypes.byref(plan)))
+    y = torch.full_like(x_dev, float("nan"))
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):  # graph capture, then replay
+        check(L.estl_packed_execute(plan, ctypes.c_void_p(x_dev.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                    ctypes.c_void_p(st)))
+    check(L.estl_packed_check(plan))
+    buf = ctypes.create_string_buffer(1024)
+    check(L.estl_packed_plan_describe(plan, buf, len(buf)))
+    desc = json.loads(buf.value.decode())
+    L.estl_packed_plan_destroy(plan)
+    return y.cpu().numpy(), desc
+
+
+@pytest.mark.gpu
+def test_gpu_uneven_configuration(engine):
+    """8192 transforms, log-uniform 2^6..2^16, N(0,1), seed 3: both modes agree
+    with each other bit for bit and with the oracle (every 8th transform)."""
+    import torch
+    offsets, sizes, x = make_batch(8192, 6, 16, 3)
+    xd = torch.from_numpy(x).cuda()
+    yp, dp = gpu_packed(offsets, sizes, xd, 0, -1)
+    ys, ds = gpu_packed(offsets, sizes, xd, 1, -1)
+    assert dp["persistent"] and dp["launches"] == 1 and not ds["persistent"] and ds["launches"] >= 11
+    assert np.array_equal(yp, ys)
+    check_against_oracle(offsets, sizes, x, yp, -1, every=8)
+
+
+@pytest.mark.gpu
+def test_gpu_packed_backward_and_gaps(engine):
+    import torch
+    offsets, sizes, x = make_batch(300, 1, 18, 7, gap=5)
+    xd = torch.from_numpy(x).cuda()
+    y, _ = gpu_packed(offsets, sizes, xd, 0, +1)
+    check_against_oracle(offsets, sizes, x, y, +1)
+    # the gaps between transforms are not written
+    mask = np.ones(len(x), bool)
+    for o, n in zip(offsets, sizes):
+        mask[o:o + n] = False
+    assert np.all(np.isnan(y[mask].real))
