@@ -150,7 +150,7 @@ def fft(x, inverse=False, out=None, stream=None):
 def autotune(n, batch, iters=5):
     """Time every candidate plan for (n, batch); cache and return the best."""
     _ensure_init()
-    buf = ctypes.create_string_buffer(4096)
+    buf = ctypes.create_string_buffer(1 << 16)
     check(lib().estl_autotune(int(n), int(batch), int(iters), buf, len(buf)))
     for key in [k for k in _plan_cache if k[0] == n and k[1] == batch]:
         _plan_cache.pop(key).close()

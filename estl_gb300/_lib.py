@@ -74,7 +74,38 @@ SIGNATURES = {
     "estl_packed_check": (_INT, [_P]),
     "estl_packed_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_packed_plan_destroy": (_INT, [_P]),
+    "estl_serve_start": (_INT, [_P, ctypes.POINTER(_P)]),
+    "estl_serve_submit": (_INT, [_P, _P, ctypes.POINTER(ctypes.c_uint64)]),
+    "estl_serve_poll": (_INT, [_P, ctypes.c_uint64, _INT, _P]),
+    "estl_serve_stats_get": (_INT, [_P, _P]),
+    "estl_serve_stop": (_INT, [_P]),
 }
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight_batches", ctypes.c_int),
+                ("max_batch_requests", ctypes.c_int), ("max_queue", ctypes.c_int64)]
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("direction", ctypes.c_int), ("flags", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("n", ctypes.c_int64), ("signal_len", ctypes.c_int64), ("filter_len", ctypes.c_int64),
+                ("in_", ctypes.c_void_p), ("filter", ctypes.c_void_p), ("out", ctypes.c_void_p)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("batch_requests", ctypes.c_int), ("latency_us", ctypes.c_double),
+                ("queue_us", ctypes.c_double), ("device_us", ctypes.c_double)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("max_batch_requests", ctypes.c_int64), ("queued", ctypes.c_int64),
+                ("inflight_bytes", ctypes.c_uint64), ("max_inflight_bytes", ctypes.c_uint64)]
+
+
+REQ_FFT = 0
+REQ_CONV = 1
 
 
 class ConvRequest(ctypes.Structure):

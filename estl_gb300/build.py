@@ -27,6 +27,7 @@ SOURCES = [
     "conv.cu",
     "packed_plan.cpp",
     "packed.cu",
+    "serve.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

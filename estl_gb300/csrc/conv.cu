@@ -6,8 +6,7 @@
 #include <mutex>
 #include <vector>
 
-#include "conv_plan.h"
-#include "engine.h"
+#include "conv_exec.h"
 
 namespace estl {
 
@@ -74,22 +73,6 @@ estl_status conv_lookup(const ConvLaunch& l, const ConvKernelDesc** out) {
 
 }  // namespace
 
-// Device pointers of one convolution batch.
-struct ConvBuffers {
-  const float* sig;
-  long long sig_elems;
-  const float* filt;
-  long long filt_elems;
-  float* out;
-  long long out_elems;
-  const ConvRow* filt_rows;
-  const ConvRow* sig_rows;
-  cf32* spec;
-  cf32* s1;
-  cf32* s2;
-};
-
-// which: 1 = spectrum launches, 2 = convolution launches, 3 = both.
 estl_status launch_conv(const ConvLayout& L, const ConvBuffers& b, int which, cudaStream_t stream) {
   Engine& E = engine();
   for (size_t i = 0; i < L.launches.size(); ++i) {

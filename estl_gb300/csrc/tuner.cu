@@ -166,6 +166,7 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
   cudaEventCreate(&e1);
   double best_ms = 1e30;
   const Plan1D* best = nullptr;
+  std::vector<std::pair<double, const Plan1D*>> timed;
   for (const Plan1D& p : plans) {
     s = launch_steps(p, in, out, scr, 1.f, st);
     if (s != ESTL_OK) continue;
@@ -180,6 +181,7 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= iters;
+    timed.push_back({ms, &p});
     if (ms < best_ms) {
       best_ms = ms;
       best = &p;
@@ -197,7 +199,15 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
     std::string j = std::string("{\"n\": ") + std::to_string((long long)n) + ", \"batch\": " +
                     std::to_string((long long)batch) + ", \"candidates\": " + std::to_string(plans.size()) +
                     ", \"best_ms\": " + std::to_string(best_ms) + ", \"choice\": " + choice_to_json(best->choice) +
-                    ", \"plan\": " + best->describe() + "}";
+                    ", \"plan\": " + best->describe() + ", \"fastest\": [";
+    std::sort(timed.begin(), timed.end(),
+              [](const std::pair<double, const Plan1D*>& a, const std::pair<double, const Plan1D*>& b) {
+                return a.first < b.first;
+              });
+    for (size_t i = 0; i < timed.size() && i < 8; ++i)
+      j += std::string(i ? ", " : "") + "{\"ms\": " + std::to_string(timed[i].first) +
+           ", \"choice\": " + choice_to_json(timed[i].second->choice) + "}";
+    j += "]}";
     std::snprintf(result_json, len, "%s", j.c_str());
   }
   return ESTL_OK;

@@ -221,6 +221,66 @@ estl_status estl_packed_check(estl_packed_plan plan);
 estl_status estl_packed_plan_describe(estl_packed_plan plan, char* buf, size_t len);
 estl_status estl_packed_plan_destroy(estl_packed_plan plan);
 
+/* ---- Serving: a request loop with continuous batching ----
+ * Requests (1D FFTs and FFT convolutions of mixed lengths, host buffers) are
+ * queued by estl_serve_submit and completed by a device-owner thread: when a
+ * stream slot is free it admits queued requests in arrival order while their
+ * device memory fits the HBM budget, runs them as one batch (inputs in,
+ * kernels grouped by size, outputs out, all stream ordered) and keeps up to
+ * max_inflight_batches batches overlapping on the device.  A request's host
+ * buffers must stay valid until its estl_serve_poll returns.  Each request's
+ * result is bit-identical alone and in any batch.
+ * max_batch_requests = 1 and max_inflight_batches = 1 give the plain
+ * per-request behaviour of the reference (FFT<D>::execute, FFT.h:35, and
+ * Convolution2D_FFT::convolve, Convolution.h:95, are blocking calls). */
+#define ESTL_REQ_FFT 0
+#define ESTL_REQ_CONV 1
+
+typedef struct estl_serve_config {
+  size_t hbm_budget_bytes;   /* device bytes in flight (0 = what the engine budget leaves) */
+  int max_inflight_batches;  /* stream slots; batches that overlap on the device (0 = 4) */
+  int max_batch_requests;    /* requests per batch (0 = 256) */
+  int64_t max_queue;         /* queued requests before submit rejects (0 = 2^20) */
+} estl_serve_config;
+
+typedef struct estl_serve_request {
+  int kind;                  /* ESTL_REQ_FFT or ESTL_REQ_CONV */
+  int direction;             /* FFT: ESTL_FORWARD / ESTL_BACKWARD */
+  int flags;                 /* CONV: ESTL_CONV_* */
+  int reserved;
+  int64_t n;                 /* FFT: length (power of two <= 2^24) */
+  int64_t signal_len;        /* CONV */
+  int64_t filter_len;        /* CONV */
+  const float* in;           /* FFT: n complex64; CONV: signal_len floats */
+  const float* filter;       /* CONV: filter_len floats */
+  float* out;                /* FFT: n complex64; CONV: estl_conv_output_length floats */
+} estl_serve_request;
+
+typedef struct estl_serve_result {
+  estl_status status;
+  int batch_requests;        /* size of the batch the request ran in */
+  double latency_us;         /* submit -> outputs in the host buffer */
+  double queue_us;           /* submit -> admitted */
+  double device_us;          /* batch launch -> outputs in the host buffer */
+} estl_serve_result;
+
+typedef struct estl_serve_stats {
+  int64_t submitted, completed, rejected, batches, max_batch_requests, queued;
+  uint64_t inflight_bytes, max_inflight_bytes;
+} estl_serve_stats;
+
+typedef struct estl_server_s* estl_server;
+estl_status estl_serve_start(const estl_serve_config* cfg, estl_server* server);
+/* Queues a request; ESTL_ADMISSION_REJECTED if it can never fit the budget or
+ * the queue is full. */
+estl_status estl_serve_submit(estl_server server, const estl_serve_request* req, uint64_t* ticket);
+/* Waits up to timeout_ms for the request (ESTL_TIMEOUT if not done; the
+ * ticket stays valid); on completion fills res and releases the ticket. */
+estl_status estl_serve_poll(estl_server server, uint64_t ticket, int timeout_ms, estl_serve_result* res);
+estl_status estl_serve_stats_get(estl_server server, estl_serve_stats* stats);
+/* Completes every queued and in-flight request, then stops the loop. */
+estl_status estl_serve_stop(estl_server server);
+
 /* Bytes currently held by the engine on the device (plans, scratch, staging,
  * twiddle bank) and the budget set at init. */
 estl_status estl_memory_usage(size_t* used_bytes, size_t* budget_bytes);

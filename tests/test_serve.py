@@ -1,0 +1,112 @@
+"""The serving loop (estl_serve_*): FFT and FFT-convolution requests of mixed
+lengths, continuous batching, HBM admission, and the same result alone and
+in the mix."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
+
+
+def conv_requests(count, seed):
+    """Served-convolution configuration shapes: signal log-uniform 2^8..2^20,
+    filter log-uniform 2^4..2^12, both N(0,1)."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(count):
+        L = int(2 ** rng.uniform(8, 20))
+        K = int(2 ** rng.uniform(4, 12))
+        s = rng.standard_normal(L).astype(np.float32)
+        f = rng.standard_normal(K).astype(np.float32)
+        reqs.append((s, f))
+    return reqs
+
+
+def run_mixed(server, convs, ffts):
+    tickets = []
+    outs = []
+    for s, f in convs:
+        out = np.full(s.size + f.size - 1, np.nan, np.float32)
+        tickets.append(server.submit_conv(s, f, out))
+        outs.append(out)
+    for x, d in ffts:
+        out = np.full_like(x, np.nan)
+        tickets.append(server.submit_fft(x, out, d))
+        outs.append(out)
+    results = [server.poll(t) for t in tickets]
+    return outs, results
+
+
+def test_mixed_requests_against_oracle(engine):
+    from estl_gb300.serve import Server
+    convs = conv_requests(40, 1)
+    rng = np.random.default_rng(2)
+    ffts = []
+    for logn in (6, 10, 12, 15, 18, 20):
+        x = (rng.standard_normal(1 << logn) + 1j * rng.standard_normal(1 << logn)).astype(np.complex64)
+        ffts.append((x, -1 if logn % 2 else +1))
+    srv = Server(max_inflight_batches=4, max_batch_requests=16)
+    try:
+        outs, results = run_mixed(srv, convs, ffts)
+        stats = srv.stats()
+    finally:
+        srv.stop()
+    for (s, f), out in zip(convs, outs[:len(convs)]):
+        assert rel(out, oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))) < 1e-6
+    for (x, d), out in zip(ffts, outs[len(convs):]):
+        assert oracle.rel_l2(out[None], oracle.fft(x[None], d))[0] < 2e-6
+    assert all(r.status == 0 and r.latency_us > 0 for r in results)
+    assert stats["completed"] == len(results) and stats["batches"] >= 3
+    assert max(r.batch_requests for r in results) > 1
+
+
+def test_same_result_alone_and_in_the_mix(engine):
+    from estl_gb300.serve import Server
+    convs = conv_requests(24, 3)
+    probe = convs[7]
+    srv = Server(max_inflight_batches=1, max_batch_requests=1)
+    try:
+        alone, _ = run_mixed(srv, [probe], [])
+    finally:
+        srv.stop()
+    srv = Server(max_inflight_batches=3, max_batch_requests=32)
+    try:
+        mixed, results = run_mixed(srv, convs, [])
+    finally:
+        srv.stop()
+    assert np.array_equal(alone[0], mixed[7])
+    assert results[7].batch_requests > 1
+
+
+def test_admission_budget(engine):
+    from estl_gb300 import EstlError
+    from estl_gb300.serve import Server
+    convs = conv_requests(30, 4)
+    budget = 160 << 20
+    srv = Server(hbm_budget_bytes=budget, max_inflight_batches=4, max_batch_requests=64)
+    try:
+        outs, results = run_mixed(srv, convs, [])
+        st = srv.stats()
+        assert st["max_inflight_bytes"] <= budget
+        # a request that can never fit the budget is refused at submit time
+        big = np.zeros((1 << 21) - 4096, np.float32)
+        f = np.zeros(4096, np.float32)
+        out = np.zeros(big.size + f.size - 1, np.float32)
+        tiny = Server(hbm_budget_bytes=1 << 20)
+        try:
+            with pytest.raises(EstlError) as e:
+                tiny.submit_conv(big, f, out)
+            assert e.value.name == "ESTL_ADMISSION_REJECTED"
+        finally:
+            tiny.stop()
+    finally:
+        srv.stop()
+    for (s, f), out in zip(convs, outs):
+        assert rel(out, oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))) < 1e-6
