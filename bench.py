@@ -38,6 +38,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
+    ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream"],
+                    help="plan mode for every N (auto: tuning cache / planner default)")
     ap.add_argument("--elements-log", type=int, default=27,
                     help="log2 complex elements per direction (27 = the 1 GiB sweep; smaller for ncu captures)")
     return ap.parse_args()
@@ -213,7 +215,8 @@ def main():
     plans = {}
     for logn in logns:
         n = 1 << logn
-        plans[logn] = (estl.Plan(n, TOTAL // n, estl.FORWARD), estl.Plan(n, TOTAL // n, estl.BACKWARD))
+        plans[logn] = (estl.Plan(n, TOTAL // n, estl.FORWARD, mode=args.mode),
+                       estl.Plan(n, TOTAL // n, estl.BACKWARD, mode=args.mode))
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
 

@@ -15,7 +15,7 @@ created for (size, batchCount, forward) and executed repeatedly.
 import ctypes
 import json
 
-from ._lib import BACKWARD, FORWARD, PREC_FP32, EstlError, check, lib
+from ._lib import BACKWARD, FORWARD, PREC_FP32, EstlError, PlanOptions, check, lib
 
 __all__ = ["init", "shutdown", "Plan", "fft", "autotune", "max_batch", "memory_usage", "EstlError",
            "FORWARD", "BACKWARD"]
@@ -66,11 +66,15 @@ def _stream_handle(stream):
 class Plan:
     """`batch` transforms of length n, forward (-1) or backward (+1)."""
 
-    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32):
+    MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3}
+
+    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0):
         _ensure_init()
         self.n, self.batch, self.direction = int(n), int(batch), int(direction)
         h = ctypes.c_void_p()
-        check(lib().estl_plan_create(self.n, self.batch, self.direction, int(precision), ctypes.byref(h)))
+        opts = PlanOptions(self.MODES[mode] if isinstance(mode, str) else int(mode), int(lag), int(chunk))
+        check(lib().estl_plan_create_ex(self.n, self.batch, self.direction, int(precision), ctypes.byref(opts),
+                                        ctypes.byref(h)))
         self._h = h
 
     @property
@@ -81,6 +85,10 @@ class Plan:
         buf = ctypes.create_string_buffer(2048)
         check(lib().estl_plan_describe(self._h, buf, len(buf)))
         return json.loads(buf.value.decode())
+
+    def check(self):
+        """Synchronise; raise if a streamed kernel's dependency wait gave up."""
+        check(lib().estl_plan_check(self._h))
 
     @property
     def launches(self):

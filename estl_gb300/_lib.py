@@ -48,9 +48,11 @@ SIGNATURES = {
     "estl_status_string": (ctypes.c_char_p, [_INT]),
     "estl_max_batch": (_I64, [_I64]),
     "estl_plan_create": (_INT, [_I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
+    "estl_plan_create_ex": (_INT, [_I64, _I64, _INT, _INT, _P, ctypes.POINTER(_P)]),
     "estl_plan_destroy": (_INT, [_P]),
     "estl_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_plan_launches": (_I64, [_P]),
+    "estl_plan_check": (_INT, [_P]),
     "estl_execute": (_INT, [_P, _P, _P, _P]),
     "estl_execute_host": (_INT, [_P, _P, _P]),
     "estl_plan_set_profiling": (_INT, [_P, _INT]),
@@ -106,6 +108,11 @@ class ServeStats(ctypes.Structure):
 
 REQ_FFT = 0
 REQ_CONV = 1
+
+
+class PlanOptions(ctypes.Structure):
+    """estl_plan_options: mode 0 auto, 1 single tile, 2 four-step, 3 streamed four-step."""
+    _fields_ = [("mode", ctypes.c_int), ("lag", ctypes.c_int), ("chunk", ctypes.c_int64)]
 
 
 class ConvRequest(ctypes.Structure):

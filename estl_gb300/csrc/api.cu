@@ -155,9 +155,15 @@ static estl_status lookup_kernel(const Step& st, const KernelDesc** out) {
 }
 
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const StreamAux* aux) {
   Engine& E = engine();
   for (const Step& st : plan.steps) {
+    if (st.kind == STEP_STREAM) {
+      if (!aux) return fail(ESTL_DEVICE_ERROR, "streamed step without a work list");
+      estl_status s = launch_stream(st, in, out, scratch, plan.scratch_elems, *aux, sgn, stream);
+      if (s != ESTL_OK) return s;
+      continue;
+    }
     const cf32* src = st.src == BUF_IN ? in : (st.src == BUF_SCRATCH ? scratch : out);
     cf32* dst = st.dst == BUF_OUT ? out : scratch;
     if (st.kind == STEP_COPY) {
@@ -200,6 +206,9 @@ struct estl_plan_s {
   int direction = ESTL_FORWARD;
   cf32* scratch = nullptr;
   size_t scratch_bytes = 0;
+  void* aux = nullptr;  // streamed plans: work list and counters
+  size_t aux_bytes = 0;
+  StreamAux saux{};
   std::mutex mu;
   cudaEvent_t done = nullptr;  // last execute of this plan (scratch reuse order)
   bool done_recorded = false;
@@ -212,6 +221,9 @@ struct estl_plan_s {
   size_t stage_bytes = 0;
   cudaStream_t st[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_h2d[2] = {}, ev_comp[2] = {}, ev_d2h[2] = {};
+  void* host_aux[2] = {nullptr, nullptr};  // streamed plans: work lists of the chunk plans
+  size_t host_aux_bytes[2] = {0, 0};
+  StreamAux host_saux[2] = {};
   // per-launch profiling (estl_plan_set_profiling)
   bool profiling = false;
   struct Rec {
@@ -231,6 +243,8 @@ static std::unordered_set<estl_plan> g_plans;
 static void plan_release(estl_plan p) {
   if (!p) return;
   dev_free(p->scratch, p->scratch_bytes);
+  dev_free(p->aux, p->aux_bytes);
+  for (int s = 0; s < 2; ++s) dev_free(p->host_aux[s], p->host_aux_bytes[s]);
   for (int s = 0; s < 2; ++s) {
     dev_free(p->din[s], p->stage_bytes);
     dev_free(p->dout[s], p->stage_bytes);
@@ -338,7 +352,23 @@ int64_t estl_max_batch(int64_t n) {
   return b > INT32_MAX ? INT32_MAX : b;
 }
 
+static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int precision,
+                                    const estl_plan_options* opt, estl_plan* plan);
+
 estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precision, estl_plan* plan) {
+  return plan_create_impl(n, batch, direction, precision, nullptr, plan);
+}
+
+estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
+                                const estl_plan_options* options, estl_plan* plan) {
+  if (options && (options->mode < 0 || options->mode > 3 || options->lag < 0 || options->chunk < 0))
+    return fail(ESTL_INVALID_ARG, "bad plan options (mode %d, lag %d, chunk %lld)", options->mode, options->lag,
+                (long long)options->chunk);
+  return plan_create_impl(n, batch, direction, precision, options, plan);
+}
+
+static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int precision,
+                                    const estl_plan_options* opt, estl_plan* plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "plan output pointer is NULL");
   *plan = nullptr;
   estl_status s = require_init();
@@ -352,10 +382,18 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
     return fail(ESTL_UNSUPPORTED_SIZE, "transform length %lld is not a power of two in [1, 2^%d]", (long long)n,
                 kMaxLogN);
   PlanChoice choice;
-  tuner_lookup(n, batch, &choice);
+  if (opt && opt->mode != 0) {
+    choice.mode = opt->mode;
+    choice.lag = opt->lag;
+    choice.chunk = opt->chunk;
+  } else {
+    tuner_lookup(n, batch, &choice);
+  }
   std::unique_ptr<estl_plan_s> p(new estl_plan_s);
   std::string err;
-  if (!make_plan(n, batch, choice, &p->layout, &err)) {
+  if (opt && opt->mode != 0) {
+    if (!make_plan(n, batch, choice, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  } else if (!make_plan(n, batch, choice, &p->layout, &err)) {
     // a stale tuning entry must not make a valid size fail: fall back to defaults
     if (!make_plan(n, batch, PlanChoice{}, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   }
@@ -364,6 +402,15 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
   p->scratch_bytes = (size_t)p->layout.scratch_elems * sizeof(cf32);
   s = dev_alloc((void**)&p->scratch, p->scratch_bytes, "plan scratch");
   if (s != ESTL_OK) return s;
+  p->aux_bytes = stream_aux_bytes(p->layout);
+  if (p->aux_bytes) {
+    s = dev_alloc(&p->aux, p->aux_bytes, "stream work list");
+    if (s == ESTL_OK) s = stream_prepare(p->layout, p->aux, p->aux_bytes, &p->saux);
+    if (s != ESTL_OK) {
+      plan_release(p.release());
+      return s;
+    }
+  }
   s = check_cuda(cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming), "cudaEventCreate");
   if (s != ESTL_OK) {
     plan_release(p.release());
@@ -393,6 +440,24 @@ estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len) {
   if (!plan || !buf || len == 0) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
   std::string d = plan->layout.describe();
   std::snprintf(buf, len, "%s", d.c_str());
+  return ESTL_OK;
+}
+
+estl_status estl_plan_check(estl_plan plan) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  estl_status s = check_cuda(cudaDeviceSynchronize(), "plan execute");
+  if (s != ESTL_OK) return s;
+  const StreamAux* auxes[3] = {&plan->saux, &plan->host_saux[0], &plan->host_saux[1]};
+  for (const StreamAux* a : auxes) {
+    if (!a->error) continue;
+    int e = 0;
+    s = check_cuda(cudaMemcpy(&e, a->error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+    if (s != ESTL_OK) return s;
+    if (e) {
+      cudaMemset(a->error, 0, sizeof(int));
+      return fail(ESTL_TIMEOUT, "a dependency wait of the streamed kernel gave up");
+    }
+  }
   return ESTL_OK;
 }
 
@@ -433,7 +498,8 @@ static estl_status resolve_profile(estl_plan p) {
   return ESTL_OK;
 }
 
-static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const cf32* in, cf32* out, cudaStream_t stream) {
+static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
+                                   cudaStream_t stream) {
   if (p->pending.size() > 65536) {
     estl_status s = resolve_profile(p);
     if (s != ESTL_OK) return s;
@@ -445,7 +511,7 @@ static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const cf32
     estl_status s = pool_event(p, &r.a);
     if (s == ESTL_OK) s = pool_event(p, &r.b);
     if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.a, stream), "cudaEventRecord");
-    if (s == ESTL_OK) s = launch_steps(one, in, out, p->scratch, p->sgn, stream);
+    if (s == ESTL_OK) s = launch_steps(one, in, out, p->scratch, p->sgn, stream, aux);
     if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.b, stream), "cudaEventRecord");
     if (s != ESTL_OK) return s;
     p->pending.push_back(r);
@@ -453,7 +519,8 @@ static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const cf32
   return ESTL_OK;
 }
 
-static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const cf32* in, cf32* out, cudaStream_t stream) {
+static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
+                               cudaStream_t stream) {
   std::lock_guard<std::mutex> g(plan->mu);
   estl_status s;
   if (plan->done_recorded) {
@@ -461,9 +528,9 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const cf32*
     if (s != ESTL_OK) return s;
   }
   if (plan->profiling)
-    s = launch_profiled(plan, layout, in, out, stream);
+    s = launch_profiled(plan, layout, aux, in, out, stream);
   else
-    s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream);
+    s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream, aux);
   if (s != ESTL_OK) return s;
   s = check_cuda(cudaEventRecord(plan->done, stream), "cudaEventRecord");
   if (s != ESTL_OK) return s;
@@ -477,7 +544,7 @@ estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* st
   if (s != ESTL_OK) return s;
   s = check_buffers(d_in, d_out);
   if (s != ESTL_OK) return s;
-  return run_plan_on(plan, plan->layout, (const cf32*)d_in, (cf32*)d_out, (cudaStream_t)stream);
+  return run_plan_on(plan, plan->layout, &plan->saux, (const cf32*)d_in, (cf32*)d_out, (cudaStream_t)stream);
 }
 
 static estl_status host_pipeline_setup(estl_plan p) {
@@ -495,6 +562,15 @@ static estl_status host_pipeline_setup(estl_plan p) {
     return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   if ((size_t)p->host_plan_full.scratch_elems * sizeof(cf32) > p->scratch_bytes)
     return fail(ESTL_DEVICE_ERROR, "chunk plan needs more scratch than the plan holds");
+  const Plan1D* chunk_plans[2] = {&p->host_plan_full, tail ? &p->host_plan_tail : nullptr};
+  for (int k = 0; k < 2; ++k) {
+    if (!chunk_plans[k]) continue;
+    p->host_aux_bytes[k] = stream_aux_bytes(*chunk_plans[k]);
+    if (!p->host_aux_bytes[k]) continue;
+    estl_status s2 = dev_alloc(&p->host_aux[k], p->host_aux_bytes[k], "stream work list");
+    if (s2 == ESTL_OK) s2 = stream_prepare(*chunk_plans[k], p->host_aux[k], p->host_aux_bytes[k], &p->host_saux[k]);
+    if (s2 != ESTL_OK) return s2;
+  }
   p->stage_bytes = (size_t)(chunk * n) * sizeof(cf32);
   estl_status s;
   for (int i = 0; i < 2; ++i) {
@@ -532,6 +608,7 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
     const long long b0 = i * chunk, cnt = std::min(chunk, batch - b0);
     const size_t bytes = (size_t)(cnt * n) * sizeof(cf32);
     const Plan1D& lay = cnt == chunk ? plan->host_plan_full : plan->host_plan_tail;
+    const StreamAux* aux = cnt == chunk ? &plan->host_saux[0] : &plan->host_saux[1];
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sh, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaMemcpyAsync(plan->din[k], h_in + 2 * b0 * n, bytes, cudaMemcpyHostToDevice, sh),
                         "cudaMemcpyAsync(H2D)")) != ESTL_OK)
@@ -539,7 +616,7 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
     if ((s = check_cuda(cudaEventRecord(plan->ev_h2d[k], sh), "record")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_h2d[k], 0), "wait")) != ESTL_OK) return s;
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_d2h[k], 0), "wait")) != ESTL_OK) return s;
-    if ((s = run_plan_on(plan, lay, plan->din[k], plan->dout[k], sc)) != ESTL_OK) return s;
+    if ((s = run_plan_on(plan, lay, aux, plan->din[k], plan->dout[k], sc)) != ESTL_OK) return s;
     if ((s = check_cuda(cudaEventRecord(plan->ev_comp[k], sc), "record")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaStreamWaitEvent(sd, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaMemcpyAsync(h_out + 2 * b0 * n, plan->dout[k], bytes, cudaMemcpyDeviceToHost, sd),

@@ -16,6 +16,7 @@
 
 #include "../../include/estl_cuda.h"
 #include "fft_core.cuh"
+#include "packed_plan.h"
 #include "planner.h"
 
 namespace estl {
@@ -42,9 +43,25 @@ estl_status require_init();
 estl_status dev_alloc(void** p, size_t bytes, const char* what);
 void dev_free(void* p, size_t bytes);
 
+// Device work list and counters of a streamed four-step plan.
+struct StreamAux {
+  PackedItem* items;
+  long long nitems;
+  unsigned int* counters;  // [0] work counter, then column and row counts per transform
+  size_t counter_bytes;
+  int* error;              // set when a dependency wait gave up
+};
+
+size_t stream_aux_bytes(const Plan1D& plan);
+// Builds the work list of a streamed plan into `aux` (device memory).
+estl_status stream_prepare(const Plan1D& plan, void* aux, size_t aux_bytes, StreamAux* out);
+estl_status launch_stream(const Step& st, const cf32* in, cf32* out, cf32* scratch, long long scratch_elems,
+                          const StreamAux& aux, float sgn, cudaStream_t stream);
+
 // Launches one plan's steps on `stream`.  in/out/scratch are device
-// pointers of interleaved complex64; sgn = +1 forward, -1 backward.
+// pointers of interleaved complex64; sgn = +1 forward, -1 backward.  aux is
+// the work list of a streamed plan (else unused).
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream);
+                         cudaStream_t stream, const StreamAux* aux = nullptr);
 
 }  // namespace estl

@@ -60,6 +60,16 @@ const std::vector<TileCfg>& tile_configs() {
   return v;
 }
 
+const StreamCfg* find_stream_cfg(int logn) {
+  static const StreamCfg table[] = {
+#define ESTL_XS(LOGN, CM, CE, CC, RM, RE, RC) {LOGN, CM, CE, CC, RM, RE, RC},
+#include "stream_list.inc"
+  };
+  for (const StreamCfg& c : table)
+    if (c.logn == logn) return &c;
+  return nullptr;
+}
+
 const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc) {
   for (const TileCfg& c : tile_configs())
     if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc) return &c;
@@ -111,6 +121,32 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
 
   int mode = choice.mode;
   if (mode == 0) mode = (logn <= kSingleMaxLog) ? 1 : 2;
+
+  if (mode == 3) {
+    const StreamCfg* sc = find_stream_cfg(logn);
+    if (!sc) {
+      set_err(err, "no streamed four-step configuration for log2 n = %lld", logn);
+      return false;
+    }
+    const int logn1 = logn - sc->cm, logn2 = sc->cm;
+    const long long ncol = 1LL << (logn1 - sc->cc), nrow = 1LL << (logn2 - sc->rc);
+    // lag: enough tiles between a transform's last column tile and its first
+    // row tile for ~1000 CTAs (every resident CTA of a GB300) to drain
+    int lag = choice.lag > 0 ? choice.lag : (int)std::max(1LL, (1024 + ncol + nrow - 1) / (ncol + nrow));
+    lag = (int)std::min<long long>(lag, batch);
+    Step s{STEP_STREAM, sc->cm, sc->ce, 4, sc->cc, 1, BUF_IN, BUF_OUT, 0, total, 0, total, batch, logn};
+    s.rlogm = sc->rm;
+    s.rloge = sc->re;
+    s.rlogc = sc->rc;
+    s.lag = lag;
+    s.ring = (int)std::min<long long>(batch, lag + 2);
+    p.steps.push_back(s);
+    p.scratch_elems = (long long)s.ring * n;
+    p.aux_items = batch * (ncol + nrow);
+    p.hbm_passes = 2;
+    *out = p;
+    return true;
+  }
 
   if (mode == 1) {
     if (logn > kSingleMaxLog) {
@@ -189,6 +225,14 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       out.push_back(ch);
     }
   }
+  if (find_stream_cfg(logn)) {
+    for (int lag : {0, 1, 2, 4, 8}) {
+      PlanChoice ch;
+      ch.mode = 3;
+      ch.lag = lag;
+      out.push_back(ch);
+    }
+  }
   if (logn >= 14) {
     for (int logn2 = 7; logn2 <= 12; ++logn2) {
       int logn1 = logn - logn2;
@@ -222,7 +266,7 @@ std::string Plan1D::describe() const {
   std::snprintf(buf, sizeof buf, "{\"n\": %lld, \"batch\": %lld, \"hbm_passes\": %d, \"launches\": %zu, \"scratch_bytes\": %lld, \"kernels\": [",
                 n, batch, hbm_passes, steps.size(), scratch_elems * 8);
   s += buf;
-  const char* names[] = {"single", "col", "row", "copy"};
+  const char* names[] = {"single", "col", "row", "copy", "stream"};
   int shown = 0;
   for (size_t i = 0; i < steps.size() && shown < 2; ++i, ++shown) {
     const Step& st = steps[i];

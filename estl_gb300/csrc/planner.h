@@ -16,7 +16,7 @@
 
 namespace estl {
 
-enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3 };
+enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_STREAM = 4 };
 enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_SCRATCH = 2 };
 
 struct TileCfg {
@@ -37,19 +37,30 @@ struct Step {
   int src, dst;
   long long src_off, src_len;  // complex elements
   long long dst_off, dst_len;
-  long long rows;  // STEP_SINGLE: transforms; STEP_COPY: elements
+  long long rows;  // STEP_SINGLE / STEP_STREAM: transforms; STEP_COPY: elements
   int logn;
+  // STEP_STREAM: row tile (the column tile is logm/loge/logc above), queue lag
+  // and scratch ring (transforms)
+  int rlogm = 0, rloge = 0, rlogc = 0;
+  int lag = 0, ring = 0;
 };
+
+// Streamed four-step configuration of a length (stream_list.inc), or nullptr.
+struct StreamCfg {
+  int logn, cm, ce, cc, rm, re, rc;
+};
+const StreamCfg* find_stream_cfg(int logn);
 
 // Tunable plan parameters (what the autotuner searches).  Zero / -1 fields
 // mean "planner default".
 struct PlanChoice {
-  int mode = 0;  // 0 default, 1 single kernel, 2 four-step
+  int mode = 0;  // 0 default, 1 single kernel, 2 four-step, 3 streamed four-step
   int single_loge = -1, single_logc = -1;
   int logn2 = -1;  // four-step: log2 N2 (column DFT length)
   int col_loge = -1, col_logc = -1;
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
+  int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
 };
 
 struct Plan1D {
@@ -58,11 +69,13 @@ struct Plan1D {
   PlanChoice choice;
   std::vector<Step> steps;
   long long scratch_elems = 0;
+  long long aux_items = 0;  // STEP_STREAM: work items (the plan uploads them)
   int hbm_passes = 0;
   std::string describe() const;  // one-line JSON
 };
 
 constexpr int kSingleMaxLog = 14;
+constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;
 
 // Returns false (with *err set) when n is not a power of two in [1, 2^24] or

@@ -168,11 +168,24 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
   const Plan1D* best = nullptr;
   std::vector<std::pair<double, const Plan1D*>> timed;
   for (const Plan1D& p : plans) {
-    s = launch_steps(p, in, out, scr, 1.f, st);
-    if (s != ESTL_OK) continue;
-    launch_steps(p, in, out, scr, 1.f, st);
+    void* aux = nullptr;
+    const size_t aux_bytes = stream_aux_bytes(p);
+    StreamAux saux{};
+    if (aux_bytes) {
+      if (dev_alloc(&aux, aux_bytes, "autotune work list") != ESTL_OK) continue;
+      if (stream_prepare(p, aux, aux_bytes, &saux) != ESTL_OK) {
+        dev_free(aux, aux_bytes);
+        continue;
+      }
+    }
+    s = launch_steps(p, in, out, scr, 1.f, st, &saux);
+    if (s != ESTL_OK) {
+      dev_free(aux, aux_bytes);
+      continue;
+    }
+    launch_steps(p, in, out, scr, 1.f, st, &saux);
     cudaEventRecord(e0, st);
-    for (int i = 0; i < iters; ++i) launch_steps(p, in, out, scr, 1.f, st);
+    for (int i = 0; i < iters; ++i) launch_steps(p, in, out, scr, 1.f, st, &saux);
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) {
       s = check_cuda(cudaGetLastError(), "autotune run");
@@ -181,6 +194,10 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= iters;
+    int stream_error = 0;
+    if (saux.error) cudaMemcpy(&stream_error, saux.error, sizeof(int), cudaMemcpyDeviceToHost);
+    dev_free(aux, aux_bytes);
+    if (stream_error) continue;  // a dependency wait gave up: not a usable configuration
     timed.push_back({ms, &p});
     if (ms < best_ms) {
       best_ms = ms;

@@ -74,12 +74,33 @@ int64_t estl_max_batch(int64_t n);
  * (n, batch). */
 estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precision, estl_plan* plan);
 
+/* Explicit plan shape (what estl_autotune searches).  mode: 0 automatic
+ * (tuning cache, else defaults), 1 single-tile kernel (n <= 2^14),
+ * 2 four-step as a column launch and a row launch per chunk of transforms
+ * (two HBM round trips), 3 streamed four-step: one persistent launch whose
+ * column and row tiles share a scratch ring small enough to stay in L2.
+ * lag (mode 3): transforms between a column tile and the row tiles that read
+ * it (0 = default).  chunk (mode 2): transforms per launch pair (0 = default). */
+typedef struct estl_plan_options {
+  int mode;
+  int lag;
+  int64_t chunk;
+} estl_plan_options;
+
+estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
+                                const estl_plan_options* options, estl_plan* plan);
+
 /* Free the plan and its device buffers (FFT_OpenCL_Contiguous.h:186-191). */
 estl_status estl_plan_destroy(estl_plan plan);
 
 /* One-line JSON description of the plan: launches, HBM passes, tile kernels,
  * scratch bytes.  Writes at most len bytes including the terminator. */
 estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len);
+
+/* Waits for the device; returns ESTL_TIMEOUT if a dependency wait inside a
+ * streamed plan's persistent kernel gave up since the last check (the
+ * outputs of that execute are then incomplete), else ESTL_OK. */
+estl_status estl_plan_check(estl_plan plan);
 
 /* Number of kernel launches (and device copies) one execute issues. */
 int64_t estl_plan_launches(estl_plan plan);

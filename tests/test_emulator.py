@@ -27,20 +27,20 @@ def emu_run(emu, n, batch, x, sign=-1, choice=None):
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 9)(*choice)
+        ch = (ctypes.c_int * 10)(*(list(choice) + [0] * (10 - len(choice))))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (9 * 4096))()
+    buf = (ctypes.c_int * (10 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[9 * i: 9 * i + 9]) for i in range(min(k, 4096))]
+    return [list(buf[10 * i: 10 * i + 10]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 9)(*choice) if choice is not None else None
+    ch = (ctypes.c_int * 10)(*(list(choice) + [0] * (10 - len(choice)))) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())
@@ -79,10 +79,13 @@ def test_every_four_step_config(emu, logn):
     n = 1 << logn
     cands = [c for c in candidates(emu, n, 2) if c[0] == 2]
     assert cands
+    assert any(c[0] == 3 for c in candidates(emu, n, 2))
     x = rand_c64((3, n), logn)
     ref = oracle.fft(x, +1)
     seen = set()
     for c in cands:
+        if c[0] != 2:
+            continue
         key = tuple(c[:8])
         if key in seen:
             continue
@@ -92,6 +95,21 @@ def test_every_four_step_config(emu, logn):
         rc, msg, y = emu_run(emu, n, 3, x, +1, c)
         assert rc == 0, (c, msg)
         assert oracle.rel_l2(y, ref).max() < TOL, c
+
+
+@pytest.mark.parametrize("logn", range(13, 19))
+def test_streamed_four_step(emu, logn):
+    """The persistent streamed kernel with a scratch ring shorter than the
+    batch: ring slots are reused, so column tiles wait for row tiles."""
+    n = 1 << logn
+    batch = 6
+    x = rand_c64((batch, n), 40 + logn)
+    for lag, sign in ((1, -1), (2, +1)):
+        rc, msg, y = emu_run(emu, n, batch, x, sign, [3, -1, -1, -1, -1, -1, -1, -1, 0, lag])
+        assert rc == 0, (lag, msg)
+        assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL
+    d = describe(emu, n, batch, [3, -1, -1, -1, -1, -1, -1, -1, 0, 1])
+    assert d["kernels"][0]["kind"] == "stream" and d["scratch_bytes"] == 3 * 8 * n
 
 
 @pytest.mark.parametrize("logn", [18, 20])
