@@ -37,6 +37,8 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other benchmark configurations (4096x256, uneven batch, served convolution)")
     ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
     ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream"],
                     help="plan mode for every N (auto: tuning cache / planner default)")
@@ -154,6 +156,169 @@ def cpu_baseline_sample(logns, threads, budget_s=20.0):
     desc = (f"FP32 restatement of FFT_OpenCL_Contiguous (radix-16 Stockham, runtime twiddles), {threads} threads; "
             f"N=2^{done[0]}..2^{done[-1]}, max(2^22, N) complex per size, forward+backward")
     return tot_bytes / tot_s / 1e9, desc
+
+
+def bench_config1(estl, torch):
+    """N = 4096, batch = 256 (8 MiB, L2-sized): a CUDA graph of 64 executes over
+    32 rotating buffer pairs (512 MiB, larger than L2), forward, plus the
+    rel-L2 error of one batch against the oracle."""
+    import numpy as np
+
+    import oracle
+    n, batch, rot, reps = 4096, 256, 32, 64
+    rng = np.random.default_rng(1)
+    x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
+    xs = [torch.from_numpy(x).cuda() for _ in range(rot)]
+    ys = [torch.empty_like(xs[0]) for _ in range(rot)]
+    plan = estl.Plan(n, batch, estl.FORWARD)
+    y0 = plan.execute(xs[0]).cpu().numpy()
+    err = float(oracle.rel_l2(y0, oracle.fft(x, -1)).max())
+    plan.close()
+    plan = estl.Plan(n, batch, estl.FORWARD)  # fresh plan: its first ordering event is recorded inside the graph
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        for i in range(reps):
+            plan.execute_ptr(xs[i % rot].data_ptr(), ys[i % rot].data_ptr(), s.cuda_stream)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / (10 * reps)
+    return {"workload": "C2C FP32 forward, N=4096, batch=256, uniform[-1,1) seed 1",
+            "method": "CUDA graph of 64 executes over 32 rotating buffer pairs (512 MiB > L2)",
+            "us_per_transform_batch": round(1e3 * ms, 3), "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1),
+            "gflops": round(5 * n * 12 * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": err}
+
+
+def bench_uneven(estl, torch):
+    """8192 transforms, lengths log-uniform over 2^6..2^16, complex N(0,1),
+    seed 3, packed with an offsets array: one persistent launch vs one launch
+    per size class (both replayed as CUDA graphs)."""
+    import ctypes
+
+    import numpy as np
+
+    from estl_gb300._lib import check, lib
+    rng = np.random.default_rng(3)
+    e = rng.integers(6, 17, 8192)
+    sizes = (1 << e).astype(np.int64)
+    offsets = np.zeros(8192, np.int64)
+    offsets[1:] = np.cumsum(sizes[:-1])
+    total = int(sizes.sum())
+    x = torch.randn(total, dtype=torch.complex64, device="cuda")
+    y = torch.empty_like(x)
+    L = lib()
+    res = {"workload": "8192 C2C FP32 transforms, N log-uniform 2^6..2^16, packed, N(0,1) seed 3",
+           "elements": total}
+    for mode, name in ((0, "persistent"), (1, "per_size")):
+        plan = ctypes.c_void_p()
+        check(L.estl_packed_plan_create(offsets.ctypes.data, sizes.ctypes.data, 8192, -1, mode, ctypes.byref(plan)))
+        st = torch.cuda.current_stream().cuda_stream
+        for _ in range(3):
+            check(L.estl_packed_execute(plan, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                        ctypes.c_void_p(st)))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            check(L.estl_packed_execute(plan, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                        ctypes.c_void_p(st)))
+        e1.record()
+        torch.cuda.synchronize()
+        check(L.estl_packed_check(plan))
+        ms = e0.elapsed_time(e1) / 10
+        buf = ctypes.create_string_buffer(1024)
+        check(L.estl_packed_plan_describe(plan, buf, len(buf)))
+        d = json.loads(buf.value.decode())
+        res[name] = {"ms": round(ms, 4), "gbs": round(16 * total / (ms * 1e-3) / 1e9, 1),
+                     "gflops": round(d["flops"] / (ms * 1e-3) / 1e9, 1), "launches": d["launches"]}
+        L.estl_packed_plan_destroy(plan)
+    res["persistent_speedup"] = round(res["per_size"]["ms"] / res["persistent"]["ms"], 3)
+    return res
+
+
+def bench_served_conv(estl, torch, count=600):
+    """Served FFT convolution: real signals of length log-uniform 2^8..2^20 with
+    filters of length log-uniform 2^4..2^12, both N(0,1), seed 5, pinned host
+    buffers, HBM admission budget 64 GiB.  Saturation throughput and Poisson
+    arrivals at 50% / 90% of it, batched server vs plain per-request (one
+    request at a time), plus rel-L2 of sampled outputs against the oracle."""
+    import threading
+
+    import numpy as np
+
+    import oracle
+    from estl_gb300.serve import Server
+    rng = np.random.default_rng(5)
+    reqs = []
+    for _ in range(count):
+        Ls = int(2 ** rng.uniform(8, 20))
+        K = int(2 ** rng.uniform(4, 12))
+        s = torch.from_numpy(rng.standard_normal(Ls).astype(np.float32)).pin_memory().numpy()
+        f = torch.from_numpy(rng.standard_normal(K).astype(np.float32)).pin_memory().numpy()
+        o = torch.empty(Ls + K - 1, dtype=torch.float32).pin_memory().numpy()
+        reqs.append((s, f, o))
+
+    def run(srv, rate):
+        """rate None: submit everything at once; else Poisson arrivals (req/s)."""
+        tickets = [None] * count
+        lat = [0.0] * count
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, count)) if rate else np.zeros(count)
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, (s, f, o) in enumerate(reqs):
+                if rate:
+                    d = t0 + arrivals[i] - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                tickets[i] = srv.submit_conv(s, f, o)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        for i in range(count):
+            while tickets[i] is None:
+                time.sleep(1e-5)
+            r = srv.poll(tickets[i])
+            lat[i] = r.latency_us
+        th.join()
+        t = time.perf_counter() - t0
+        lat = np.sort(np.array(lat))
+        return {"req_per_s": round(count / t, 1), "p50_ms": round(lat[len(lat) // 2] / 1e3, 3),
+                "p99_ms": round(lat[int(0.99 * (len(lat) - 1))] / 1e3, 3)}
+
+    out = {"workload": f"{count} FFT-convolution requests, signal log-uniform 2^8..2^20, filter 2^4..2^12, "
+                       "N(0,1) seed 5, pinned host buffers", "hbm_budget_gib": 64}
+    for name, kw in (("batched", dict(max_inflight_batches=4, max_batch_requests=64)),
+                     ("per_request", dict(max_inflight_batches=1, max_batch_requests=1))):
+        srv = Server(hbm_budget_bytes=64 << 30, **kw)
+        try:
+            run(srv, None)  # warm-up: plans, kernels, memory pool
+            sat = run(srv, None)
+            res = {"saturated": sat}
+            for frac in (0.5, 0.9):
+                res[f"poisson_{int(frac * 100)}pct"] = dict(run(srv, frac * sat["req_per_s"]),
+                                                            rate=round(frac * sat["req_per_s"], 1))
+            res["stats"] = {k: v for k, v in srv.stats().items() if k in ("batches", "max_batch_requests",
+                                                                             "max_inflight_bytes")}
+        finally:
+            srv.stop()
+        out[name] = res
+    out["batched_vs_per_request"] = round(out["batched"]["saturated"]["req_per_s"] /
+                                          out["per_request"]["saturated"]["req_per_s"], 2)
+    errs = []
+    for i in range(0, count, count // 6):
+        s, f, o = reqs[i]
+        errs.append(float(np.sqrt(np.sum((o - oracle.conv_fft(s, f)) ** 2) /
+                                  np.sum(oracle.conv_fft(s, f) ** 2))))
+    out["rel_l2_max_sampled"] = max(errs)
+    return out
 
 
 def run_reference(args):
@@ -335,6 +500,15 @@ def main():
                "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
                "path": "estl_execute_host (C ABI), pinned host buffers, chunked H2D/compute/D2H pipeline"}
 
+    configs = {}
+    if rank == 0 and not args.no_configs:
+        for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
+                        ("served_conv", bench_served_conv)):
+            try:
+                configs[key] = fn(estl, torch)
+            except Exception as ex:  # reported, never silently dropped
+                configs[key] = {"error": f"{type(ex).__name__}: {ex}"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -358,6 +532,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -115,7 +115,7 @@ class Plan:
         check(lib().estl_execute_host(self._h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(out.ctypes.data)))
         return out
 
-    KERNEL_KINDS = ("single", "col", "row", "copy")
+    KERNEL_KINDS = ("single", "col", "row", "copy", "stream")
 
     def set_profiling(self, enable=True):
         """Bracket every launch with CUDA events (per-kernel timers)."""
@@ -123,9 +123,10 @@ class Plan:
 
     def kernel_stats(self):
         """{kind: (launches, total_ms, algorithmic_bytes)} of profiled launches."""
-        L = (ctypes.c_int64 * 4)()
-        T = (ctypes.c_double * 4)()
-        B = (ctypes.c_double * 4)()
+        k = len(self.KERNEL_KINDS)
+        L = (ctypes.c_int64 * k)()
+        T = (ctypes.c_double * k)()
+        B = (ctypes.c_double * k)()
         check(lib().estl_plan_kernel_stats(self._h, L, T, B))
         return {k: (int(L[i]), float(T[i]), float(B[i])) for i, k in enumerate(self.KERNEL_KINDS) if L[i]}
 

@@ -233,8 +233,8 @@ struct estl_plan_s {
   };
   std::vector<Rec> pending;
   std::vector<cudaEvent_t> event_pool;
-  long long prof_launches[4] = {0, 0, 0, 0};
-  double prof_ms[4] = {0, 0, 0, 0}, prof_bytes[4] = {0, 0, 0, 0};
+  long long prof_launches[kStepKinds] = {};
+  double prof_ms[kStepKinds] = {}, prof_bytes[kStepKinds] = {};
 };
 
 static std::mutex g_plans_mu;
@@ -633,7 +633,7 @@ estl_status estl_plan_set_profiling(estl_plan plan, int enable) {
   estl_status s = resolve_profile(plan);
   if (s != ESTL_OK) return s;
   plan->profiling = enable != 0;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kStepKinds; ++k) {
     plan->prof_launches[k] = 0;
     plan->prof_ms[k] = 0;
     plan->prof_bytes[k] = 0;
@@ -646,7 +646,7 @@ estl_status estl_plan_kernel_stats(estl_plan plan, int64_t* launches, double* to
   std::lock_guard<std::mutex> g(plan->mu);
   estl_status s = resolve_profile(plan);
   if (s != ESTL_OK) return s;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kStepKinds; ++k) {
     if (launches) launches[k] = plan->prof_launches[k];
     if (total_ms) total_ms[k] = plan->prof_ms[k];
     if (bytes) bytes[k] = plan->prof_bytes[k];

@@ -17,6 +17,7 @@
 namespace estl {
 
 enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_STREAM = 4 };
+constexpr int kStepKinds = 5;
 enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_SCRATCH = 2 };
 
 struct TileCfg {

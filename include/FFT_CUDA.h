@@ -123,11 +123,12 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
     if (describe.find("\"col\"") != std::string::npos) kinds.push_back(1);
     if (describe.find("\"row\"") != std::string::npos) kinds.push_back(2);
     if (describe.find("\"copy\"") != std::string::npos) kinds.push_back(3);
+    if (describe.find("\"stream\"") != std::string::npos) kinds.push_back(4);
     kernelTimers.resize(kinds.size());
     const size_t bytes = sizeof(D) * 2 * (size_t)this->size * this->batchCount;
     registered = estl_host_register(arrays->in->getData(), bytes) == ESTL_OK &&
                  estl_host_register(arrays->out->getData(), bytes) == ESTL_OK;
-    for (int k = 0; k < 4; ++k) lastMs[k] = 0;
+    for (int k = 0; k < ESTL_KERNEL_KINDS; ++k) lastMs[k] = 0;
   }
 
   virtual double getTotalComputationFlops(int kernel) {
@@ -138,15 +139,15 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
   }
 
   virtual std::string getKernelInfo(int kernel) {
-    static const char* names[] = {"tile", "column", "row", "copy"};
+    static const char* names[] = {"tile", "column", "row", "copy", "streamed four-step"};
     return (kernel >= 0 && kernel < (int)kinds.size()) ? names[kinds[kernel]] : "";
   }
 
   /* FFT<D>::execute: the result is in the data interface's output array. */
   virtual void execute() {
     estlCheck(estl_execute_host(plan, arrays->in->getData(), arrays->out->getData()), "estl_execute_host");
-    int64_t launches[4];
-    double ms[4], bytes[4];
+    int64_t launches[ESTL_KERNEL_KINDS];
+    double ms[ESTL_KERNEL_KINDS], bytes[ESTL_KERNEL_KINDS];
     estlCheck(estl_plan_kernel_stats(plan, launches, ms, bytes), "estl_plan_kernel_stats");
     double total = 0;
     for (size_t i = 0; i < kinds.size(); ++i) {
@@ -154,7 +155,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
       kernelTimers[i].addRun(1e-3 * d);
       total += d;
     }
-    for (int k = 0; k < 4; ++k) lastMs[k] = ms[k];
+    for (int k = 0; k < ESTL_KERNEL_KINDS; ++k) lastMs[k] = ms[k];
     if (timerComputation) timerComputation->addRun(1e-3 * total);
   }
 
@@ -174,7 +175,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
   bool registered;
   std::string describe;
   std::vector<int> kinds;
-  double lastMs[4];
+  double lastMs[ESTL_KERNEL_KINDS];
 };
 
 #endif  // FFT_CUDA_H

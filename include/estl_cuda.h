@@ -133,9 +133,11 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out);
 estl_status estl_plan_set_profiling(estl_plan plan, int enable);
 
 /* Per kernel kind (index 0 single-tile, 1 column pass, 2 row pass, 3 device
- * copy): launches, summed device milliseconds and summed algorithmic bytes
- * (16 bytes per complex element read and written).  Waits for the profiled
- * launches to finish.  Arrays have 4 entries; any may be NULL. */
+ * copy, 4 streamed four-step): launches, summed device milliseconds and
+ * summed algorithmic bytes (16 bytes per complex element read and written).
+ * Waits for the profiled launches to finish.  Arrays have ESTL_KERNEL_KINDS
+ * entries; any may be NULL. */
+#define ESTL_KERNEL_KINDS 5
 estl_status estl_plan_kernel_stats(estl_plan plan, int64_t* launches, double* total_ms, double* bytes);
 
 /* Page-lock / unlock host memory for estl_execute_host. */
