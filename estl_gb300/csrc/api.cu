@@ -34,10 +34,11 @@ estl_status ok() { return ESTL_OK; }
 
 estl_status check_cuda(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return ESTL_OK;
-  if (e == cudaErrorMemoryAllocation) {
-    cudaGetLastError();
-    return fail(ESTL_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
-  }
+  // The error is reported through the status code; clear the runtime's
+  // last-error slot so that the caller's next CUDA call (or another library's)
+  // does not trip over an error this call already handled.
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation) return fail(ESTL_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
   return fail(ESTL_DEVICE_ERROR, "%s: %s", what, cudaGetErrorString(e));
 }
 
@@ -111,6 +112,7 @@ __global__ void bank_init_kernel(cf32* bank) {
 struct KernelTable {
   std::vector<KernelDesc> descs;
   std::vector<char> attr_set;
+  std::vector<int> resident;  // pipelined kernels: CTAs resident on the device
 };
 
 static KernelTable& ktable() {
@@ -124,6 +126,7 @@ static KernelTable& ktable() {
     n = registry_row(&d);
     k.descs.insert(k.descs.end(), d, d + n);
     k.attr_set.assign(k.descs.size(), 0);
+    k.resident.assign(k.descs.size(), 0);
     return k;
   }();
   return t;
@@ -131,11 +134,12 @@ static KernelTable& ktable() {
 
 static std::mutex g_attr_mu;
 
-static estl_status lookup_kernel(const Step& st, const KernelDesc** out) {
+static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** out, int* resident = nullptr) {
   KernelTable& kt = ktable();
   for (size_t i = 0; i < kt.descs.size(); ++i) {
     const KernelDesc& d = kt.descs[i];
-    if (d.kind == st.kind && d.logm == st.logm && d.loge == st.loge && d.logr == st.logr && d.logc == st.logc) {
+    if (d.kind == st.kind && d.logm == st.logm && d.loge == st.loge && d.logr == st.logr && d.logc == st.logc &&
+        d.pipe == pipe) {
       if (!kt.attr_set[i]) {
         std::lock_guard<std::mutex> g(g_attr_mu);
         if (!kt.attr_set[i]) {
@@ -143,10 +147,16 @@ static estl_status lookup_kernel(const Step& st, const KernelDesc** out) {
               cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem_bytes),
               "cudaFuncSetAttribute(max dynamic shared memory)");
           if (s != ESTL_OK) return s;
+          int per_sm = 0;
+          s = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, d.fn, d.nthreads, d.smem_bytes),
+                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+          if (s != ESTL_OK) return s;
+          kt.resident[i] = std::max(1, per_sm) * engine().num_sms;
           kt.attr_set[i] = 1;
         }
       }
       *out = &d;
+      if (resident) *resident = kt.resident[i];
       return ESTL_OK;
     }
   }
@@ -173,10 +183,15 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
       if (s != ESTL_OK) return s;
       continue;
     }
+    // pipelined kernels move 16-byte chunks: they need 16-byte aligned data
+    const bool aligned = !(((uintptr_t)(src + st.src_off) | (uintptr_t)(dst + st.dst_off)) & 15);
+    const int pipe = (st.pipe && aligned) ? 1 : 0;
     const KernelDesc* d = nullptr;
-    estl_status s = lookup_kernel(st, &d);
+    int resident = 0;
+    estl_status s = lookup_kernel(st, pipe, &d, &resident);
     if (s != ESTL_OK) return s;
     if (st.grid < 1 || st.grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "grid of %lld CTAs", st.grid);
+    const long long grid = pipe ? std::min<long long>(st.grid, resident) : st.grid;
     TileArgs a;
     a.in = Ptr<const cf32>{src + st.src_off, st.src_len};
     a.out = Ptr<cf32>{dst + st.dst_off, st.dst_len};
@@ -185,8 +200,9 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.logn = st.logn;
     a.logn1 = 0;
     a.sgn = sgn;
+    a.grid = grid;
     void* args[] = {&a};
-    s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)st.grid), dim3(d->nthreads), args, d->smem_bytes, stream),
+    s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel");
     if (s != ESTL_OK) return s;
   }
@@ -431,7 +447,10 @@ estl_status estl_plan_destroy(estl_plan plan) {
     std::lock_guard<std::mutex> g(g_plans_mu);
     if (!g_plans.erase(plan)) return fail(ESTL_INVALID_ARG, "unknown plan handle");
   }
-  if (plan->done_recorded) cudaEventSynchronize(plan->done);
+  // wait for the plan's last execute (an event last recorded inside a stream
+  // capture has nothing to wait for here and only reports an error, which is
+  // cleared)
+  if (plan->done_recorded && cudaEventSynchronize(plan->done) != cudaSuccess) cudaGetLastError();
   plan_release(plan);
   return ESTL_OK;
 }

@@ -392,6 +392,7 @@ struct TileArgs {
   int logn;        // log2 of the full transform length
   int logn1;       // four-step: log2 N1 (N = N1 * N2)
   float sgn;       // +1 forward; -1 = backward via conj(FFT(conj(x)))
+  long long grid;  // CTAs launched (grid-stride kernels of pipe_core.cuh)
 };
 
 ESTL_HD cf32 conj_if(cf32 v, float sgn) { return {v.x, v.y * sgn}; }

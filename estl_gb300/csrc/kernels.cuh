@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "fft_core.cuh"
+#include "pipe_core.cuh"
 
 namespace estl {
 
@@ -15,6 +16,7 @@ struct KernelDesc {
   int nthreads;
   int smem_bytes;
   const void* fn;
+  int pipe;  // grid-stride, cp.async double-buffered variant (pipe_core.cuh)
 };
 
 template <class K>
@@ -24,14 +26,19 @@ __global__ void __launch_bounds__(K::NT, min_blocks(K::NT, K::TL::E)) tile_kerne
 }
 
 template <class K>
-KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc) {
+KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc, int pipe = 0) {
   return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
-                    reinterpret_cast<const void*>(&tile_kernel<K>)};
+                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe};
 }
+
+constexpr long long kMaxSmemBytes = 227 * 1024;
 
 #define ESTL_SINGLE(M, E, R, C) make_desc<SingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C)
 #define ESTL_COL(M, E, R, C) make_desc<ColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
 #define ESTL_ROW(M, E, R, C) make_desc<RowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C)
+#define ESTL_PIPE_SINGLE(M, E, R, C) make_desc<PipeSingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C, 1)
+#define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
+#define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
 
 // Per translation unit tables (kernels_*.cu).
 int registry_single(const KernelDesc** out);

@@ -1,10 +1,22 @@
 // Registry of the col tile FFT kernels listed in kernel_list.inc.
 #include "kernels.cuh"
 
+// every pipelined variant must fit the shared memory of one SM
+#define ESTL_X_PIPE_SINGLE(M, E, R, C) \
+  static_assert(PipeSingleKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
+#define ESTL_X_PIPE_COL(M, E, R, C) \
+  static_assert(PipeColKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
+#define ESTL_X_PIPE_ROW(M, E, R, C) \
+  static_assert(PipeRowKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
+namespace estl {
+#include "kernel_list.inc"
+}
+
 namespace estl {
 
 static const KernelDesc kTable[] = {
 #define ESTL_X_COL(M, E, R, C) ESTL_COL(M, E, R, C),
+#define ESTL_X_PIPE_COL(M, E, R, C) ESTL_PIPE_COL(M, E, R, C),
 #include "kernel_list.inc"
 };
 

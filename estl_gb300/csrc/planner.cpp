@@ -5,14 +5,15 @@
 #include <cstdio>
 
 #include "fft_core.cuh"
+#include "pipe_core.cuh"
 
 namespace estl {
 
 namespace {
 
 template <class K>
-TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc) {
-  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32))};
+TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc, int pipe = 0) {
+  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32)), pipe};
 }
 
 std::vector<TileCfg> build_configs() {
@@ -20,6 +21,9 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_SINGLE(M, E, R, C) v.push_back(cfg_of<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
 #define ESTL_X_COL(M, E, R, C) v.push_back(cfg_of<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
 #define ESTL_X_ROW(M, E, R, C) v.push_back(cfg_of<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
+#define ESTL_X_PIPE_SINGLE(M, E, R, C) v.push_back(cfg_of<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
+#define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
+#define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #include "kernel_list.inc"
   return v;
 }
@@ -31,7 +35,7 @@ std::vector<TileCfg> build_configs() {
 const TileCfg* default_single(int logm) {
   const TileCfg* best = nullptr;
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != STEP_SINGLE || c.logm != logm) continue;
+    if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe) continue;
     if (c.loge != std::min(4, logm)) continue;
     if (!best || std::abs(c.nthreads - 256) < std::abs(best->nthreads - 256)) best = &c;
   }
@@ -41,13 +45,13 @@ const TileCfg* default_single(int logm) {
 const TileCfg* default_pass(int kind, int logm, int max_logc) {
   const TileCfg* best = nullptr;
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > max_logc) continue;
+    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > max_logc || c.pipe) continue;
     if (c.nthreads > 512) continue;
     if (!best || c.logc > best->logc) best = &c;
   }
   if (!best)
     for (const TileCfg& c : tile_configs()) {
-      if (c.kind != kind || c.logm != logm || c.logc > max_logc) continue;
+      if (c.kind != kind || c.logm != logm || c.logc > max_logc || c.pipe) continue;
       if (!best || c.nthreads < best->nthreads) best = &c;
     }
   return best;
@@ -70,10 +74,17 @@ const StreamCfg* find_stream_cfg(int logn) {
   return nullptr;
 }
 
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc) {
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe) {
   for (const TileCfg& c : tile_configs())
-    if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc) return &c;
+    if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc && c.pipe == pipe)
+      return &c;
   return nullptr;
+}
+
+// Whether a step of this configuration runs as its pipelined variant.
+static int use_pipe(const PlanChoice& ch, const TileCfg* c) {
+  if (ch.pipe == 0) return 0;
+  return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, 1) ? 1 : 0;
 }
 
 int ilog2_exact(long long n) {
@@ -165,6 +176,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     const long long per = 1LL << c->logc;
     Step s{STEP_SINGLE, c->logm, c->loge, c->logr, c->logc, (batch + per - 1) / per, BUF_IN, BUF_OUT,
            0, total, 0, total, batch, logn};
+    s.pipe = use_pipe(choice, c);
     p.steps.push_back(s);
     p.hbm_passes = 1;
     *out = p;
@@ -201,6 +213,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
            b0 * n, cnt * n, 0, cnt * n, cnt, logn};
     Step b{STEP_ROW, row->logm, row->loge, row->logr, row->logc, cnt << (logn2 - row->logc), BUF_SCRATCH, BUF_OUT,
            0, cnt * n, b0 * n, cnt * n, cnt, logn};
+    a.pipe = use_pipe(choice, col);
+    b.pipe = use_pipe(choice, row);
     p.steps.push_back(a);
     p.steps.push_back(b);
   }
@@ -222,6 +236,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       ch.mode = 1;
       ch.single_loge = c.loge;
       ch.single_logc = c.logc;
+      ch.pipe = c.pipe;
       out.push_back(ch);
     }
   }
@@ -238,10 +253,11 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       int logn1 = logn - logn2;
       if (logn1 < 7 || logn1 > 12) continue;
       for (const TileCfg& c : tile_configs()) {
-        if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1) continue;
+        if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1 || c.pipe) continue;
         for (const TileCfg& r : tile_configs()) {
-          if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2) continue;
-          for (long long chunk : {0LL, 4LL << 20, 16LL << 20, 64LL << 20}) {
+          if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe) continue;
+          for (long long chunk : {0LL, 16LL << 20, 64LL << 20}) {
+           for (int pipe : {0, -1}) {
             PlanChoice ch;
             ch.mode = 2;
             ch.logn2 = logn2;
@@ -250,7 +266,9 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
             ch.row_loge = r.loge;
             ch.row_logc = r.logc;
             ch.chunk = chunk == 0 ? 0 : std::max(1LL, chunk / n);
+            ch.pipe = pipe;
             out.push_back(ch);
+           }
           }
         }
       }
@@ -270,8 +288,9 @@ std::string Plan1D::describe() const {
   int shown = 0;
   for (size_t i = 0; i < steps.size() && shown < 2; ++i, ++shown) {
     const Step& st = steps[i];
-    std::snprintf(buf, sizeof buf, "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"grid\": %lld}",
-                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid);
+    std::snprintf(buf, sizeof buf,
+                  "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"tiles\": %lld, \"pipe\": %d}",
+                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe);
     s += buf;
   }
   s += "]}";

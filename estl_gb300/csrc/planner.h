@@ -25,11 +25,12 @@ struct TileCfg {
   int logm, loge, logr, logc;
   int nthreads;
   int smem_bytes;
+  int pipe;  // pipelined (grid-stride, cp.async double-buffered) variant
 };
 
 // All instantiated tile kernels (kernel_list.inc).
 const std::vector<TileCfg>& tile_configs();
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc);
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe = 0);
 
 struct Step {
   int kind;
@@ -44,6 +45,8 @@ struct Step {
   // and scratch ring (transforms)
   int rlogm = 0, rloge = 0, rlogc = 0;
   int lag = 0, ring = 0;
+  // pipelined variant (grid = tiles; the launcher runs min(tiles, resident CTAs))
+  int pipe = 0;
 };
 
 // Streamed four-step configuration of a length (stream_list.inc), or nullptr.
@@ -62,6 +65,7 @@ struct PlanChoice {
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
   int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
+  int pipe = -1;        // tile kernels: -1 pipelined variant where one exists, 0 plain, 1 pipelined
 };
 
 struct Plan1D {

@@ -70,11 +70,12 @@ std::string tuner_cache_path() {
 }
 
 std::string choice_to_json(const PlanChoice& c) {
-  char buf[320];
+  char buf[400];
   std::snprintf(buf, sizeof buf,
                 "{\"mode\": %d, \"single_loge\": %d, \"single_logc\": %d, \"logn2\": %d, \"col_loge\": %d, "
-                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld}",
-                c.mode, c.single_loge, c.single_logc, c.logn2, c.col_loge, c.col_logc, c.row_loge, c.row_logc, c.chunk);
+                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"lag\": %d, \"pipe\": %d}",
+                c.mode, c.single_loge, c.single_logc, c.logn2, c.col_loge, c.col_logc, c.row_loge, c.row_logc, c.chunk,
+                c.lag, c.pipe);
   return buf;
 }
 
@@ -99,6 +100,8 @@ void tuner_load_cache() {
     e.choice.row_loge = (int)json_int(line, "row_loge", -1);
     e.choice.row_logc = (int)json_int(line, "row_logc", -1);
     e.choice.chunk = json_int(line, "chunk", 0);
+    e.choice.lag = (int)json_int(line, "lag", 0);
+    e.choice.pipe = (int)json_int(line, "pipe", -1);
     g_cache[{gpu, n, bb}] = e;  // later lines win
   }
 }

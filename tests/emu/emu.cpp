@@ -6,8 +6,11 @@
 // std::barrier, and every global / shared / twiddle access is bounds checked.
 // A CPU test can therefore prove that a kernel configuration stays in bounds
 // and computes the right transform before it is launched on a GPU.
-#include <barrier>
+#include <ucontext.h>
+
 #include <cmath>
+#include <condition_variable>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -20,13 +23,13 @@
 #include "conv_plan.h"
 #include "fft_core.cuh"
 #include "packed_core.cuh"
+#include "pipe_core.cuh"
 #include "stream_core.cuh"
 #include "planner.h"
 
 using namespace estl;
 
 namespace {
-thread_local std::barrier<>* tl_bar = nullptr;
 std::mutex g_msg_mu;
 std::string g_msg;
 
@@ -35,7 +38,7 @@ struct EmuFault : std::runtime_error {
 };
 }  // namespace
 
-void estl_emu_sync() { tl_bar->arrive_and_wait(); }
+void estl_emu_sync();
 
 void estl_emu_fail(const char* what, long long idx, long long n) {
   char buf[256];
@@ -54,11 +57,12 @@ struct EmuKernel {
   int kind, logm, loge, logr, logc, nt;
   long long smem;
   RunFn fn;
+  int pipe;
 };
 
 template <class K>
-EmuKernel mk(int kind, int m, int e, int r, int c) {
-  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run};
+EmuKernel mk(int kind, int m, int e, int r, int c, int pipe = 0) {
+  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, pipe};
 }
 
 const std::vector<EmuKernel>& emu_kernels() {
@@ -67,6 +71,9 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_SINGLE(M, E, R, C) k.push_back(mk<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
 #define ESTL_X_COL(M, E, R, C) k.push_back(mk<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
 #define ESTL_X_ROW(M, E, R, C) k.push_back(mk<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
+#define ESTL_X_PIPE_SINGLE(M, E, R, C) k.push_back(mk<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
+#define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
+#define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #include "kernel_list.inc"
     return k;
   }();
@@ -101,36 +108,93 @@ const std::vector<cf32>& host_bank() {
   return b;
 }
 
-bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
-  std::barrier<> bar(k.nt);
-  std::vector<cf32> smem((size_t)std::max<long long>(k.smem, 1));
+// The threads of one emulated CTA are fibers (ucontext coroutines) on the
+// calling host thread: a barrier is a yield to a round-robin scheduler that
+// resumes every fiber once per round, so all fibers reach each barrier before
+// any passes it.  No OS threads, no futexes.
+struct FiberSched {
+  std::vector<ucontext_t> ctx;
+  std::vector<std::vector<char>> stacks;
+  std::vector<char> done;
+  ucontext_t main;
+  int current = 0;
+  const std::function<void(int)>* body = nullptr;
+};
+thread_local FiberSched* tl_sched = nullptr;
+constexpr size_t kFiberStack = 256 * 1024;
+
+void fiber_entry() {
+  FiberSched* s = tl_sched;
+  const int tid = s->current;
+  (*s->body)(tid);
+  s->done[tid] = 1;
+  // returning resumes uc_link (the scheduler)
+}
+
+void run_fibers(int nt, const std::function<void(int)>& body) {
+  static thread_local FiberSched sched;
+  FiberSched& s = sched;
+  if ((int)s.stacks.size() < nt) {
+    s.stacks.resize(nt);
+    for (auto& st : s.stacks)
+      if (st.empty()) st.resize(kFiberStack);
+  }
+  s.ctx.assign(nt, ucontext_t{});
+  s.done.assign(nt, 0);
+  s.body = &body;
+  tl_sched = &s;
+  for (int t = 0; t < nt; ++t) {
+    getcontext(&s.ctx[t]);
+    s.ctx[t].uc_stack.ss_sp = s.stacks[t].data();
+    s.ctx[t].uc_stack.ss_size = kFiberStack;
+    s.ctx[t].uc_link = &s.main;
+    makecontext(&s.ctx[t], fiber_entry, 0);
+  }
+  for (;;) {
+    bool any = false;
+    for (int t = 0; t < nt; ++t) {
+      if (s.done[t]) continue;
+      any = true;
+      s.current = t;
+      swapcontext(&s.main, &s.ctx[t]);
+    }
+    if (!any) break;
+  }
+  tl_sched = nullptr;
+}
+
+template <class Fn, class Args>
+bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
+  std::vector<cf32> smem((size_t)std::max<long long>(smem_elems, 1));
   const float nan = std::numeric_limits<float>::quiet_NaN();
-  for (auto& e : smem) e = cf32{nan, nan};
-  std::atomic<bool> failed{false};
-  std::vector<std::thread> th;
-  th.reserve(k.nt);
-  for (int tid = 0; tid < k.nt; ++tid) {
-    th.emplace_back([&, tid] {
-      tl_bar = &bar;
+  bool failed = false;
+  for (long long cta = 0; cta < grid && !failed; ++cta) {
+    // poison shared memory so that a read of a slot this CTA never wrote
+    // shows up as NaN in the output
+    for (auto& e : smem) e = cf32{nan, nan};
+    std::function<void(int)> body = [&](int tid) {
       try {
-        for (long long cta = 0; cta < grid; ++cta) {
-          k.fn(a, cta, tid, smem.data());
-          estl_emu_sync();
-          // poison shared memory between CTAs so that a read of a slot the
-          // current CTA never wrote shows up as NaN in the output
-          if (tid == 0)
-            for (auto& e : smem) e = cf32{nan, nan};
-          estl_emu_sync();
-        }
+        fn(a, cta, tid, smem.data());
       } catch (const EmuFault&) {
         failed = true;
-        bar.arrive_and_drop();
       }
-    });
+    };
+    run_fibers(nt, body);
   }
-  for (auto& t : th) t.join();
   return !failed;
 }
+
+bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) { return run_generic(k.nt, k.smem, k.fn, a, grid); }
+
+}  // namespace
+
+// __syncthreads of an emulated thread: yield to the CTA's scheduler.
+void estl_emu_sync() {
+  FiberSched* s = tl_sched;
+  swapcontext(&s->ctx[s->current], &s->main);
+}
+
+namespace {
 
 // ---- convolution kernels ----
 using ConvFn = void (*)(const ConvArgs&, long long, int, cf32*);
@@ -189,36 +253,6 @@ const std::vector<EmuStreamKernel>& emu_stream_kernels() {
   return v;
 }
 
-template <class Fn, class Args>
-bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
-  std::barrier<> bar(nt);
-  std::vector<cf32> smem((size_t)std::max<long long>(smem_elems, 1));
-  const float nan = std::numeric_limits<float>::quiet_NaN();
-  for (auto& e : smem) e = cf32{nan, nan};
-  std::atomic<bool> failed{false};
-  std::vector<std::thread> th;
-  th.reserve(nt);
-  for (int tid = 0; tid < nt; ++tid) {
-    th.emplace_back([&, tid] {
-      tl_bar = &bar;
-      try {
-        for (long long cta = 0; cta < grid; ++cta) {
-          fn(a, cta, tid, smem.data());
-          estl_emu_sync();
-          if (tid == 0)
-            for (auto& e : smem) e = cf32{nan, nan};
-          estl_emu_sync();
-        }
-      } catch (const EmuFault&) {
-        failed = true;
-        bar.arrive_and_drop();
-      }
-    });
-  }
-  for (auto& t : th) t.join();
-  return !failed;
-}
-
 void set_err(char* err, int len, const std::string& s) {
   if (err && len > 0) std::snprintf(err, (size_t)len, "%s", s.c_str());
 }
@@ -236,6 +270,7 @@ PlanChoice choice_from(const int* f) {
   c.row_logc = f[7];
   c.chunk = f[8];
   c.lag = f[9];
+  c.pipe = f[10];
   return c;
 }
 
@@ -244,7 +279,7 @@ PlanChoice choice_from(const int* f) {
 extern "C" {
 
 // Runs the plan for (n, batch) on interleaved complex64 host data.
-// choice: 10 ints (PlanChoice fields) or NULL for the planner default.
+// choice: 11 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
 int emu_plan_run(long long n, long long batch, const int* choice, int sign, const float* in, float* out, char* err,
@@ -321,7 +356,9 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     }
     const EmuKernel* k = nullptr;
     for (const EmuKernel& c : emu_kernels())
-      if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc) k = &c;
+      if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc &&
+          c.pipe == st.pipe)
+        k = &c;
     if (!k) {
       set_err(err, errlen, "no emulated kernel for a plan step");
       return 3;
@@ -334,7 +371,11 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     a.logn = st.logn;
     a.logn1 = 0;
     a.sgn = sign < 0 ? 1.f : -1.f;
-    if (!run_kernel(*k, a, st.grid)) {
+    // pipelined kernels are grid-stride: emulate a few CTAs so that every CTA
+    // loops over several tiles and both tile buffers
+    const long long grid = k->pipe ? std::min<long long>(st.grid, 3) : st.grid;
+    a.grid = grid;
+    if (!run_kernel(*k, a, grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
       set_err(err, errlen, g_msg);
       return 1;
@@ -356,13 +397,13 @@ int emu_plan_describe(long long n, long long batch, const int* choice, char* buf
 }
 
 // Candidate choices of the autotuner for (n, batch): writes up to max rows
-// of 10 ints, returns the number of candidates.
+// of 11 ints, returns the number of candidates.
 int emu_plan_candidates(long long n, long long batch, int* out, int max) {
   std::vector<PlanChoice> c = plan_candidates(n, batch);
   int k = 0;
   for (const PlanChoice& ch : c) {
     if (k >= max) break;
-    int* f = out + 10 * k++;
+    int* f = out + 11 * k++;
     f[0] = ch.mode;
     f[1] = ch.single_loge;
     f[2] = ch.single_logc;
@@ -373,6 +414,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[7] = ch.row_logc;
     f[8] = (int)ch.chunk;
     f[9] = ch.lag;
+    f[10] = ch.pipe;
   }
   return (int)c.size();
 }

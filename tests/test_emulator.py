@@ -22,25 +22,36 @@ def rand_c64(shape, seed):
     return (rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)).astype(np.complex64)
 
 
+def pad_choice(choice):
+    """PlanChoice fields: mode, single_loge, single_logc, logn2, col_loge,
+    col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available)."""
+    c = list(choice)
+    if len(c) < 10:
+        c += [0] * (10 - len(c))
+    if len(c) < 11:
+        c.append(-1)
+    return c
+
+
 def emu_run(emu, n, batch, x, sign=-1, choice=None):
     y = np.full((batch, n), np.nan + 1j * np.nan, dtype=np.complex64)
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 10)(*(list(choice) + [0] * (10 - len(choice))))
+        ch = (ctypes.c_int * 11)(*pad_choice(choice))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (10 * 4096))()
+    buf = (ctypes.c_int * (11 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[10 * i: 10 * i + 10]) for i in range(min(k, 4096))]
+    return [list(buf[11 * i: 11 * i + 11]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 10)(*(list(choice) + [0] * (10 - len(choice)))) if choice is not None else None
+    ch = (ctypes.c_int * 11)(*pad_choice(choice)) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())
@@ -73,26 +84,27 @@ def test_every_single_kernel_config(emu, logn):
         assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < TOL, c
 
 
-@pytest.mark.parametrize("logn", [14, 15, 16, 17])
+@pytest.mark.parametrize("logn", [14, 16, 19])
 def test_every_four_step_config(emu, logn):
-    """All column/row tile pairs the autotuner may pick, with chunking."""
+    """Every column tile and every row tile the autotuner may pick (each at
+    least once, plain and pipelined), with a chunk of two transforms."""
     n = 1 << logn
     cands = [c for c in candidates(emu, n, 2) if c[0] == 2]
     assert cands
     assert any(c[0] == 3 for c in candidates(emu, n, 2))
-    x = rand_c64((3, n), logn)
+    x = rand_c64((2, n), logn)
     ref = oracle.fft(x, +1)
-    seen = set()
+    seen_col, seen_row = set(), set()
     for c in cands:
-        if c[0] != 2:
+        col = (c[3], c[4], c[5], c[10])
+        row = (c[3], c[6], c[7], c[10])
+        if col in seen_col and row in seen_row:
             continue
-        key = tuple(c[:8])
-        if key in seen:
-            continue
-        seen.add(key)
+        seen_col.add(col)
+        seen_row.add(row)
         c = list(c)
-        c[8] = 2  # chunk of two transforms: exercises the chunk loop with a tail
-        rc, msg, y = emu_run(emu, n, 3, x, +1, c)
+        c[8] = 1  # one transform per chunk: exercises the chunk loop
+        rc, msg, y = emu_run(emu, n, 2, x, +1, c)
         assert rc == 0, (c, msg)
         assert oracle.rel_l2(y, ref).max() < TOL, c
 
