@@ -14,18 +14,23 @@
 // cp.async moves 16 bytes (two complex64), so these kernels need 16-byte
 // aligned transform data; the launcher uses the plain kernels otherwise.
 #pragma once
+#include <stdint.h>
+
 #include <cstring>
 
 #include "fft_core.cuh"
 
 namespace estl {
 
-// 16-byte async copy global -> shared (bounds checked by the emulator).
+// 16-byte async copy global -> shared.  Both addresses must be 16-byte
+// aligned (the emulator checks bounds and alignment).
 ESTL_HD void cp_async16(const Ptr<cf32>& sm, long long sidx, const Ptr<const cf32>& g, long long gidx) {
   ESTL_CHECK(sidx + 1, sm.n, "cp.async shared destination");
   ESTL_CHECK(gidx + 1, g.n, "cp.async global source");
   ESTL_CHECK(sidx, sm.n, "cp.async shared destination");
   ESTL_CHECK(gidx, g.n, "cp.async global source");
+  ESTL_CHECK((long long)((uintptr_t)(sm.p + sidx) & 15), 1, "cp.async shared destination alignment (16 B)");
+  ESTL_CHECK((long long)((uintptr_t)(g.p + gidx) & 15), 1, "cp.async global source alignment (16 B)");
 #if defined(__CUDA_ARCH__)
   const unsigned s = (unsigned)__cvta_generic_to_shared(sm.p + sidx);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(g.p + gidx) : "memory");
@@ -78,7 +83,8 @@ struct PipeSingleKernel {
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int TILE = C * TL::M;
-  static constexpr long long TILE_BUF = (Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE;
+  // each buffer a multiple of 16 bytes, so that the second one stays aligned
+  static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
   static_assert(TL::M >= 2 && (TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
@@ -126,7 +132,8 @@ struct PipeColKernel {
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int TILE = C * TL::M;
-  static constexpr long long TILE_BUF = (Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE;
+  // each buffer a multiple of 16 bytes, so that the second one stays aligned
+  static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
   static_assert(C >= 2 && (TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
@@ -185,7 +192,8 @@ struct PipeRowKernel {
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int TILE = C * TL::M;
-  static constexpr long long TILE_BUF = (Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE;
+  // each buffer a multiple of 16 bytes, so that the second one stays aligned
+  static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
   static_assert((TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 

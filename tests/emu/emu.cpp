@@ -165,7 +165,16 @@ void run_fibers(int nt, const std::function<void(int)>& body) {
 
 template <class Fn, class Args>
 bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
-  std::vector<cf32> smem((size_t)std::max<long long>(smem_elems, 1));
+  // shared memory base 256-byte aligned, like the device's dynamic shared memory
+  std::vector<cf32> smem_store((size_t)std::max<long long>(smem_elems, 1) + 32);
+  cf32* smem_base = reinterpret_cast<cf32*>(((uintptr_t)smem_store.data() + 255) & ~(uintptr_t)255);
+  struct View {
+    cf32* p;
+    size_t n;
+    cf32* begin() { return p; }
+    cf32* end() { return p + n; }
+    cf32* data() { return p; }
+  } smem{smem_base, (size_t)std::max<long long>(smem_elems, 1)};
   const float nan = std::numeric_limits<float>::quiet_NaN();
   bool failed = false;
   for (long long cta = 0; cta < grid && !failed; ++cta) {
@@ -371,9 +380,9 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     a.logn = st.logn;
     a.logn1 = 0;
     a.sgn = sign < 0 ? 1.f : -1.f;
-    // pipelined kernels are grid-stride: emulate a few CTAs so that every CTA
-    // loops over several tiles and both tile buffers
-    const long long grid = k->pipe ? std::min<long long>(st.grid, 3) : st.grid;
+    // pipelined kernels are grid-stride: emulate one or two CTAs so that every
+    // CTA loops over several tiles and uses both tile buffers
+    const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
     a.grid = grid;
     if (!run_kernel(*k, a, grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
