@@ -41,7 +41,9 @@ def parse():
                     help="skip the other benchmark configurations (4096x256, uneven batch, served convolution)")
     ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
     ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream"],
-                    help="plan mode for every N (auto: tuning cache / planner default)")
+                    help="plan mode for every N (auto: autotuned / tuning cache / planner default)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner pass that picks each N's plan before the timed region")
     ap.add_argument("--elements-log", type=int, default=27,
                     help="log2 complex elements per direction (27 = the 1 GiB sweep; smaller for ncu captures)")
     return ap.parse_args()
@@ -377,6 +379,12 @@ def main():
     xin = torch.view_as_complex((torch.rand((TOTAL, 2), device="cuda", generator=g) * 2 - 1).contiguous())
     yfwd = torch.empty_like(xin)
     zbwd = torch.empty_like(xin)
+    tuned = {}
+    if args.mode == "auto" and not args.no_autotune:
+        # the engine's autotuner picks each size's plan (cached per GPU, n, log2 batch)
+        for logn in logns:
+            r = estl.autotune(1 << logn, TOTAL >> logn, iters=3)
+            tuned[f"2^{logn}"] = {"ms": round(r["best_ms"], 4), "candidates": r["candidates"], "plan": r["plan"]}
     plans = {}
     for logn in logns:
         n = 1 << logn
@@ -464,7 +472,8 @@ def main():
         gflops = 2 * 5.0 * n * logn * (TOTAL // n) / (ms_n / 1e3) / 1e9
         passes = plans[logn][0].describe()["hbm_passes"]
         per_n_out[f"2^{logn}"] = {"gbs": round(gbs, 1), "frac": round(gbs / peak, 3), "gflops": round(gflops, 1),
-                                  "hbm_passes": passes, "actual_traffic_gbs": round(gbs * passes, 1)}
+                                  "hbm_passes": passes, "actual_traffic_gbs": round(gbs * passes, 1),
+                                  "plan": plans[logn][0].describe()["kernels"]}
 
     # end to end through the C ABI with pinned host buffers (H2D + D2H inside)
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 3))
@@ -533,6 +542,7 @@ def main():
             "clocks": clk,
             "cpu_baseline": cpu,
             "configs": configs,
+            "autotune": {"used": bool(tuned), "note": "autotuner pass before the timed region (engine API estl_autotune)"},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -28,31 +28,38 @@ std::vector<TileCfg> build_configs() {
   return v;
 }
 
-// Planner defaults: the configuration used before any autotuning.
-// Single kernel: elements/thread 16, about 256 threads per CTA.
-// Four-step: N2 = 2^floor(log2 N / 2) column DFTs, the widest column/row
-// chunk whose CTA still fits 512 threads.
+// Planner defaults: the configuration used before any autotuning, from
+// autotuner runs on a GB300 (the tuning cache overrides them per size).
+// Single kernel: 16 elements per thread and about 256 threads per CTA up to
+// 2^12; 32 elements per thread (256 / 512 threads, one transform per CTA)
+// for 2^13 and 2^14.
+// Four-step: N2 = 2^floor(log2 N / 2) column DFTs; column tiles as wide as
+// 512 threads allow; row tiles of 8 rows (N1 <= 2^9) or 4 rows (larger);
+// chunks of 2^26 elements.
 const TileCfg* default_single(int logm) {
   const TileCfg* best = nullptr;
+  const int want_e = logm >= 13 ? 5 : std::min(4, logm);
   for (const TileCfg& c : tile_configs()) {
     if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe) continue;
-    if (c.loge != std::min(4, logm)) continue;
+    if (c.loge != want_e) continue;
     if (!best || std::abs(c.nthreads - 256) < std::abs(best->nthreads - 256)) best = &c;
   }
   return best;
 }
 
-const TileCfg* default_pass(int kind, int logm, int max_logc) {
+// The widest E=16 tile of at most 512 threads whose chunk is at most
+// 2^want_logc transforms; failing that, the narrowest chunk up to 2^max_logc.
+const TileCfg* default_pass(int kind, int logm, int want_logc, int max_logc) {
   const TileCfg* best = nullptr;
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > max_logc || c.pipe) continue;
+    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > want_logc || c.pipe) continue;
     if (c.nthreads > 512) continue;
     if (!best || c.logc > best->logc) best = &c;
   }
   if (!best)
     for (const TileCfg& c : tile_configs()) {
       if (c.kind != kind || c.logm != logm || c.logc > max_logc || c.pipe) continue;
-      if (!best || c.nthreads < best->nthreads) best = &c;
+      if (!best || c.logc < best->logc || (c.logc == best->logc && c.nthreads < best->nthreads)) best = &c;
     }
   return best;
 }
@@ -191,11 +198,11 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   if (choice.col_loge >= 0)
     col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
   else
-    col = default_pass(STEP_COL, logn2, logn1);
+    col = default_pass(STEP_COL, logn2, logn1, logn1);
   if (choice.row_loge >= 0)
     row = find_tile(STEP_ROW, logn1, choice.row_loge, 4, choice.row_logc);
   else
-    row = default_pass(STEP_ROW, logn1, logn2);
+    row = default_pass(STEP_ROW, (int)logn1, std::min((int)logn2, logn1 <= 9 ? 3 : 2), (int)logn2);
   if (!col || !row) {
     set_err(err, "no four-step tiles instantiated for N1 = 2^%lld, N2 = 2^%lld", logn1, logn2);
     return false;
@@ -204,7 +211,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     set_err(err, "four-step chunk wider than the transform (N1 = 2^%lld, N2 = 2^%lld)", logn1, logn2);
     return false;
   }
-  long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (256LL << 20) / (8 * n));
+  long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (1LL << 26) / n);
   chunk = std::min(chunk, batch);
   p.scratch_elems = chunk * n;
   for (long long b0 = 0; b0 < batch; b0 += chunk) {
@@ -256,8 +263,8 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
         if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1 || c.pipe) continue;
         for (const TileCfg& r : tile_configs()) {
           if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe) continue;
-          for (long long chunk : {0LL, 16LL << 20, 64LL << 20}) {
-           for (int pipe : {0, -1}) {
+          for (long long chunk : {0LL, 16LL << 20, 128LL << 20}) {
+           for (int pipe : {0, 1}) {
             PlanChoice ch;
             ch.mode = 2;
             ch.logn2 = logn2;

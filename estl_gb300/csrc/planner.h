@@ -65,7 +65,7 @@ struct PlanChoice {
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
   int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
-  int pipe = -1;        // tile kernels: -1 pipelined variant where one exists, 0 plain, 1 pipelined
+  int pipe = 0;         // tile kernels: 0 plain, 1 pipelined variant (where one exists), -1 pipelined if any
 };
 
 struct Plan1D {

@@ -101,7 +101,7 @@ void tuner_load_cache() {
     e.choice.row_logc = (int)json_int(line, "row_logc", -1);
     e.choice.chunk = json_int(line, "chunk", 0);
     e.choice.lag = (int)json_int(line, "lag", 0);
-    e.choice.pipe = (int)json_int(line, "pipe", -1);
+    e.choice.pipe = (int)json_int(line, "pipe", 0);
     g_cache[{gpu, n, bb}] = e;  // later lines win
   }
 }
