@@ -49,6 +49,15 @@ def parse():
     return ap.parse_args()
 
 
+def compact_choice(c):
+    """Short text form of an autotuner plan choice."""
+    if c["mode"] == 1:
+        return f"single {c['single_loge']}.{c['single_logc']}"
+    kind = "stream" if c["mode"] == 3 else "four-step"
+    return (f"{kind} col {c['logn2']}.{c['col_loge']}.{c['col_logc']} row {c['row_loge']}.{c['row_logc']} "
+            f"chunk {c['chunk']} lag {c['lag']} pipe {c['pipe']}")
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -384,7 +393,8 @@ def main():
         # the engine's autotuner picks each size's plan (cached per GPU, n, log2 batch)
         for logn in logns:
             r = estl.autotune(1 << logn, TOTAL >> logn, iters=3)
-            tuned[f"2^{logn}"] = {"ms": round(r["best_ms"], 4), "candidates": r["candidates"], "plan": r["plan"]}
+            tuned[f"2^{logn}"] = {"candidates": r["candidates"],
+                                  "fastest": [[round(f["ms"], 4), compact_choice(f["choice"])] for f in r["fastest"][:3]]}
     plans = {}
     for logn in logns:
         n = 1 << logn
@@ -542,7 +552,8 @@ def main():
             "clocks": clk,
             "cpu_baseline": cpu,
             "configs": configs,
-            "autotune": {"used": bool(tuned), "note": "autotuner pass before the timed region (engine API estl_autotune)"},
+            "autotune": {"used": bool(tuned), "note": "autotuner pass before the timed region (engine API estl_autotune); "
+                         "fastest: ms per execute and plan (mode/tiles as m.e.c, chunk, lag, pipe)", "per_n": tuned},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -68,11 +68,23 @@ class Plan:
 
     MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3}
 
-    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0):
+    TILE_FIELDS = ("split_log2", "single_loge", "single_logc", "col_loge", "col_logc", "row_loge", "row_logc",
+                   "pipelined")
+
+    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0, tiles=None):
+        """tiles: optional dict of estl_plan_options tile fields (split_log2, col_loge, ...; modes
+        single / four_step), missing ones left to the planner."""
         _ensure_init()
         self.n, self.batch, self.direction = int(n), int(batch), int(direction)
         h = ctypes.c_void_p()
         opts = PlanOptions(self.MODES[mode] if isinstance(mode, str) else int(mode), int(lag), int(chunk))
+        if tiles:
+            unknown = set(tiles) - set(self.TILE_FIELDS)
+            if unknown:
+                raise EstlError(1, f"unknown tile fields {sorted(unknown)}")
+            opts.explicit_tiles = 1
+            for f in self.TILE_FIELDS:
+                setattr(opts, f, int(tiles.get(f, -1)))
         check(lib().estl_plan_create_ex(self.n, self.batch, self.direction, int(precision), ctypes.byref(opts),
                                         ctypes.byref(h)))
         self._h = h

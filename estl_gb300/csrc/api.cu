@@ -402,6 +402,16 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
     choice.mode = opt->mode;
     choice.lag = opt->lag;
     choice.chunk = opt->chunk;
+    if (opt->explicit_tiles) {
+      choice.logn2 = opt->split_log2;
+      choice.single_loge = opt->single_loge;
+      choice.single_logc = opt->single_logc;
+      choice.col_loge = opt->col_loge;
+      choice.col_logc = opt->col_logc;
+      choice.row_loge = opt->row_loge;
+      choice.row_logc = opt->row_logc;
+      choice.pipe = opt->pipelined < 0 ? 0 : opt->pipelined;
+    }
   } else {
     tuner_lookup(n, batch, &choice);
   }

@@ -238,6 +238,27 @@ ESTL_HD cf32 twiddle_n(const Ptr<const cf32>& bank, int logn, int a) {
   return cmul(lo, hi);
 }
 
+// x_r *= w^r for r = 1..15 given w, w^2, w^4 and w^8: every other power is
+// a product of at most three of them.
+ESTL_HD void apply_powers16(cf32* x, cf32 w1, cf32 w2, cf32 w4, cf32 w8) {
+  cf32 w3 = cmul(w1, w2), w5 = cmul(w1, w4), w6 = cmul(w2, w4), w7 = cmul(w3, w4);
+  x[1] = cmul(x[1], w1);
+  x[2] = cmul(x[2], w2);
+  x[3] = cmul(x[3], w3);
+  x[4] = cmul(x[4], w4);
+  x[5] = cmul(x[5], w5);
+  x[6] = cmul(x[6], w6);
+  x[7] = cmul(x[7], w7);
+  x[8] = cmul(x[8], w8);
+  x[9] = cmul(x[9], cmul(w1, w8));
+  x[10] = cmul(x[10], cmul(w2, w8));
+  x[11] = cmul(x[11], cmul(w3, w8));
+  x[12] = cmul(x[12], cmul(w4, w8));
+  x[13] = cmul(x[13], cmul(w5, w8));
+  x[14] = cmul(x[14], cmul(w6, w8));
+  x[15] = cmul(x[15], cmul(w7, w8));
+}
+
 // x_r *= w_M^{r u} for r = 1..R-1 with w_M^{u}, w_M^{2u}, w_M^{4u}, w_M^{8u}
 // loaded from the table (tw points at w_M^0) and the other powers formed by at
 // most three products.
@@ -261,23 +282,7 @@ ESTL_HD void twiddle_apply(cf32* x, const Ptr<const cf32>& tw, int u) {
     x[6] = cmul(x[6], cmul(w2, w4));
     x[7] = cmul(x[7], cmul(w3, w4));
   } else if constexpr (R == 16) {
-    cf32 w1 = ldg(tw, u), w2 = ldg(tw, 2 * u), w4 = ldg(tw, 4 * u), w8 = ldg(tw, 8 * u);
-    cf32 w3 = cmul(w1, w2), w5 = cmul(w1, w4), w6 = cmul(w2, w4), w7 = cmul(w3, w4);
-    x[1] = cmul(x[1], w1);
-    x[2] = cmul(x[2], w2);
-    x[3] = cmul(x[3], w3);
-    x[4] = cmul(x[4], w4);
-    x[5] = cmul(x[5], w5);
-    x[6] = cmul(x[6], w6);
-    x[7] = cmul(x[7], w7);
-    x[8] = cmul(x[8], w8);
-    x[9] = cmul(x[9], cmul(w1, w8));
-    x[10] = cmul(x[10], cmul(w2, w8));
-    x[11] = cmul(x[11], cmul(w3, w8));
-    x[12] = cmul(x[12], cmul(w4, w8));
-    x[13] = cmul(x[13], cmul(w5, w8));
-    x[14] = cmul(x[14], cmul(w6, w8));
-    x[15] = cmul(x[15], cmul(w7, w8));
+    apply_powers16(x, ldg(tw, u), ldg(tw, 2 * u), ldg(tw, 4 * u), ldg(tw, 8 * u));
   }
 }
 
@@ -473,15 +478,40 @@ struct ColKernel {
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
     cf32 v[TL::E];
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) v[j] = conj_if(ldcs(in, n1 + ((t + TL::T * j) << logn1)), sgn);
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    {
+      const int step = TL::T << logn1;
+      int off = n1 + (t << logn1);
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int k2 = t + TL::T * j;
-      cf32 w = twiddle_n(bank, logn, n1 * k2);
-      out[(k2 << logn1) + n1] = cmul(v[j], w);
-      if ((j & 3) == 3) schedule_fence();
+      for (int j = 0; j < TL::E; ++j, off += step) v[j] = conj_if(ldcs(in, off), sgn);
     }
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    store_twiddled(v, out, n1, t, logn, bank);
+  }
+
+  // Four-step twiddle and store: S[k2 * N1 + n1] = y[k2] * w_N^{n1 k2} for
+  // the thread's outputs k2 = t + T*j.  w_N^{n1 k2} = w_N^{n1 t} * W^j with
+  // W = w_N^{n1 T} = w_{E N1}^{n1}: one two-level table lookup for the base,
+  // four for W, W^2, W^4, W^8, and the other powers by products (instead of a
+  // scattered two-level lookup per element).
+  ESTL_HD static void store_twiddled(cf32 (&v)[TL::E], const Ptr<cf32>& out, int n1, int t, int logn,
+                                     const Ptr<const cf32>& bank) {
+    static_assert(TL::E == 16 || TL::E == 32, "column tiles hold 16 or 32 elements per thread");
+    const int logn1 = logn - LOGM;
+    const int logq = LOGE + logn1;  // W = w_{2^logq}^{n1}
+    const cf32 base = twiddle_n(bank, logn, n1 * t);
+    const cf32 w1 = twiddle_n(bank, logq, n1), w2 = twiddle_n(bank, logq, 2 * n1);
+    const cf32 w4 = twiddle_n(bank, logq, 4 * n1), w8 = twiddle_n(bank, logq, 8 * n1);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = cmul(v[j], base);
+    apply_powers16(v, w1, w2, w4, w8);
+    if constexpr (TL::E == 32) {
+      const cf32 base16 = cmul(base, twiddle_n(bank, logq, 16 * n1));
+#pragma unroll
+      for (int j = 16; j < 32; ++j) v[j] = cmul(v[j], base16);
+      apply_powers16(v + 16, w1, w2, w4, w8);
+    }
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << logn1) + n1] = v[j];
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
@@ -495,49 +525,39 @@ struct ColKernel {
 };
 
 // Four-step row pass: reads S[k2 * N1 + n1] (C contiguous rows of N1 = M),
-// runs the N1-point DFTs and writes X[k2 + N2 k1].  The rows are loaded
-// unit-stride; the results are staged in shared memory and stored
-// column-fastest so that every store moves a run of C elements.
+// runs the N1-point DFTs and writes X[k2 + N2 k1].  Threads are mapped
+// column-fastest (c = tid mod C), as in the column pass: a warp loads C runs
+// of 32/C consecutive row elements and stores runs of C consecutive outputs
+// (X[k2_0 .. k2_0 + C - 1 + N2 k1]) straight from registers, with the tile
+// exchanged through shared memory laid out [m][c].
 template <int LOGM, int LOGE, int LOGR, int LOGC>
 struct RowKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int SMEM_ELEMS = C * CS;
+  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
   static_assert(NT <= 1024, "too many threads");
-  static_assert(NT % C == 0 && (NT / C) * TL::E >= TL::M, "store remap must cover the tile");
 
   struct Sidx {
-    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+    ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
 
   // Rows k2_0 .. k2_0 + C - 1 of one transform's scratch `in` (N elements)
   // -> the transform's output `out` (N elements, X[k2 + N2 k1]).
   ESTL_HD static void body(const Ptr<cf32>& in, const Ptr<cf32>& out, int k2_0, int logn, int tid, cf32* smraw,
                            const Ptr<const cf32>& bank, float sgn) {
-    const int t = tid & (TL::T - 1);
-    const int c = tid >> TL::LOGT;
+    const int c = tid & (C - 1);
+    const int t = tid >> LOGC;
     const int logn2 = logn - LOGM;
     const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
-    const Sidx sidx{};
     cf32 v[TL::E];
     const Ptr<cf32> row = in.sub((long long)(k2_0 + c) * TL::M, TL::M);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = ldcg(row, t + TL::T * j);
-    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
-    ESTL_SYNC();
-    const int c2 = tid & (C - 1);
-    const int t2 = tid >> LOGC;
-    constexpr int T2 = NT / C;  // == TL::T
-#pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int k1 = t2 + T2 * j;
-      stcs(out, k2_0 + c2 + (k1 << logn2), conj_if(sm[sidx(c2, k1)], sgn));
-    }
+    for (int j = 0; j < TL::E; ++j) stcs(out, k2_0 + c + ((t + TL::T * j) << logn2), conj_if(v[j], sgn));
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {

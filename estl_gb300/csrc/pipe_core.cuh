@@ -169,13 +169,7 @@ struct PipeColKernel {
     for (int j = 0; j < TL::E; ++j) v[j] = conj_if(buf[(t + TL::T * j) * C + c], a.sgn);
     ESTL_SYNC();
     run_passes<TL, 0>(v, t, c, buf, tw, typename Base::Sidx{});
-    const Ptr<cf32> out = a.out.sub(f * N, N);
-#pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int k2 = t + TL::T * j;
-      out[(k2 << logn1) + n1] = cmul(v[j], twiddle_n(a.bank, a.logn, n1 * k2));
-      if ((j & 3) == 3) schedule_fence();
-    }
+    Base::store_twiddled(v, a.out.sub(f * N, N), n1, t, a.logn, a.bank);
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* sm) {
@@ -188,12 +182,17 @@ struct PipeColKernel {
 template <int LOGM, int LOGE, int LOGR, int LOGC>
 struct PipeRowKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
-  using Base = RowKernel<LOGM, LOGE, LOGR, LOGC>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int TILE = C * TL::M;
+  // row-major exchange layout (rows CS apart, conflict-free for the
+  // column-fastest remap of the stores)
+  static constexpr int CS = row_stride(TL::MP, C);
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
   // each buffer a multiple of 16 bytes, so that the second one stays aligned
-  static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
+  static constexpr long long TILE_BUF = (((C * CS > TILE) ? C * CS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
   static_assert((TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
@@ -217,7 +216,7 @@ struct PipeRowKernel {
     const long long f = tile / nblk;
     const int k2_0 = (int)(tile - f * nblk) * C;
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const typename Base::Sidx sidx{};
+    const Sidx sidx{};
     cf32 v[TL::E];
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = buf[c * TL::M + t + TL::T * j];

@@ -80,11 +80,23 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
  * (two HBM round trips), 3 streamed four-step: one persistent launch whose
  * column and row tiles share a scratch ring small enough to stay in L2.
  * lag (mode 3): transforms between a column tile and the row tiles that read
- * it (0 = default).  chunk (mode 2): transforms per launch pair (0 = default). */
+ * it (0 = default).  chunk (mode 2): transforms per launch pair (0 = default).
+ * explicit_tiles != 0 (modes 1 and 2) also fixes the tile kernels, each field
+ * -1 for the planner's choice: split_log2 = log2 N2 of N = N1 * N2 (the column
+ * DFT length), *_loge = log2 elements per thread, *_logc = log2 transforms
+ * (single) or columns / rows (four-step) per CTA, pipelined = 1 for the
+ * cp.async double-buffered variant where one exists.  A zero-initialised
+ * struct with mode = 0 is the automatic plan. */
 typedef struct estl_plan_options {
   int mode;
   int lag;
   int64_t chunk;
+  int explicit_tiles;
+  int split_log2;
+  int single_loge, single_logc;
+  int col_loge, col_logc;
+  int row_loge, row_logc;
+  int pipelined;
 } estl_plan_options;
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
