@@ -15,7 +15,8 @@ created for (size, batchCount, forward) and executed repeatedly.
 import ctypes
 import json
 
-from ._lib import BACKWARD, FORWARD, PREC_FP32, EstlError, PlanOptions, check, lib
+from ._lib import (BACKWARD, FORWARD, PREC_FP32, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, PREC_SPLIT_FP16, EstlError,
+                   PlanOptions, check, lib)
 
 __all__ = ["init", "shutdown", "Plan", "fft", "autotune", "max_batch", "memory_usage", "EstlError",
            "FORWARD", "BACKWARD"]

@@ -24,6 +24,9 @@ STATUS = {
 FORWARD = -1
 BACKWARD = +1
 PREC_FP32 = 0
+PREC_SPLIT_FP16 = 1    # fp16 hi+lo tensor-core radix-16 stages (butterflies scaled by powers of two)
+PREC_SPLIT_BF16 = 2    # bf16 hi+lo
+PREC_SPLIT_BF16X3 = 3  # bf16 hi+mid+lo
 
 
 class EstlError(RuntimeError):

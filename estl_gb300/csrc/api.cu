@@ -139,7 +139,7 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
   for (size_t i = 0; i < kt.descs.size(); ++i) {
     const KernelDesc& d = kt.descs[i];
     if (d.kind == st.kind && d.logm == st.logm && d.loge == st.loge && d.logr == st.logr && d.logc == st.logc &&
-        d.pipe == pipe) {
+        d.pipe == pipe && d.tc == st.tc) {
       if (!kt.attr_set[i]) {
         std::lock_guard<std::mutex> g(g_attr_mu);
         if (!kt.attr_set[i]) {
@@ -201,6 +201,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.logn1 = 0;
     a.sgn = sgn;
     a.grid = grid;
+    a.split = st.tc ? plan.choice.split : SPLIT_NONE;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel");
@@ -391,7 +392,8 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
   if (s != ESTL_OK) return s;
   if (direction != ESTL_FORWARD && direction != ESTL_BACKWARD)
     return fail(ESTL_INVALID_ARG, "direction must be ESTL_FORWARD (-1) or ESTL_BACKWARD (+1), got %d", direction);
-  if (precision != ESTL_PREC_FP32) return fail(ESTL_INVALID_ARG, "unknown precision %d", precision);
+  if (precision < ESTL_PREC_FP32 || precision > ESTL_PREC_SPLIT_BF16X3)
+    return fail(ESTL_INVALID_ARG, "unknown precision %d", precision);
   if (batch < 1) return fail(ESTL_INVALID_ARG, "batch must be >= 1 (got %lld)", (long long)batch);
   int logn = ilog2_exact(n);
   if (logn < 0 || logn > kMaxLogN)
@@ -413,15 +415,18 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
       choice.pipe = opt->pipelined < 0 ? 0 : opt->pipelined;
     }
   } else {
-    tuner_lookup(n, batch, &choice);
+    if (precision == ESTL_PREC_FP32) tuner_lookup(n, batch, &choice);
   }
+  choice.split = precision;  // ESTL_PREC_SPLIT_* == SplitKind
   std::unique_ptr<estl_plan_s> p(new estl_plan_s);
   std::string err;
   if (opt && opt->mode != 0) {
     if (!make_plan(n, batch, choice, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   } else if (!make_plan(n, batch, choice, &p->layout, &err)) {
     // a stale tuning entry must not make a valid size fail: fall back to defaults
-    if (!make_plan(n, batch, PlanChoice{}, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+    PlanChoice dflt;
+    dflt.split = precision;
+    if (!make_plan(n, batch, dflt, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   }
   p->direction = direction;
   p->sgn = direction == ESTL_FORWARD ? 1.f : -1.f;

@@ -330,6 +330,18 @@ struct Tile {
     }
   }
 
+  // The twiddle step of pass p alone (the tensor-core passes run the DFT
+  // elsewhere); only for one butterfly per thread (E == R).
+  template <int p>
+  ESTL_HD static void twiddle_only(cf32 (&v)[E], int t, const Ptr<const cf32>& tw) {
+    constexpr int LR = lr(p), R = 1 << LR, LNS = lns(p), NS = 1 << LNS;
+    static_assert(R == E, "one butterfly per thread");
+    if constexpr (NS > 1) {
+      const int k = t & (NS - 1);
+      twiddle_apply<R>(v, tw, k << (LOGM - LNS - LR));
+    }
+  }
+
   // Output position of slot j after pass p.
   template <int p>
   ESTL_HD static int out_pos(int t, int j) {
@@ -377,7 +389,9 @@ ESTL_HD void run_passes(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, con
 // Blocks per SM requested from the compiler: 16 elements per thread are built
 // for 1024 resident threads per SM (64 registers), 32 elements per thread for
 // 512 (128 registers).
-ESTL_CX int min_blocks(int nt, int e) { return nt * e >= 16384 ? 1 : 16384 / (nt * e); }
+ESTL_CX int min_blocks(int nt, int e) {
+  return nt * e >= 16384 ? 1 : (16384 / (nt * e) < 2048 / nt ? 16384 / (nt * e) : 2048 / nt);
+}
 
 // Keeps the compiler from hoisting every iteration's table loads to the top
 // of an unrolled epilogue (which costs 2 registers per load in flight).
@@ -386,6 +400,12 @@ ESTL_HD void schedule_fence() {
   asm volatile("" ::: "memory");
 #endif
 }
+
+}  // namespace estl
+
+#include "tc_core.cuh"
+
+namespace estl {
 
 // Launch parameters shared by all tile kernels.
 // ---------------------------------------------------------------------------
@@ -398,33 +418,48 @@ struct TileArgs {
   int logn1;       // four-step: log2 N1 (N = N1 * N2)
   float sgn;       // +1 forward; -1 = backward via conj(FFT(conj(x)))
   long long grid;  // CTAs launched (grid-stride kernels of pipe_core.cuh)
+  int split;       // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
 };
 
 ESTL_HD cf32 conj_if(cf32 v, float sgn) { return {v.x, v.y * sgn}; }
 
 // Whole transforms of length M = 2^LOGM, C transforms per CTA.  Thread
 // (c, t) = (tid >> LOGT, tid & (T-1)): unit-stride rows for loads and stores.
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+// TC: radix-16 passes on the tensor cores with the split precision
+// TileArgs::split (tc_core.cuh); the shared memory then also holds the
+// tensor-core area after the exchange buffer.
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct SingleKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static constexpr int EXCH = (TL::P > 1 || TC) ? C * CS : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;  // 16-byte aligned tensor-core area
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
+  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  struct Own {
+    ESTL_HD void operator()(int tid, int& t, int& c) const {
+      t = tid & (TL::T - 1);
+      c = tid >> TL::LOGT;
+    }
   };
 
   // One tile: row c of the tile is transform `in` -> `out` (length M each);
   // rows with valid == false only take part in the barriers.
   ESTL_HD static void body(const Ptr<const cf32>& in, const Ptr<cf32>& out, bool valid, int tid, cf32* smraw,
-                           const Ptr<const cf32>& bank, float sgn) {
+                           const Ptr<const cf32>& bank, float sgn, int split = SPLIT_NONE) {
     const int t = tid & (TL::T - 1);
     const int c = tid >> TL::LOGT;
     const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, split, tid, NT);
     cf32 v[TL::E];
     if (valid) {
 #pragma unroll
@@ -433,7 +468,12 @@ struct SingleKernel {
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
     }
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    if constexpr (TC) {
+      ESTL_SYNC();  // the DFT matrix table is complete
+      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+    } else {
+      run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    }
     if (valid) {
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) stcs(out, t + TL::T * j, conj_if(v[j], sgn));
@@ -446,7 +486,7 @@ struct SingleKernel {
     const bool valid = row < a.rows;
     const Ptr<const cf32> in = valid ? a.in.sub(row * TL::M, TL::M) : Ptr<const cf32>{a.in.p, 0};
     const Ptr<cf32> out = valid ? a.out.sub(row * TL::M, TL::M) : Ptr<cf32>{a.out.p, 0};
-    body(in, out, valid, tid, smraw, a.bank, a.sgn);
+    body(in, out, valid, tid, smraw, a.bank, a.sgn, a.split);
   }
 };
 
@@ -454,37 +494,52 @@ struct SingleKernel {
 // columns n1 of one transform and runs their N2-point DFTs (M = N2), then
 // multiplies by w_N^{n1 k2} and writes S[k2 * N1 + n1].  Thread mapping is
 // column-fastest so both the loads and the stores move runs of C elements.
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ColKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
+  static constexpr int EXCH = (TL::P > 1 || TC) ? TL::MP * C : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
+  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
+  };
+  struct Own {
+    ESTL_HD void operator()(int tid, int& t, int& c) const {
+      c = tid & (C - 1);
+      t = tid >> LOGC;
+    }
   };
 
   // Columns n1_0 .. n1_0 + C - 1 of one transform: in = the transform
   // (N elements), out = its scratch (N elements, S[k2*N1 + n1]).
   ESTL_HD static void body(const Ptr<const cf32>& in, const Ptr<cf32>& out, int n1_0, int logn, int tid,
-                           cf32* smraw, const Ptr<const cf32>& bank, float sgn) {
+                           cf32* smraw, const Ptr<const cf32>& bank, float sgn, int split = SPLIT_NONE) {
     const int c = tid & (C - 1);
     const int t = tid >> LOGC;
     const int logn1 = logn - LOGM;
     const int n1 = n1_0 + c;
     const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, split, tid, NT);
     cf32 v[TL::E];
-#pragma unroll
     {
       const int step = TL::T << logn1;
       int off = n1 + (t << logn1);
 #pragma unroll
       for (int j = 0; j < TL::E; ++j, off += step) v[j] = conj_if(ldcs(in, off), sgn);
     }
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    if constexpr (TC) {
+      ESTL_SYNC();  // the DFT matrix table is complete
+      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+    } else {
+      run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    }
     store_twiddled(v, out, n1, t, logn, bank);
   }
 
@@ -520,7 +575,7 @@ struct ColKernel {
     const int nblk = (1 << logn1) >> LOGC;
     const long long f = cta / nblk;
     const int n1_0 = (int)(cta - f * nblk) * C;
-    body(a.in.sub(f * N, N), a.out.sub(f * N, N), n1_0, a.logn, tid, smraw, a.bank, a.sgn);
+    body(a.in.sub(f * N, N), a.out.sub(f * N, N), n1_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
   }
 };
 
@@ -530,32 +585,48 @@ struct ColKernel {
 // of 32/C consecutive row elements and stores runs of C consecutive outputs
 // (X[k2_0 .. k2_0 + C - 1 + N2 k1]) straight from registers, with the tile
 // exchanged through shared memory laid out [m][c].
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct RowKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
+  static constexpr int EXCH = (TL::P > 1 || TC) ? TL::MP * C : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
+  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
+  };
+  struct Own {
+    ESTL_HD void operator()(int tid, int& t, int& c) const {
+      c = tid & (C - 1);
+      t = tid >> LOGC;
+    }
   };
 
   // Rows k2_0 .. k2_0 + C - 1 of one transform's scratch `in` (N elements)
   // -> the transform's output `out` (N elements, X[k2 + N2 k1]).
   ESTL_HD static void body(const Ptr<cf32>& in, const Ptr<cf32>& out, int k2_0, int logn, int tid, cf32* smraw,
-                           const Ptr<const cf32>& bank, float sgn) {
+                           const Ptr<const cf32>& bank, float sgn, int split = SPLIT_NONE) {
     const int c = tid & (C - 1);
     const int t = tid >> LOGC;
     const int logn2 = logn - LOGM;
     const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, split, tid, NT);
     cf32 v[TL::E];
     const Ptr<cf32> row = in.sub((long long)(k2_0 + c) * TL::M, TL::M);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = ldcg(row, t + TL::T * j);
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    if constexpr (TC) {
+      ESTL_SYNC();  // the DFT matrix table is complete
+      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+    } else {
+      run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    }
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) stcs(out, k2_0 + c + ((t + TL::T * j) << logn2), conj_if(v[j], sgn));
   }
@@ -569,7 +640,7 @@ struct RowKernel {
     // the scratch written by the column pass is read-only here
     const Ptr<cf32> in{const_cast<cf32*>(a.in.p) + f * N, N};
     ESTL_CHECK(f * N + N, a.in.n + 1, "row pass input range");
-    body(in, a.out.sub(f * N, N), k2_0, a.logn, tid, smraw, a.bank, a.sgn);
+    body(in, a.out.sub(f * N, N), k2_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
   }
 };
 

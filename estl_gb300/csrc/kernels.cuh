@@ -17,18 +17,19 @@ struct KernelDesc {
   int smem_bytes;
   const void* fn;
   int pipe;  // grid-stride, cp.async double-buffered variant (pipe_core.cuh)
+  int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
 };
 
 template <class K>
-__global__ void __launch_bounds__(K::NT, min_blocks(K::NT, K::TL::E)) tile_kernel(TileArgs a) {
+__global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tile_kernel(TileArgs a) {
   extern __shared__ float2 estl_smem[];
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
 }
 
 template <class K>
-KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc, int pipe = 0) {
+KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0) {
   return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
-                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe};
+                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe, tc};
 }
 
 constexpr long long kMaxSmemBytes = 227 * 1024;
@@ -39,6 +40,9 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_PIPE_SINGLE(M, E, R, C) make_desc<PipeSingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C, 1)
 #define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
 #define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
+#define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
+#define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)
+#define ESTL_TC_ROW(M, C) make_desc<RowKernel<M, 4, 4, C, true>>(KIND_ROW, M, 4, 4, C, 0, 1)
 
 // Per translation unit tables (kernels_*.cu).
 int registry_single(const KernelDesc** out);

@@ -8,6 +8,12 @@
   static_assert(PipeColKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
 #define ESTL_X_PIPE_ROW(M, E, R, C) \
   static_assert(PipeRowKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
+#define ESTL_X_TC_SINGLE(M, C) \
+  static_assert(SingleKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
+#define ESTL_X_TC_COL(M, C) \
+  static_assert(ColKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
+#define ESTL_X_TC_ROW(M, C) \
+  static_assert(RowKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
 namespace estl {
 #include "kernel_list.inc"
 }
@@ -17,6 +23,7 @@ namespace estl {
 static const KernelDesc kTable[] = {
 #define ESTL_X_SINGLE(M, E, R, C) ESTL_SINGLE(M, E, R, C),
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) ESTL_PIPE_SINGLE(M, E, R, C),
+#define ESTL_X_TC_SINGLE(M, C) ESTL_TC_SINGLE(M, C),
 #include "kernel_list.inc"
 };
 

@@ -81,7 +81,8 @@ const KernelDesc* find_desc(const Step& st) {
   const KernelDesc* d = nullptr;
   int n = st.kind == STEP_COL ? registry_col(&d) : registry_row(&d);
   for (int i = 0; i < n; ++i)
-    if (d[i].logm == st.logm && d[i].loge == st.loge && d[i].logr == st.logr && d[i].logc == st.logc && !d[i].pipe)
+    if (d[i].logm == st.logm && d[i].loge == st.loge && d[i].logr == st.logr && d[i].logc == st.logc && !d[i].pipe &&
+        !d[i].tc)
       return &d[i];
   return nullptr;
 }
@@ -141,6 +142,7 @@ extern "C" estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direct
     a.logn1 = 0;
     a.sgn = direction == ESTL_FORWARD ? 1.f : -1.f;
     a.grid = step.grid;
+    a.split = SPLIT_NONE;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)step.grid), dim3(d->nthreads), args, d->smem_bytes, st),
                    "cudaLaunchKernel");

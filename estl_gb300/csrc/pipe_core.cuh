@@ -86,6 +86,7 @@ struct PipeSingleKernel {
   // each buffer a multiple of 16 bytes, so that the second one stays aligned
   static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
+  static constexpr int MIN_BLOCKS = min_blocks(NT, TL::E);
   static_assert(TL::M >= 2 && (TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
   ESTL_HD static long long ntiles(const TileArgs& a) { return (a.rows + C - 1) / C; }
@@ -135,6 +136,7 @@ struct PipeColKernel {
   // each buffer a multiple of 16 bytes, so that the second one stays aligned
   static constexpr long long TILE_BUF = (((Base::SMEM_ELEMS > TILE) ? Base::SMEM_ELEMS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
+  static constexpr int MIN_BLOCKS = min_blocks(NT, TL::E);
   static_assert(C >= 2 && (TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
   ESTL_HD static long long ntiles(const TileArgs& a) { return a.rows << (a.logn - LOGM - LOGC); }
@@ -194,6 +196,7 @@ struct PipeRowKernel {
   // each buffer a multiple of 16 bytes, so that the second one stays aligned
   static constexpr long long TILE_BUF = (((C * CS > TILE) ? C * CS : TILE) + 1) & ~1LL;
   static constexpr long long SMEM_ELEMS = 2 * TILE_BUF;
+  static constexpr int MIN_BLOCKS = min_blocks(NT, TL::E);
   static_assert((TILE / 2) % NT == 0, "16-byte chunks must split evenly");
 
   ESTL_HD static long long ntiles(const TileArgs& a) { return a.rows << (a.logn - LOGM - LOGC); }

@@ -12,8 +12,8 @@ namespace estl {
 namespace {
 
 template <class K>
-TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc, int pipe = 0) {
-  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32)), pipe};
+TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0) {
+  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32)), pipe, tc};
 }
 
 std::vector<TileCfg> build_configs() {
@@ -24,6 +24,9 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) v.push_back(cfg_of<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
+#define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
+#define ESTL_X_TC_ROW(M, C) v.push_back(cfg_of<RowKernel<M, 4, 4, C, true>>(STEP_ROW, M, 4, 4, C, 0, 1));
 #include "kernel_list.inc"
   return v;
 }
@@ -40,7 +43,7 @@ const TileCfg* default_single(int logm) {
   const TileCfg* best = nullptr;
   const int want_e = logm >= 13 ? 5 : std::min(4, logm);
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe) continue;
+    if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe || c.tc) continue;
     if (c.loge != want_e) continue;
     if (!best || std::abs(c.nthreads - 256) < std::abs(best->nthreads - 256)) best = &c;
   }
@@ -52,13 +55,13 @@ const TileCfg* default_single(int logm) {
 const TileCfg* default_pass(int kind, int logm, int want_logc, int max_logc) {
   const TileCfg* best = nullptr;
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > want_logc || c.pipe) continue;
+    if (c.kind != kind || c.logm != logm || c.loge != 4 || c.logc > want_logc || c.pipe || c.tc) continue;
     if (c.nthreads > 512) continue;
     if (!best || c.logc > best->logc) best = &c;
   }
   if (!best)
     for (const TileCfg& c : tile_configs()) {
-      if (c.kind != kind || c.logm != logm || c.logc > max_logc || c.pipe) continue;
+      if (c.kind != kind || c.logm != logm || c.logc > max_logc || c.pipe || c.tc) continue;
       if (!best || c.logc < best->logc || (c.logc == best->logc && c.nthreads < best->nthreads)) best = &c;
     }
   return best;
@@ -81,10 +84,19 @@ const StreamCfg* find_stream_cfg(int logn) {
   return nullptr;
 }
 
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe) {
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe, int tc) {
   for (const TileCfg& c : tile_configs())
-    if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc && c.pipe == pipe)
+    if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc && c.pipe == pipe &&
+        c.tc == tc)
       return &c;
+  return nullptr;
+}
+
+// The tensor-core tile of a kind and length (kernel_list.inc instantiates one
+// per length), or the one with the requested rows / columns per CTA.
+static const TileCfg* find_tc(int kind, int logm, int logc) {
+  for (const TileCfg& c : tile_configs())
+    if (c.tc && c.kind == kind && c.logm == logm && (logc < 0 || c.logc == logc)) return &c;
   return nullptr;
 }
 
@@ -137,8 +149,19 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     return true;
   }
 
+  // split precision: the radix-16 passes on the tensor cores.  n < 16 has no
+  // radix-16 pass and runs the FP32 tiles.
+  const bool tc = choice.split != 0 && logn >= 4;
+  if (choice.split < 0 || choice.split > 3) {
+    set_err(err, "unknown split precision %lld", choice.split);
+    return false;
+  }
+  if (tc && (choice.mode == 3 || choice.pipe > 0)) {
+    set_err(err, "split precision runs the plain single / four-step tiles (mode %lld)", choice.mode);
+    return false;
+  }
   int mode = choice.mode;
-  if (mode == 0) mode = (logn <= kSingleMaxLog) ? 1 : 2;
+  if (mode == 0) mode = (logn <= (tc ? kTcSingleMaxLog : kSingleMaxLog)) ? 1 : 2;
 
   if (mode == 3) {
     const StreamCfg* sc = find_stream_cfg(logn);
@@ -172,7 +195,9 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
       return false;
     }
     const TileCfg* c = nullptr;
-    if (choice.single_loge >= 0)
+    if (tc)
+      c = find_tc(STEP_SINGLE, logn, choice.single_logc);
+    else if (choice.single_loge >= 0)
       c = find_tile(STEP_SINGLE, logn, choice.single_loge, 4, choice.single_logc);
     else
       c = default_single(logn);
@@ -183,7 +208,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     const long long per = 1LL << c->logc;
     Step s{STEP_SINGLE, c->logm, c->loge, c->logr, c->logc, (batch + per - 1) / per, BUF_IN, BUF_OUT,
            0, total, 0, total, batch, logn};
-    s.pipe = use_pipe(choice, c);
+    s.pipe = tc ? 0 : use_pipe(choice, c);
+    s.tc = tc ? 1 : 0;
     p.steps.push_back(s);
     p.hbm_passes = 1;
     *out = p;
@@ -195,14 +221,19 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   int logn1 = logn - logn2;
   const TileCfg* col = nullptr;
   const TileCfg* row = nullptr;
-  if (choice.col_loge >= 0)
-    col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
-  else
-    col = default_pass(STEP_COL, logn2, logn1, logn1);
-  if (choice.row_loge >= 0)
-    row = find_tile(STEP_ROW, logn1, choice.row_loge, 4, choice.row_logc);
-  else
-    row = default_pass(STEP_ROW, (int)logn1, std::min((int)logn2, logn1 <= 9 ? 3 : 2), (int)logn2);
+  if (tc) {
+    col = find_tc(STEP_COL, logn2, choice.col_logc);
+    row = find_tc(STEP_ROW, logn1, choice.row_logc);
+  } else {
+    if (choice.col_loge >= 0)
+      col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
+    else
+      col = default_pass(STEP_COL, logn2, logn1, logn1);
+    if (choice.row_loge >= 0)
+      row = find_tile(STEP_ROW, logn1, choice.row_loge, 4, choice.row_logc);
+    else
+      row = default_pass(STEP_ROW, (int)logn1, std::min((int)logn2, logn1 <= 9 ? 3 : 2), (int)logn2);
+  }
   if (!col || !row) {
     set_err(err, "no four-step tiles instantiated for N1 = 2^%lld, N2 = 2^%lld", logn1, logn2);
     return false;
@@ -220,8 +251,9 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
            b0 * n, cnt * n, 0, cnt * n, cnt, logn};
     Step b{STEP_ROW, row->logm, row->loge, row->logr, row->logc, cnt << (logn2 - row->logc), BUF_SCRATCH, BUF_OUT,
            0, cnt * n, b0 * n, cnt * n, cnt, logn};
-    a.pipe = use_pipe(choice, col);
-    b.pipe = use_pipe(choice, row);
+    a.pipe = tc ? 0 : use_pipe(choice, col);
+    b.pipe = tc ? 0 : use_pipe(choice, row);
+    a.tc = b.tc = tc ? 1 : 0;
     p.steps.push_back(a);
     p.steps.push_back(b);
   }
@@ -238,7 +270,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
   if (logn == 0) return out;
   if (logn <= kSingleMaxLog) {
     for (const TileCfg& c : tile_configs()) {
-      if (c.kind != STEP_SINGLE || c.logm != logn) continue;
+      if (c.kind != STEP_SINGLE || c.logm != logn || c.tc) continue;
       PlanChoice ch;
       ch.mode = 1;
       ch.single_loge = c.loge;
@@ -260,9 +292,9 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       int logn1 = logn - logn2;
       if (logn1 < 7 || logn1 > 12) continue;
       for (const TileCfg& c : tile_configs()) {
-        if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1 || c.pipe) continue;
+        if (c.kind != STEP_COL || c.logm != logn2 || c.logc > logn1 || c.pipe || c.tc) continue;
         for (const TileCfg& r : tile_configs()) {
-          if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe) continue;
+          if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe || r.tc) continue;
           for (long long chunk : {0LL, 16LL << 20, 128LL << 20}) {
            for (int pipe : {0, 1}) {
             PlanChoice ch;
@@ -288,16 +320,21 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
 std::string Plan1D::describe() const {
   std::string s;
   char buf[512];
-  std::snprintf(buf, sizeof buf, "{\"n\": %lld, \"batch\": %lld, \"hbm_passes\": %d, \"launches\": %zu, \"scratch_bytes\": %lld, \"kernels\": [",
-                n, batch, hbm_passes, steps.size(), scratch_elems * 8);
+  static const char* splits[] = {"fp32", "fp16x2", "bf16x2", "bf16x3"};
+  std::snprintf(buf, sizeof buf,
+                "{\"n\": %lld, \"batch\": %lld, \"precision\": \"%s\", \"hbm_passes\": %d, \"launches\": %zu, "
+                "\"scratch_bytes\": %lld, \"kernels\": [",
+                n, batch, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes, steps.size(),
+                scratch_elems * 8);
   s += buf;
   const char* names[] = {"single", "col", "row", "copy", "stream"};
   int shown = 0;
   for (size_t i = 0; i < steps.size() && shown < 2; ++i, ++shown) {
     const Step& st = steps[i];
     std::snprintf(buf, sizeof buf,
-                  "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"tiles\": %lld, \"pipe\": %d}",
-                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe);
+                  "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"tiles\": %lld, \"pipe\": %d, "
+                  "\"tc\": %d}",
+                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe, st.tc);
     s += buf;
   }
   s += "]}";

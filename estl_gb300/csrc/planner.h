@@ -26,11 +26,12 @@ struct TileCfg {
   int nthreads;
   int smem_bytes;
   int pipe;  // pipelined (grid-stride, cp.async double-buffered) variant
+  int tc;    // radix-16 passes on the tensor cores (split precision)
 };
 
 // All instantiated tile kernels (kernel_list.inc).
 const std::vector<TileCfg>& tile_configs();
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe = 0);
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0);
 
 struct Step {
   int kind;
@@ -47,6 +48,8 @@ struct Step {
   int lag = 0, ring = 0;
   // pipelined variant (grid = tiles; the launcher runs min(tiles, resident CTAs))
   int pipe = 0;
+  // tensor-core variant (radix-16 passes as split-precision GEMMs)
+  int tc = 0;
 };
 
 // Streamed four-step configuration of a length (stream_list.inc), or nullptr.
@@ -66,6 +69,7 @@ struct PlanChoice {
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
   int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
   int pipe = 0;         // tile kernels: 0 plain, 1 pipelined variant (where one exists), -1 pipelined if any
+  int split = 0;        // 0 FP32; else the SplitKind of tensor-core radix-16 passes (tc_core.cuh)
 };
 
 struct Plan1D {
@@ -80,6 +84,7 @@ struct Plan1D {
 };
 
 constexpr int kSingleMaxLog = 14;
+constexpr int kTcSingleMaxLog = 13;  // split precision: larger n run four-step
 constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;
 

@@ -41,6 +41,16 @@ typedef enum estl_status {
 
 /* Arithmetic of a plan.  FP32 is the plain path. */
 #define ESTL_PREC_FP32 0
+/* Split precision (north star "Precision"): every radix-16 DFT stage runs as a
+ * tensor-core GEMM (mma.sync m16n8k16, FP32 accumulate) on operands split
+ * into 16-bit terms; twiddles and the other passes stay FP32.
+ *   FP16:     fp16 hi + lo, each butterfly scaled by a power of two first
+ *   BF16:     bf16 hi + lo (about 16 significant bits)
+ *   BF16X3:   bf16 hi + mid + lo (FP32-level, six products per stage)
+ * n <= 2^13 runs one tile kernel, larger n four-step (n <= 2^24). */
+#define ESTL_PREC_SPLIT_FP16 1
+#define ESTL_PREC_SPLIT_BF16 2
+#define ESTL_PREC_SPLIT_BF16X3 3
 
 typedef struct estl_plan_s* estl_plan;
 
@@ -67,7 +77,8 @@ const char* estl_status_string(estl_status status);
 int64_t estl_max_batch(int64_t n);
 
 /* Plan `batch` transforms of length n (power of two, 1 <= n <= 2^24).
- * direction: ESTL_FORWARD / ESTL_BACKWARD; precision: ESTL_PREC_FP32.
+ * direction: ESTL_FORWARD / ESTL_BACKWARD; precision: ESTL_PREC_FP32 or one of
+ * the ESTL_PREC_SPLIT_* tensor-core forms.
  * Replaces the FFT_OpenCL_Contiguous constructor (FFT_OpenCL_Contiguous.h:46-71):
  * radix plan, kernels (precompiled, no runtime compile) and device scratch.
  * Uses an autotuned configuration when the tuning cache holds one for

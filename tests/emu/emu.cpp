@@ -58,11 +58,12 @@ struct EmuKernel {
   long long smem;
   RunFn fn;
   int pipe;
+  int tc;
 };
 
 template <class K>
-EmuKernel mk(int kind, int m, int e, int r, int c, int pipe = 0) {
-  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, pipe};
+EmuKernel mk(int kind, int m, int e, int r, int c, int pipe = 0, int tc = 0) {
+  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, pipe, tc};
 }
 
 const std::vector<EmuKernel>& emu_kernels() {
@@ -74,6 +75,9 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) k.push_back(mk<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
+#define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
+#define ESTL_X_TC_ROW(M, C) k.push_back(mk<RowKernel<M, 4, 4, C, true>>(STEP_ROW, M, 4, 4, C, 0, 1));
 #include "kernel_list.inc"
     return k;
   }();
@@ -280,6 +284,7 @@ PlanChoice choice_from(const int* f) {
   c.chunk = f[8];
   c.lag = f[9];
   c.pipe = f[10];
+  c.split = f[11];
   return c;
 }
 
@@ -288,7 +293,7 @@ PlanChoice choice_from(const int* f) {
 extern "C" {
 
 // Runs the plan for (n, batch) on interleaved complex64 host data.
-// choice: 11 ints (PlanChoice fields) or NULL for the planner default.
+// choice: 12 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
 int emu_plan_run(long long n, long long batch, const int* choice, int sign, const float* in, float* out, char* err,
@@ -366,7 +371,7 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     const EmuKernel* k = nullptr;
     for (const EmuKernel& c : emu_kernels())
       if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc &&
-          c.pipe == st.pipe)
+          c.pipe == st.pipe && c.tc == st.tc)
         k = &c;
     if (!k) {
       set_err(err, errlen, "no emulated kernel for a plan step");
@@ -384,6 +389,7 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     // CTA loops over several tiles and uses both tile buffers
     const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
     a.grid = grid;
+    a.split = st.tc ? p.choice.split : SPLIT_NONE;
     if (!run_kernel(*k, a, grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
       set_err(err, errlen, g_msg);
@@ -406,13 +412,13 @@ int emu_plan_describe(long long n, long long batch, const int* choice, char* buf
 }
 
 // Candidate choices of the autotuner for (n, batch): writes up to max rows
-// of 11 ints, returns the number of candidates.
+// of 12 ints, returns the number of candidates.
 int emu_plan_candidates(long long n, long long batch, int* out, int max) {
   std::vector<PlanChoice> c = plan_candidates(n, batch);
   int k = 0;
   for (const PlanChoice& ch : c) {
     if (k >= max) break;
-    int* f = out + 11 * k++;
+    int* f = out + 12 * k++;
     f[0] = ch.mode;
     f[1] = ch.single_loge;
     f[2] = ch.single_logc;
@@ -424,6 +430,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[8] = (int)ch.chunk;
     f[9] = ch.lag;
     f[10] = ch.pipe;
+    f[11] = ch.split;
   }
   return (int)c.size();
 }
@@ -548,3 +555,10 @@ long long emu_bank(float* out) {
 }
 
 }  // extern "C"
+
+extern "C" {
+// The host emulator's 16-bit conversions (tc_core.cuh), for the conversion
+// tests: bf = 1 bfloat16, 0 IEEE binary16; returns the 16-bit pattern.
+unsigned emu_to16(float x, int bf) { return estl::to16(x, bf != 0); }
+float emu_from16(unsigned h, int bf) { return estl::from16(h, bf != 0); }
+}

@@ -24,12 +24,13 @@ def rand_c64(shape, seed):
 
 def pad_choice(choice):
     """PlanChoice fields: mode, single_loge, single_logc, logn2, col_loge,
-    col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available)."""
+    col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available),
+    split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes)."""
     c = list(choice)
     if len(c) < 10:
         c += [0] * (10 - len(c))
-    if len(c) < 11:
-        c.append(0)
+    if len(c) < 12:
+        c += [0] * (12 - len(c))
     return c
 
 
@@ -38,20 +39,20 @@ def emu_run(emu, n, batch, x, sign=-1, choice=None):
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 11)(*pad_choice(choice))
+        ch = (ctypes.c_int * 12)(*pad_choice(choice))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (11 * 4096))()
+    buf = (ctypes.c_int * (12 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[11 * i: 11 * i + 11]) for i in range(min(k, 4096))]
+    return [list(buf[12 * i: 12 * i + 12]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 11)(*pad_choice(choice)) if choice is not None else None
+    ch = (ctypes.c_int * 12)(*pad_choice(choice)) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())
