@@ -169,13 +169,35 @@ def cpu_baseline_sample(logns, threads, budget_s=20.0):
     return tot_bytes / tot_s / 1e9, desc
 
 
+def fp64_fft(x, sign=-1):
+    """Double-precision DFT of the rows of x (numpy's pocketfft on complex128):
+    the error reference of the benchmark lines, forward e^{-2 pi i jk/n} for
+    sign -1, unnormalised e^{+2 pi i jk/n} for +1."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.complex128)
+    return np.fft.fft(x, axis=-1) if sign < 0 else np.fft.ifft(x, axis=-1) * x.shape[-1]
+
+
+def fp64_conv(s, f):
+    """Full linear convolution in double precision (FFT of length >= the output)."""
+    import numpy as np
+    L = len(s) + len(f) - 1
+    m = 1 << (L - 1).bit_length()
+    return np.fft.irfft(np.fft.rfft(np.float64(s), m) * np.fft.rfft(np.float64(f), m), m)[:L]
+
+
+def rel_l2_rows(y, ref):
+    import numpy as np
+    y = np.asarray(y, dtype=np.complex128)
+    return np.sqrt(np.sum(np.abs(y - ref) ** 2, axis=-1) / np.sum(np.abs(ref) ** 2, axis=-1))
+
+
 def bench_config1(estl, torch):
     """N = 4096, batch = 256 (8 MiB, L2-sized): a CUDA graph of 64 executes over
     32 rotating buffer pairs (512 MiB, larger than L2), forward, plus the
-    rel-L2 error of one batch against the oracle."""
+    rel-L2 error of one batch against an FP64 DFT."""
     import numpy as np
 
-    import oracle
     n, batch, rot, reps = 4096, 256, 32, 64
     rng = np.random.default_rng(1)
     x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
@@ -183,7 +205,7 @@ def bench_config1(estl, torch):
     ys = [torch.empty_like(xs[0]) for _ in range(rot)]
     plan = estl.Plan(n, batch, estl.FORWARD)
     y0 = plan.execute(xs[0]).cpu().numpy()
-    err = float(oracle.rel_l2(y0, oracle.fft(x, -1)).max())
+    err = float(rel_l2_rows(y0, fp64_fft(x, -1)).max())
     plan.close()
     plan = estl.Plan(n, batch, estl.FORWARD)  # fresh plan: its first ordering event is recorded inside the graph
     s = torch.cuda.Stream()
@@ -259,12 +281,12 @@ def bench_served_conv(estl, torch, count=600):
     filters of length log-uniform 2^4..2^12, both N(0,1), seed 5, pinned host
     buffers, HBM admission budget 64 GiB.  Saturation throughput and Poisson
     arrivals at 50% / 90% of it, batched server vs plain per-request (one
-    request at a time), plus rel-L2 of sampled outputs against the oracle."""
+    request at a time), plus rel-L2 of sampled outputs against an FP64
+    convolution."""
     import threading
 
     import numpy as np
 
-    import oracle
     from estl_gb300.serve import Server
     rng = np.random.default_rng(5)
     reqs = []
@@ -326,9 +348,53 @@ def bench_served_conv(estl, torch, count=600):
     errs = []
     for i in range(0, count, count // 6):
         s, f, o = reqs[i]
-        errs.append(float(np.sqrt(np.sum((o - oracle.conv_fft(s, f)) ** 2) /
-                                  np.sum(oracle.conv_fft(s, f) ** 2))))
+        ref = fp64_conv(s, f)
+        errs.append(float(np.sqrt(np.sum((o - ref) ** 2) / np.sum(ref ** 2))))
     out["rel_l2_max_sampled"] = max(errs)
+    return out
+
+
+def bench_split_precision(estl, torch):
+    """Split-precision tensor-core path: C2C forward at N in {2^12, 2^16, 2^20},
+    batch 2^26 / N, re/im uniform[-1,1) with 1% of the entries scaled by 1e3
+    (seed 4); FP32 and the three split forms (radix-16 stages as fp16 / bf16
+    tensor-core GEMMs, FP32 accumulate).  Time: CUDA events over 10 executes
+    (512 MiB per buffer, larger than L2); error: rel-L2 against an FP64 DFT on
+    a sample of the batch's transforms."""
+    import numpy as np
+    out = {"workload": "C2C forward, N in {2^12, 2^16, 2^20}, batch 2^26/N, uniform[-1,1) + 1% x1e3, seed 4",
+           "error_reference": "numpy pocketfft complex128 on the first transforms of the batch"}
+    forms = (("fp32", estl.PREC_FP32), ("fp16x2", estl.PREC_SPLIT_FP16), ("bf16x2", estl.PREC_SPLIT_BF16),
+             ("bf16x3", estl.PREC_SPLIT_BF16X3))
+    st = torch.cuda.Stream()
+    for logn in (12, 16, 20):
+        n = 1 << logn
+        batch = (1 << 26) // n
+        g = torch.Generator(device="cuda").manual_seed(4 + logn)
+        x = torch.view_as_complex((torch.rand((n * batch, 2), device="cuda", generator=g) * 2 - 1).contiguous())
+        x[torch.rand(n * batch, device="cuda", generator=g) < 0.01] *= 1000
+        y = torch.empty_like(x)
+        rows = max(1, min(batch, (1 << 21) // n))
+        ref = fp64_fft(x[: rows * n].view(rows, n).cpu().numpy(), -1)
+        entry = {}
+        for name, prec in forms:
+            plan = estl.Plan(n, batch, estl.FORWARD, precision=prec)
+            for _ in range(3):
+                plan.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+            st.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(10):
+                plan.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+            e1.record(st)
+            st.synchronize()
+            ms = e0.elapsed_time(e1) / 10
+            err = float(rel_l2_rows(y[: rows * n].view(rows, n).cpu().numpy(), ref).max())
+            entry[name] = {"ms": round(ms, 4), "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1),
+                           "rel_l2_max": float(f"{err:.3e}"),
+                           "tensor_core": any(k["tc"] for k in plan.describe()["kernels"])}
+            plan.close()
+        out[f"2^{logn}"] = entry
     return out
 
 
@@ -481,8 +547,19 @@ def main():
         gbs = 2 * 16.0 * TOTAL / (ms_n / 1e3) / 1e9
         gflops = 2 * 5.0 * n * logn * (TOTAL // n) / (ms_n / 1e3) / 1e9
         passes = plans[logn][0].describe()["hbm_passes"]
+        # accuracy (outside the timed region): forward vs an FP64 DFT and the
+        # round trip backward(forward(x)) / N vs x, on the first transforms
+        f, b = plans[logn]
+        f.execute_ptr(xin.data_ptr(), yfwd.data_ptr(), sh)
+        b.execute_ptr(yfwd.data_ptr(), zbwd.data_ptr(), sh)
+        torch.cuda.synchronize()
+        rows = max(1, min(TOTAL // n, (1 << 21) // n))
+        x_s = xin[: rows * n].view(rows, n).cpu().numpy()
+        e_fwd = float(rel_l2_rows(yfwd[: rows * n].view(rows, n).cpu().numpy(), fp64_fft(x_s, -1)).max())
+        e_rt = float(rel_l2_rows(zbwd[: rows * n].view(rows, n).cpu().numpy() / n, x_s).max())
         per_n_out[f"2^{logn}"] = {"gbs": round(gbs, 1), "frac": round(gbs / peak, 3), "gflops": round(gflops, 1),
                                   "hbm_passes": passes, "actual_traffic_gbs": round(gbs * passes, 1),
+                                  "rel_l2_fwd": float(f"{e_fwd:.3e}"), "rel_l2_roundtrip": float(f"{e_rt:.3e}"),
                                   "plan": plans[logn][0].describe()["kernels"]}
 
     # end to end through the C ABI with pinned host buffers (H2D + D2H inside)
@@ -522,7 +599,7 @@ def main():
     configs = {}
     if rank == 0 and not args.no_configs:
         for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
-                        ("served_conv", bench_served_conv)):
+                        ("split_precision", bench_split_precision), ("served_conv", bench_served_conv)):
             try:
                 configs[key] = fn(estl, torch)
             except Exception as ex:  # reported, never silently dropped

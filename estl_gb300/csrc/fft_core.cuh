@@ -444,12 +444,6 @@ struct SingleKernel {
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
-  struct Own {
-    ESTL_HD void operator()(int tid, int& t, int& c) const {
-      t = tid & (TL::T - 1);
-      c = tid >> TL::LOGT;
-    }
-  };
 
   // One tile: row c of the tile is transform `in` -> `out` (length M each);
   // rows with valid == false only take part in the barriers.
@@ -470,7 +464,7 @@ struct SingleKernel {
     }
     if constexpr (TC) {
       ESTL_SYNC();  // the DFT matrix table is complete
-      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+      run_passes_tc<TL>(v, t, c, sm, tw, Sidx{}, tc_ctx(smraw + TC_OFF, split, tid));
     } else {
       run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     }
@@ -509,12 +503,6 @@ struct ColKernel {
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
-  struct Own {
-    ESTL_HD void operator()(int tid, int& t, int& c) const {
-      c = tid & (C - 1);
-      t = tid >> LOGC;
-    }
-  };
 
   // Columns n1_0 .. n1_0 + C - 1 of one transform: in = the transform
   // (N elements), out = its scratch (N elements, S[k2*N1 + n1]).
@@ -536,7 +524,7 @@ struct ColKernel {
     }
     if constexpr (TC) {
       ESTL_SYNC();  // the DFT matrix table is complete
-      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+      run_passes_tc<TL>(v, t, c, sm, tw, Sidx{}, tc_ctx(smraw + TC_OFF, split, tid));
     } else {
       run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     }
@@ -600,12 +588,6 @@ struct RowKernel {
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
-  struct Own {
-    ESTL_HD void operator()(int tid, int& t, int& c) const {
-      c = tid & (C - 1);
-      t = tid >> LOGC;
-    }
-  };
 
   // Rows k2_0 .. k2_0 + C - 1 of one transform's scratch `in` (N elements)
   // -> the transform's output `out` (N elements, X[k2 + N2 k1]).
@@ -623,7 +605,7 @@ struct RowKernel {
     for (int j = 0; j < TL::E; ++j) v[j] = ldcg(row, t + TL::T * j);
     if constexpr (TC) {
       ESTL_SYNC();  // the DFT matrix table is complete
-      run_passes_tc<TL, 0>(v, t, c, sm, tw, Sidx{}, Own{}, tc_ctx(smraw + TC_OFF, split, tid));
+      run_passes_tc<TL>(v, t, c, sm, tw, Sidx{}, tc_ctx(smraw + TC_OFF, split, tid));
     } else {
       run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     }

@@ -24,8 +24,9 @@
 //   [butterfly][k] 16-bit pairs (row stride 20 words: conflict-free for both
 //   the 128-bit staging stores and the 32-bit fragment loads)
 //   -> B fragments, A fragments from a per-CTA table of the split DFT matrix
-//   -> mma -> each D fragment element Y[r][n] is written straight to the
-//   Stockham exchange slot of output r of butterfly n, which another lane owns.
+//   -> mma -> D staged as [butterfly][output] (18-element rows) -> each lane
+//   reads back its own butterfly's 16 outputs and continues exactly like the
+//   FP32 path after DFT<16> (Stockham exchange, next pass).
 // The emulator (ESTL_EMU) computes the same D elements directly from the
 // staged terms, so every shared-memory index of this file is bounds checked
 // on the host; the fragment layouts (PTX ISA, mma.m16n8k16 for 16-bit types)
@@ -55,11 +56,11 @@ ESTL_CX int split_terms(int kind) { return kind == SPLIT_BF16X3 ? 3 : 2; }
 
 // Shared-memory words of the tensor-core area: the split DFT matrix (three
 // term tables of 32 rows x 20 words) and, per warp, three staging tables of
-// the same shape plus 32 butterfly scale factors.
+// the same shape (B operand terms; the first two then hold D).
 constexpr int kTcRowWords = 20;
 constexpr int kTcTableWords = 32 * kTcRowWords;
 constexpr int kTcAtabWords = 3 * kTcTableWords;
-constexpr int kTcWarpWords = 3 * kTcTableWords + 32;
+constexpr int kTcWarpWords = 3 * kTcTableWords;
 ESTL_CX long long tc_area_words(int nwarps) { return kTcAtabWords + (long long)nwarps * kTcWarpWords; }
 
 // ---- 16-bit conversions (round to nearest even) ----------------------------
@@ -171,58 +172,92 @@ ESTL_HD void tc_init_atab(const Ptr<uint32_t>& atab, int kind, int tid, int nt) 
 // Per-warp view of the tensor-core area.
 struct TcCtx {
   Ptr<uint32_t> atab;   // 3 term tables of the DFT matrix
-  Ptr<uint32_t> stage;  // this warp's 3 staging tables
-  Ptr<float> scale;     // this warp's 32 butterfly scale factors
+  Ptr<uint32_t> stage;  // this warp's staging words (B terms, then D)
   int kind;
   int lane;
-  int tid0;  // thread index of lane 0 of this warp
 };
 
 ESTL_HD TcCtx tc_ctx(cf32* area, int kind, int tid) {
   uint32_t* w = reinterpret_cast<uint32_t*>(area);
   const int warp = tid >> 5;
   uint32_t* ws = w + kTcAtabWords + (long long)warp * kTcWarpWords;
-  return TcCtx{Ptr<uint32_t>{w, kTcAtabWords}, Ptr<uint32_t>{ws, 3 * kTcTableWords},
-               Ptr<float>{reinterpret_cast<float*>(ws + 3 * kTcTableWords), 32}, kind, tid & 31, tid & ~31};
+  return TcCtx{Ptr<uint32_t>{w, kTcAtabWords}, Ptr<uint32_t>{ws, kTcWarpWords}, kind, tid & 31};
 }
 
-// Lane `lane` stages its butterfly: the 32 real inputs (16 re, 16 im), scaled
-// (fp16) and split into terms, as row `lane` of each staging table.
-ESTL_HD void tc_stage(const cf32 (&x)[16], const TcCtx& ctx) {
-  const bool bf = ctx.kind != SPLIT_FP16X2;
-  const int terms = split_terms(ctx.kind);
-  float s = 1.f;
-  if (!bf) {
-    float m = 0.f;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) m = fmaxf(m, fmaxf(fabsf(x[k].x), fabsf(x[k].y)));
-    int e = 0;
-    if (m > 0.f) (void)frexpf(m, &e);  // m = f 2^e, 0.5 <= f < 1
-    s = ldexpf(1.f, -e);
-    ctx.scale[ctx.lane] = ldexpf(1.f, e);
-  } else {
-    ctx.scale[ctx.lane] = 1.f;
-  }
-#pragma unroll
-  for (int w = 0; w < 16; ++w) {
-    // word w holds k = 2w, 2w + 1: real parts for w < 8, imaginary parts after
-    float r0 = (w < 8 ? x[2 * w].x : x[2 * w - 16].y) * s;
-    float r1 = (w < 8 ? x[2 * w + 1].x : x[2 * w - 15].y) * s;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      if (q < terms) {
-        const uint32_t h0 = to16(r0, bf), h1 = to16(r1, bf);
-        r0 -= from16(h0, bf);
-        r1 -= from16(h1, bf);
-        ctx.stage[q * kTcTableWords + ctx.lane * kTcRowWords + w] = h0 | (h1 << 16);
-      }
-    }
-  }
+ESTL_HD uint32_t f32_bits_hd(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+ESTL_HD float bits_f32_hd(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+#endif
 }
 
 #if defined(__CUDA_ARCH__)
-ESTL_HD void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1, bool bf) {
-  if (bf)
+// ldmatrix .x4: four 8 x 8 16-bit matrices; lane L supplies the address of
+// row L & 7 of matrix L >> 3; register i receives matrix i, row lane / 4,
+// elements 2 (lane % 4) and 2 (lane % 4) + 1.
+ESTL_HD void ldmatrix_x4(uint32_t (&r)[4], const uint32_t* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+#endif
+
+// Two floats -> one word of two 16-bit values (a in the low half).
+template <bool BF>
+ESTL_HD uint32_t pack16(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (BF) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  } else {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
+#else
+  return to16(a, BF) | (to16(b, BF) << 16);
+#endif
+}
+template <bool BF>
+ESTL_HD void unpack16(uint32_t w, float& a, float& b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (BF) {
+    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+    a = f.x;
+    b = f.y;
+  } else {
+    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w));
+    a = f.x;
+    b = f.y;
+  }
+#else
+  a = from16(w & 0xffffu, BF);
+  b = from16(w >> 16, BF);
+#endif
+}
+
+// D staging: butterfly n's 16 outputs at complex index n * kTcDRow + r
+// (18-element rows: conflict-free for the fragment stores and the 16-byte
+// row reads).
+constexpr int kTcDRow = 18;
+static_assert(32 * kTcDRow * 2 <= 2 * kTcTableWords, "D staging must fit the first two B tables");
+
+#if defined(__CUDA_ARCH__)
+template <bool BF>
+ESTL_HD void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  if constexpr (BF)
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};\n"
@@ -237,105 +272,165 @@ ESTL_HD void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32
 }
 #endif
 
-// The warp's 32 staged butterflies through the tensor cores; every output
-// y_r of butterfly n (owned by lane n, thread tid0 + n) is written to the
-// exchange slot sidx(c_n, out_pos<p>(t_n, r)), times the butterfly's scale.
-// OWN(tid, t, c) gives a thread's (t, c) in the kernel's thread mapping.
-template <class TL, int p, class SIDX, class OWN>
-ESTL_HD void tc_dft16_scatter(const TcCtx& ctx, const Ptr<cf32>& sm, SIDX sidx, OWN own) {
-  const bool bf = ctx.kind != SPLIT_FP16X2;
-  const int terms = split_terms(ctx.kind);
-  const int g = ctx.lane >> 2, tig = ctx.lane & 3;
-#pragma unroll 1
-  for (int nt = 0; nt < 4; ++nt) {
-    float d[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#if defined(__CUDA_ARCH__)
+// The 16-point DFT of every lane's butterfly x (twiddled, FP32) through the
+// tensor cores: split and stage, GEMM, stage D, read back.  On return x[r]
+// holds output r of the lane's own butterfly, as DFT<16>::run leaves it.
+// Warp-collective: all 32 lanes call it together.
+template <int KIND>
+ESTL_HD void tc_dft16(cf32 (&x)[16], const TcCtx& ctx) {
+  constexpr bool BF = KIND != SPLIT_FP16X2;
+  constexpr int TERMS = split_terms(KIND);
+  // 1. scale (fp16) and split the 32 real inputs into TERMS 16-bit terms
+  float sc = 1.f, inv = 1.f;
+  if constexpr (!BF) {
+    float m = 0.f;
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-      uint32_t b[3][2];
+    for (int k = 0; k < 16; ++k) m = fmaxf(m, fmaxf(fabsf(x[k].x), fabsf(x[k].y)));
+    // 2^e with m < 2^e <= 2m from the exponent field of m (clamped so that
+    // 2^e and 2^-e are normal floats; m = 0 leaves the butterfly unscaled)
+    int be = (int)((f32_bits_hd(m) >> 23) & 0xff) - 126;  // m = f 2^be, 0.5 <= f < 1
+    be = be < -125 ? -125 : (be > 126 ? 126 : be);
+    if (m == 0.f) be = 0;
+    sc = bits_f32_hd((uint32_t)(127 + be) << 23);
+    inv = bits_f32_hd((uint32_t)(127 - be) << 23);
+  }
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        if (q < terms) {
-          const int base = q * kTcTableWords + (8 * nt + g) * kTcRowWords + 8 * kt + tig;
-          b[q][0] = ctx.stage[base];
-          b[q][1] = ctx.stage[base + 4];
-        }
-      }
+  for (int w = 0; w < 16; ++w) {
+    // word w: k = 2w, 2w + 1 (real parts for w < 8, imaginary parts after)
+    float r0 = (w < 8 ? x[2 * w].x : x[2 * w - 16].y) * inv;
+    float r1 = (w < 8 ? x[2 * w + 1].x : x[2 * w - 15].y) * inv;
 #pragma unroll
-      for (int qa = 0; qa < 3; ++qa) {
-        if (qa < terms) {
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt) {
-            const int base = qa * kTcTableWords + (16 * mt + g) * kTcRowWords + 8 * kt + tig;
-            const uint32_t a[4] = {ctx.atab[base], ctx.atab[base + 8 * kTcRowWords], ctx.atab[base + 4],
-                                   ctx.atab[base + 8 * kTcRowWords + 4]};
-#pragma unroll
-            for (int qb = 0; qb < 3; ++qb)
-              if (qa + qb < terms) mma16816(d[mt], a, b[qb][0], b[qb][1], bf);
-          }
-        }
+    for (int q = 0; q < TERMS; ++q) {
+      const uint32_t h = pack16<BF>(r0, r1);
+      ctx.stage[q * kTcTableWords + ctx.lane * kTcRowWords + w] = h;
+      if (q + 1 < TERMS) {
+        float f0, f1;
+        unpack16<BF>(h, f0, f1);
+        r0 -= f0;
+        r1 -= f1;
       }
     }
+  }
+  ESTL_SYNCWARP();
+  // 2. D = A B: 2 m-tiles (Re, Im rows) x 4 n-tiles (8 butterflies) per lane
+  const int g = ctx.lane >> 2, tig = ctx.lane & 3;
+  float d[4][2][4];
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) d[nt][mt][i] = 0.f;
+#if defined(__CUDA_ARCH__)
+  // B fragments of butterfly columns 8 nt .. 8 nt + 7, all 32 k: one
+  // ldmatrix.x4 per (n-tile, term): registers {b0, b1} of k-tile 0, then 1
+  // (row address: butterfly 8 nt + (lane & 7), k = 8 (lane >> 3)).
+  uint32_t b[4][TERMS][4];
+  const int lrow = ctx.lane & 7, lblk = ctx.lane >> 3;
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+    for (int q = 0; q < TERMS; ++q)
+      ldmatrix_x4(b[nt][q], ctx.stage.p + q * kTcTableWords + (8 * nt + lrow) * kTcRowWords + 4 * lblk);
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) {
+#pragma unroll
+    for (int qa = 0; qa < TERMS; ++qa) {
+      // A fragment of rows 16 mt .. +15, k = 16 kt .. +15: matrices
+      // (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
+      uint32_t a[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+        ldmatrix_x4(a[mt], ctx.atab.p + qa * kTcTableWords + (16 * mt + lrow + 8 * (lblk & 1)) * kTcRowWords +
+                               8 * kt + 4 * (lblk >> 1));
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+        for (int qb = 0; qa + qb < TERMS; ++qb)
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) mma16816<BF>(d[nt][mt], a[mt], b[nt][qb][2 * kt], b[nt][qb][2 * kt + 1]);
+    }
+  }
 #else
-    // emulator: the same D elements from the staged terms
+  // emulator: the same D elements from the staged terms
+  for (int nt = 0; nt < 4; ++nt)
     for (int mt = 0; mt < 2; ++mt)
       for (int i = 0; i < 4; ++i) {
         const int m = 16 * mt + g + ((i & 2) ? 8 : 0);
         const int n = 8 * nt + 2 * tig + (i & 1);
         float acc = 0.f;
-        for (int qa = 0; qa < terms; ++qa)
-          for (int qb = 0; qa + qb < terms; ++qb)
+        for (int qa = 0; qa < TERMS; ++qa)
+          for (int qb = 0; qa + qb < TERMS; ++qb)
             for (int k = 0; k < 32; ++k) {
               const uint32_t aw = ctx.atab[qa * kTcTableWords + m * kTcRowWords + (k >> 1)];
               const uint32_t bw = ctx.stage[qb * kTcTableWords + n * kTcRowWords + (k >> 1)];
-              acc += from16((k & 1) ? aw >> 16 : aw & 0xffffu, bf) * from16((k & 1) ? bw >> 16 : bw & 0xffffu, bf);
+              acc += from16((k & 1) ? aw >> 16 : aw & 0xffffu, BF) * from16((k & 1) ? bw >> 16 : bw & 0xffffu, BF);
             }
-        d[mt][i] = acc;
+        d[nt][mt][i] = acc;
       }
 #endif
-    // D element i of m-tile mt: row g (+8 for i >= 2), column 2 tig + (i & 1)
+  ESTL_SYNCWARP();  // every lane has its B fragments before D overwrites them
+  // 3. D element i of m-tile mt: row g (+8 for i >= 2), butterfly 8 nt + 2 tig + (i & 1)
+  const Ptr<cf32> dst{reinterpret_cast<cf32*>(ctx.stage.p), 32 * kTcDRow};
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = g + ((i & 2) ? 8 : 0);
       const int n = 8 * nt + 2 * tig + (i & 1);
-      const float s = ctx.scale[n];
-      int tn, cn;
-      own(ctx.tid0 + n, tn, cn);
-      sm[sidx(cn, TL::template out_pos<p>(tn, r))] = cf32{d[0][i] * s, d[1][i] * s};
+      dst[n * kTcDRow + r] = cf32{d[nt][0][i], d[nt][1][i]};
     }
+  ESTL_SYNCWARP();
+#if defined(__CUDA_ARCH__)
+  const float4* row = reinterpret_cast<const float4*>(dst.p + ctx.lane * kTcDRow);  // 144-byte rows: 16-byte aligned
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const float4 y = row[r];
+    x[2 * r] = cf32{y.x * sc, y.y * sc};
+    x[2 * r + 1] = cf32{y.z * sc, y.w * sc};
   }
+#else
+  for (int r = 0; r < 16; ++r) {
+    const cf32 y = dst[ctx.lane * kTcDRow + r];
+    x[r] = cf32{y.x * sc, y.y * sc};
+  }
+#endif
+  ESTL_SYNCWARP();  // D rows read before the next pass stages over them
 }
 
-// run_passes with the radix-16 passes on the tensor cores (E = 16: one
-// butterfly per thread).  Other passes are FP32 as in run_passes.  On exit
-// v[j] holds position t + T*j of the transformed tile, as run_passes leaves it.
-template <class TL, int p, class SIDX, class OWN>
-ESTL_HD void run_passes_tc(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw,
-                           SIDX sidx, OWN own, const TcCtx& ctx) {
+// run_passes with the radix-16 DFTs on the tensor cores (E = 16: one
+// butterfly per thread; the other radices stay FP32).  Same exchanges and
+// the same register state on exit as run_passes.
+template <int KIND, class TL, int p, class SIDX>
+ESTL_HD void run_passes_tc_k(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw,
+                             SIDX sidx, const TcCtx& ctx) {
   static_assert(TL::E == 16 && TL::LR_FULL == 4, "tensor-core passes need radix-16 tiles of 16 elements per thread");
   if constexpr (p < TL::P) {
-    constexpr bool last = p + 1 == TL::P;
     if constexpr (TL::lr(p) == 4) {
       TL::template twiddle_only<p>(v, t, tw);
-      tc_stage(v, ctx);
-      ESTL_SYNCWARP();
-      tc_dft16_scatter<TL, p>(ctx, sm, sidx, own);
+      tc_dft16<KIND>(v, ctx);
+    } else {
+      TL::template compute<p>(v, t, tw);
+    }
+    if constexpr (p + 1 < TL::P) {
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) sm[sidx(c, TL::template out_pos<p>(t, j))] = v[j];
       ESTL_SYNC();
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) v[j] = sm[sidx(c, t + TL::T * j)];
-      if constexpr (!last) ESTL_SYNC();
-    } else {
-      TL::template compute<p>(v, t, tw);
-      if constexpr (!last) {
-#pragma unroll
-        for (int j = 0; j < TL::E; ++j) sm[sidx(c, TL::template out_pos<p>(t, j))] = v[j];
-        ESTL_SYNC();
-#pragma unroll
-        for (int j = 0; j < TL::E; ++j) v[j] = sm[sidx(c, t + TL::T * j)];
-        ESTL_SYNC();
-      }
+      ESTL_SYNC();
     }
-    run_passes_tc<TL, p + 1>(v, t, c, sm, tw, sidx, own, ctx);
+    run_passes_tc_k<KIND, TL, p + 1>(v, t, c, sm, tw, sidx, ctx);
+  }
+}
+
+template <class TL, class SIDX>
+ESTL_HD void run_passes_tc(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw,
+                           SIDX sidx, const TcCtx& ctx) {
+  switch (ctx.kind) {
+    case SPLIT_FP16X2: run_passes_tc_k<SPLIT_FP16X2, TL, 0>(v, t, c, sm, tw, sidx, ctx); break;
+    case SPLIT_BF16X2: run_passes_tc_k<SPLIT_BF16X2, TL, 0>(v, t, c, sm, tw, sidx, ctx); break;
+    default: run_passes_tc_k<SPLIT_BF16X3, TL, 0>(v, t, c, sm, tw, sidx, ctx); break;
   }
 }
 
