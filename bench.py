@@ -298,6 +298,8 @@ def bench_served_conv(estl, torch, count=600):
         o = torch.empty(Ls + K - 1, dtype=torch.float32).pin_memory().numpy()
         reqs.append((s, f, o))
 
+    run_flags = [0]
+
     def run(srv, rate):
         """rate None: submit everything at once; else Poisson arrivals (req/s)."""
         tickets = [None] * count
@@ -311,7 +313,7 @@ def bench_served_conv(estl, torch, count=600):
                     d = t0 + arrivals[i] - time.perf_counter()
                     if d > 0:
                         time.sleep(d)
-                tickets[i] = srv.submit_conv(s, f, o)
+                tickets[i] = srv.submit_conv(s, f, o, flags=run_flags[0])
 
         th = threading.Thread(target=submitter)
         th.start()
@@ -328,9 +330,12 @@ def bench_served_conv(estl, torch, count=600):
 
     out = {"workload": f"{count} FFT-convolution requests, signal log-uniform 2^8..2^20, filter 2^4..2^12, "
                        "N(0,1) seed 5, pinned host buffers", "hbm_budget_gib": 64}
-    for name, kw in (("batched", dict(max_inflight_batches=4, max_batch_requests=64)),
-                     ("per_request", dict(max_inflight_batches=1, max_batch_requests=1))):
+    for name, kw, flags in (("batched", dict(max_inflight_batches=4, max_batch_requests=64), 0),
+                            ("batched_split_fp16", dict(max_inflight_batches=4, max_batch_requests=64),
+                             estl.PREC_SPLIT_FP16 << 8),
+                            ("per_request", dict(max_inflight_batches=1, max_batch_requests=1), 0)):
         srv = Server(hbm_budget_bytes=64 << 30, **kw)
+        run_flags[0] = flags
         try:
             run(srv, None)  # warm-up: plans, kernels, memory pool
             sat = run(srv, None)
@@ -343,8 +348,18 @@ def bench_served_conv(estl, torch, count=600):
         finally:
             srv.stop()
         out[name] = res
+        if name == "batched_split_fp16":
+            errs = []
+            for i in range(0, count, count // 6):
+                s_, f_, o_ = reqs[i]
+                ref = fp64_conv(s_, f_)
+                errs.append(float(np.sqrt(np.sum((o_ - ref) ** 2) / np.sum(ref ** 2))))
+            out_split_err = max(errs)
     out["batched_vs_per_request"] = round(out["batched"]["saturated"]["req_per_s"] /
                                           out["per_request"]["saturated"]["req_per_s"], 2)
+    out["batched_split_fp16_vs_per_request_fp32"] = round(out["batched_split_fp16"]["saturated"]["req_per_s"] /
+                                                          out["per_request"]["saturated"]["req_per_s"], 2)
+    out["batched_split_fp16"]["rel_l2_max_sampled"] = out_split_err
     errs = []
     for i in range(0, count, count // 6):
         s, f, o = reqs[i]

@@ -133,6 +133,11 @@ CONV_CORRELATE = 1
 CONV_REFERENCE_COMPAT = 2
 
 
+def conv_precision(p):
+    """ESTL_CONV_PRECISION: the split precision of a convolution's FFT stages, or'd into its flags."""
+    return int(p) << 8
+
+
 def lib():
     """Load libestl_cuda.so (built by estl_gb300.build / __graft_entry__.build)."""
     global _lib

@@ -23,12 +23,13 @@ struct ConvKernelDesc {
   int nthreads, smem_bytes;
   const void* fn;
   bool attr_set;
+  int tc;
 };
 
 template <class K>
-ConvKernelDesc cdesc(int kind, int m, int e, int r, int c) {
+ConvKernelDesc cdesc(int kind, int m, int e, int r, int c, int tc = 0) {
   return ConvKernelDesc{kind, m, e, r, c, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
-                        reinterpret_cast<const void*>(&conv_kernel<K>), false};
+                        reinterpret_cast<const void*>(&conv_kernel<K>), false, tc};
 }
 
 std::vector<ConvKernelDesc>& conv_table() {
@@ -45,16 +46,42 @@ std::vector<ConvKernelDesc>& conv_table() {
   v.push_back(cdesc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));
 #define ESTL_XC_OUT(M, E, R, C) v.push_back(cdesc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C));
 #include "conv_list.inc"
+    // split-precision (tensor-core) variants of the 16-elements-per-thread tiles
+#define ESTL_XC_SINGLE(M, E, R, C)                                                        \
+  if constexpr (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog) {                             \
+    v.push_back(cdesc<SpecSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(      \
+        CK_SPEC_SINGLE, M, E, R, C, 1));                                                                    \
+    v.push_back(cdesc<ConvSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(      \
+        CK_CONV_SINGLE, M, E, R, C, 1));                                                                    \
+  }
+#define ESTL_XC_COL(M, E, R, C)                                                \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C, true>>(CK_COL_FILTER, M, E, R, C, 1)); \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C, true>>(CK_COL_SIGNAL, M, E, R, C, 1));
+#define ESTL_XC_ROW(M, E, R, C)                                              \
+  v.push_back(cdesc<SpecRowKernel<M, E, R, C, true>>(CK_SPEC_ROW, M, E, R, C, 1)); \
+  v.push_back(cdesc<ConvMidKernel<M, E, R, C, true>>(CK_MID, M, E, R, C, 1));
+#define ESTL_XC_OUT(M, E, R, C) v.push_back(cdesc<ConvOutKernel<M, E, R, C, true>>(CK_OUT, M, E, R, C, 1));
+#include "conv_list.inc"
     return v;
   }();
   return t;
 }
 
+// every kernel of the table fits the shared memory of one SM
+bool conv_table_fits() {
+  for (const ConvKernelDesc& d : conv_table())
+    if (d.smem_bytes > kMaxConvSmemBytes) return false;
+  return true;
+}
+
 std::mutex g_conv_attr_mu;
 
 estl_status conv_lookup(const ConvLaunch& l, const ConvKernelDesc** out) {
+  static const bool fits = conv_table_fits();
+  if (!fits) return fail(ESTL_DEVICE_ERROR, "a convolution kernel needs more shared memory than an SM has");
   for (ConvKernelDesc& d : conv_table()) {
-    if (d.kind == l.kind && d.logm == l.logm && d.loge == l.loge && d.logr == l.logr && d.logc == l.logc) {
+    if (d.kind == l.kind && d.logm == l.logm && d.loge == l.loge && d.logr == l.logr && d.logc == l.logc &&
+        d.tc == l.tc) {
       if (!d.attr_set) {
         std::lock_guard<std::mutex> g(g_conv_attr_mu);
         if (!d.attr_set) {
@@ -96,6 +123,7 @@ estl_status launch_conv(const ConvLayout& L, const ConvBuffers& b, int which, cu
     a.s2 = Ptr<cf32>{b.s2 + l.s_off, l.row_count * N};
     a.bank = Ptr<const cf32>{E.bank, kBankSize};
     a.logn = l.logn;
+    a.split = l.tc ? L.split : SPLIT_NONE;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)l.grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel(conv)");
@@ -131,7 +159,7 @@ static_assert(sizeof(estl_conv_request) == sizeof(ConvReq), "request layout");
 static estl_status conv_layout_from(const estl_conv_request* reqs, int64_t count, int flags, ConvLayout* L,
                                     bool shared) {
   if (count < 1 || count > INT_MAX || !reqs) return fail(ESTL_INVALID_ARG, "need 1..INT_MAX requests");
-  if (flags & ~(ESTL_CONV_CORRELATE | ESTL_CONV_REFERENCE_COMPAT)) return fail(ESTL_INVALID_ARG, "unknown flags %d", flags);
+  if (flags & ~kConvFlagMask) return fail(ESTL_INVALID_ARG, "unknown flags %d", flags);
   std::string err;
   if (!build_conv_layout(reinterpret_cast<const ConvReq*>(reqs), (int)count, flags, L, &err, shared))
     return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());

@@ -48,6 +48,7 @@ struct ConvArgs {
   Ptr<cf32> s2;        // four-step scratch: N per row
   Ptr<const cf32> bank;
   int logn;
+  int split;  // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
 };
 
 ESTL_HD cf32 cconj(cf32 v) { return {v.x, -v.y}; }
@@ -63,15 +64,18 @@ ESTL_HD float dc_factor(const ConvArgs& a, const ConvRow& r) {
 // ---------------------------------------------------------------------------
 // N <= 2^14: whole requests in one CTA (C requests per CTA)
 // ---------------------------------------------------------------------------
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ConvSingleKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static constexpr int EXCH = (TL::P > 1) ? C * CS : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;  // 16-byte aligned tensor-core area
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
-  static constexpr int MINB = min_blocks(NT, TL::E);
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
+  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -93,7 +97,8 @@ struct ConvSingleKernel {
     const long long ri = cta * C + c;
     const bool valid = ri < a.nrows;
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, NT);
     ConvRow r{};
     if (valid) r = a.rows[ri];
     cf32 v[TL::E];
@@ -103,7 +108,7 @@ struct ConvSingleKernel {
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
     }
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
     if constexpr (MODE == 1) {
       if (valid) {
         const Ptr<cf32> o = a.spec_out.sub(r.spec_off, TL::M);
@@ -116,7 +121,7 @@ struct ConvSingleKernel {
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
       }
-      run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+      any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
       if (valid) {
         const Ptr<float> o = a.out.sub(r.out_off, r.out_len);
         const float g = dc_factor(a, r);
@@ -131,9 +136,9 @@ struct ConvSingleKernel {
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) { run_mode<0>(a, cta, tid, sm); }
 };
 
-template <int LOGM, int LOGE, int LOGR, int LOGC>
-struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC> {
-  using B = ConvSingleKernel<LOGM, LOGE, LOGR, LOGC>;
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
+struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
+  using B = ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC>;
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) {
     B::template run_mode<1>(a, cta, tid, sm);
   }
@@ -144,14 +149,17 @@ struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC> {
 // ---------------------------------------------------------------------------
 // A: column pass over the zero-padded real input of row f: C adjacent
 // columns n1, N2-point DFTs, times w_N^{n1 k2}, to s1[f*N + k2*N1 + n1].
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ConvColKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? TL::MP * C : 0;
+  static constexpr int EXCH = (TL::P > 1) ? TL::MP * C : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
-  static constexpr int MINB = min_blocks(NT, TL::E);
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
+  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
@@ -165,7 +173,8 @@ struct ConvColKernel {
     const int n1 = (int)(cta - f * nblk) * C + c;
     const ConvRow r = a.rows[f];
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, NT);
     const Ptr<const float> s = a.sig.sub(r.sig_off, r.sig_len);
     cf32 v[TL::E];
 #pragma unroll
@@ -173,7 +182,7 @@ struct ConvColKernel {
       const int n = n1 + ((t + TL::T * j) << logn1);
       v[j] = cf32{n < r.sig_len ? s[n] : 0.f, 0.f};
     }
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
     const Ptr<cf32> o = a.s1.sub(f * N, N);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
@@ -186,15 +195,18 @@ struct ConvColKernel {
 // B (spectrum): row pass of the filter: row k2 of s1 -> N1-point DFT ->
 // Hp[k2*N1 + k1] = scale * H[k2 + N2 k1] (conjugated for correlation), stored
 // unit-stride in the permuted order the convolution kernels read.
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct SpecRowKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
-  static constexpr int SMEM_ELEMS = (TL::P > 1) ? C * CS : 0;
+  static constexpr int EXCH = (TL::P > 1) ? C * CS : 0;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;  // 16-byte aligned tensor-core area
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
-  static constexpr int MINB = min_blocks(NT, TL::E);
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
+  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -208,12 +220,13 @@ struct SpecRowKernel {
     const int k2 = (int)(cta - f * nblk) * C + c;
     const ConvRow r = a.rows[f];
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, NT);
     const Ptr<cf32> s1 = a.s1.sub(f * N + (long long)k2 * TL::M, TL::M);
     cf32 v[TL::E];
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
-    run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
+    any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
     const Ptr<cf32> o = a.spec_out.sub(r.spec_off + (long long)k2 * TL::M, TL::M);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) o[t + TL::T * j] = cf32{v[j].x * r.scale, v[j].y * r.scale * r.conj};
@@ -223,14 +236,17 @@ struct SpecRowKernel {
 // B (convolution): row k2 of s1 -> N1-point DFT (X[k2 + N2 k1]) -> times
 // Hp -> conj -> N1-point DFT over k1 (V[k2][n1]) -> times w_N^{k2 n1} ->
 // s2[f*N + n1*N2 + k2], stored through shared memory in runs of C rows.
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ConvMidKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int SMEM_ELEMS = C * CS;
+  static constexpr int EXCH = C * CS;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
   // two DFTs, the spectrum multiply and the twiddle epilogue: allow 128 registers
   static constexpr int MINB = 1;
   struct Sidx {
@@ -247,17 +263,18 @@ struct ConvMidKernel {
     const int k2 = k2_0 + c;
     const ConvRow r = a.rows[f];
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, NT);
     const Sidx sidx{};
     const Ptr<cf32> s1 = a.s1.sub(f * N + (long long)k2 * TL::M, TL::M);
     cf32 v[TL::E];
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
-    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
     const Ptr<const cf32> h = a.spec.sub(r.spec_off + (long long)k2 * TL::M, TL::M);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
-    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int n1 = t + TL::T * j;
@@ -278,15 +295,18 @@ struct ConvMidKernel {
 // C: row n1 of s2 (N2 contiguous values over k2) -> N2-point DFT over k2 ->
 // conj(result)[n1 + N1 n2] -> real part, staged through shared memory and
 // stored in runs of C columns, cropped to [out_shift, out_shift + out_len).
-template <int LOGM, int LOGE, int LOGR, int LOGC>
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ConvOutKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
   static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int SMEM_ELEMS = C * CS;
+  static constexpr int EXCH = C * CS;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
-  static constexpr int MINB = min_blocks(NT, TL::E);
+  static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
+  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -300,13 +320,14 @@ struct ConvOutKernel {
     const int n1_0 = (int)(cta - f * nblk) * C;
     const ConvRow r = a.rows[f];
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
-    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Ptr<cf32> sm{smraw, EXCH};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, NT);
     const Sidx sidx{};
     const Ptr<cf32> s2 = a.s2.sub(f * N + (long long)(n1_0 + c) * TL::M, TL::M);
     cf32 v[TL::E];
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = s2[t + TL::T * j];
-    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();

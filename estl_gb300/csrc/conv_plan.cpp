@@ -131,6 +131,12 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
     }
   }
   L.buckets = (int)buckets.size();
+  L.split = conv_split(flags);
+  // split precision: the tiles with radix-16 passes run their tensor-core variant
+  for (ConvLaunch& l : L.launches) {
+    const bool single = l.kind == CK_SPEC_SINGLE || l.kind == CK_CONV_SINGLE;
+    l.tc = (L.split != 0 && l.loge == 4 && l.logm >= 4 && (!single || l.logm <= kConvTcSingleMaxLog)) ? 1 : 0;
+  }
   for (const ConvLaunch& l : L.launches)
     L.is_spectrum_launch.push_back(l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW);
   L.spec_elems = spec;

@@ -13,6 +13,11 @@
 namespace estl {
 
 enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2 };
+// Bits 8-9 of the flags: the split precision of the FFT stages (SplitKind;
+// 0 = FP32), ESTL_CONV_PRECISION(p) in the C ABI.
+constexpr int kConvSplitShift = 8;
+constexpr int kConvFlagMask = CONV_CORRELATE | CONV_REFERENCE_COMPAT | (3 << kConvSplitShift);
+inline int conv_split(int flags) { return (flags >> kConvSplitShift) & 3; }
 
 // One convolution request: offsets (in floats) into the caller's packed
 // signal / filter / output arrays.
@@ -38,6 +43,7 @@ struct ConvLaunch {
   int logn;
   long long row_begin, row_count;  // rows in the filter (CK_SPEC_*, CK_COL_FILTER) or signal row array
   long long s_off;                 // element offset of this bucket's scratch in s1 / s2
+  int tc = 0;                      // split-precision (tensor-core) variant
 };
 
 struct ConvLayout {
@@ -52,9 +58,15 @@ struct ConvLayout {
   // launches that compute spectra come first in each bucket; these counts let
   // a caller run the spectrum launches once and the convolution launches often
   std::vector<char> is_spectrum_launch;
+  int split = 0;  // SplitKind of the tensor-core launches
 };
 
 constexpr int kConvMaxLogN = 22;
+// Split-precision single-tile convolutions up to 2^13: a 2^14 tile with the
+// tensor-core staging of its 32 warps exceeds the 227 KB of shared memory, so
+// that bucket runs its FP32 tiles.
+constexpr int kConvTcSingleMaxLog = 13;
+constexpr long long kMaxConvSmemBytes = 227 * 1024;
 
 // Output length of one request (signal_len + filter_len - 1, or signal_len
 // in reference-compatible mode).

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -111,6 +112,7 @@ estl_status validate(const estl_serve_request& r) {
     const int l = ilog2_exact(r.n);
     if (l < 0 || l > kMaxLogN) return fail(ESTL_UNSUPPORTED_SIZE, "FFT request length %lld", (long long)r.n);
     if (r.direction != ESTL_FORWARD && r.direction != ESTL_BACKWARD) return fail(ESTL_INVALID_ARG, "bad direction");
+    if (r.flags & ~(3 << kConvSplitShift)) return fail(ESTL_INVALID_ARG, "FFT request flags: only a precision");
     if (!r.in || !r.out) return fail(ESTL_INVALID_ARG, "FFT request needs in and out host buffers");
     return ESTL_OK;
   }
@@ -118,7 +120,7 @@ estl_status validate(const estl_serve_request& r) {
     if (r.signal_len < 1 || r.filter_len < 1) return fail(ESTL_INVALID_ARG, "convolution lengths must be >= 1");
     if (conv_logn(r.signal_len, r.filter_len) > kConvMaxLogN)
       return fail(ESTL_UNSUPPORTED_SIZE, "convolution padded length above 2^%d", kConvMaxLogN);
-    if (r.flags & ~(ESTL_CONV_CORRELATE | ESTL_CONV_REFERENCE_COMPAT)) return fail(ESTL_INVALID_ARG, "bad flags");
+    if (r.flags & ~kConvFlagMask) return fail(ESTL_INVALID_ARG, "bad flags");
     if (!r.in || !r.filter || !r.out) return fail(ESTL_INVALID_ARG, "convolution request needs three host buffers");
     return ESTL_OK;
   }
@@ -144,12 +146,13 @@ estl_status enqueue_batch(estl_server_s* srv, Batch* b) {
   cudaStream_t st = sl.stream;
   // ---- layout of the batch allocation
   std::map<int, std::vector<Req*>> conv_groups;                // flags -> requests
-  std::map<std::pair<long long, int>, std::vector<Req*>> fft;  // (n, direction) -> requests
+  // (n, direction, split precision) -> requests
+  std::map<std::tuple<long long, int, int>, std::vector<Req*>> fft;
   for (Req* q : b->reqs) {
     if (q->r.kind == ESTL_REQ_CONV)
       conv_groups[q->r.flags].push_back(q);
     else
-      fft[{q->r.n, q->r.direction}].push_back(q);
+      fft[{q->r.n, q->r.direction, conv_split(q->r.flags)}].push_back(q);
   }
   struct ConvGroup {
     std::vector<Req*> reqs;
@@ -201,10 +204,13 @@ estl_status enqueue_batch(estl_server_s* srv, Batch* b) {
     FftGroup g;
     g.reqs = kv.second;
     std::string err;
-    if (!make_plan(kv.first.first, (long long)g.reqs.size(), PlanChoice{}, &g.plan, &err))
+    const long long n = std::get<0>(kv.first);
+    PlanChoice choice;
+    choice.split = std::get<2>(kv.first);
+    if (!make_plan(n, (long long)g.reqs.size(), choice, &g.plan, &err))
       return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
-    const size_t bytes = 8 * (size_t)kv.first.first * g.reqs.size();
-    g.sgn = kv.first.second == ESTL_FORWARD ? 1.f : -1.f;
+    const size_t bytes = 8 * (size_t)n * g.reqs.size();
+    g.sgn = std::get<1>(kv.first) == ESTL_FORWARD ? 1.f : -1.f;
     g.o_in = off;
     off = up256(off + bytes);
     g.o_out = off;

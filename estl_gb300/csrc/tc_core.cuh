@@ -332,23 +332,34 @@ ESTL_HD void tc_dft16(cf32 (&x)[16], const TcCtx& ctx) {
 #pragma unroll
     for (int q = 0; q < TERMS; ++q)
       ldmatrix_x4(b[nt][q], ctx.stage.p + q * kTcTableWords + (8 * nt + lrow) * kTcRowWords + 4 * lblk);
+  // The tensor cores accumulate with truncation relative to the largest
+  // term: the small correction products (qa + qb >= 1) go first, into an
+  // accumulator that is still small, and the large hi x hi products last, so
+  // that the large partial sums are truncated only twice (once per k-tile).
 #pragma unroll
-  for (int kt = 0; kt < 2; ++kt) {
+  for (int phase = 0; phase < 2; ++phase) {
 #pragma unroll
-    for (int qa = 0; qa < TERMS; ++qa) {
-      // A fragment of rows 16 mt .. +15, k = 16 kt .. +15: matrices
-      // (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
-      uint32_t a[2][4];
+    for (int kt = 0; kt < 2; ++kt) {
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
-        ldmatrix_x4(a[mt], ctx.atab.p + qa * kTcTableWords + (16 * mt + lrow + 8 * (lblk & 1)) * kTcRowWords +
-                               8 * kt + 4 * (lblk >> 1));
+      for (int qa = 0; qa < TERMS; ++qa) {
+        if (phase == 1 && qa > 0) continue;
+        // A fragment of rows 16 mt .. +15, k = 16 kt .. +15: matrices
+        // (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
+        uint32_t a[2][4];
 #pragma unroll
-      for (int nt = 0; nt < 4; ++nt)
+        for (int mt = 0; mt < 2; ++mt)
+          ldmatrix_x4(a[mt], ctx.atab.p + qa * kTcTableWords + (16 * mt + lrow + 8 * (lblk & 1)) * kTcRowWords +
+                                 8 * kt + 4 * (lblk >> 1));
 #pragma unroll
-        for (int qb = 0; qa + qb < TERMS; ++qb)
+        for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt) mma16816<BF>(d[nt][mt], a[mt], b[nt][qb][2 * kt], b[nt][qb][2 * kt + 1]);
+          for (int qb = 0; qa + qb < TERMS; ++qb) {
+            if ((phase == 0) == (qa + qb == 0)) continue;  // phase 0: corrections, phase 1: hi x hi
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+              mma16816<BF>(d[nt][mt], a[mt], b[nt][qb][2 * kt], b[nt][qb][2 * kt + 1]);
+          }
+      }
     }
   }
 #else
@@ -421,6 +432,24 @@ ESTL_HD void run_passes_tc_k(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm
       ESTL_SYNC();
     }
     run_passes_tc_k<KIND, TL, p + 1>(v, t, c, sm, tw, sidx, ctx);
+  }
+}
+
+template <class TL, class SIDX>
+ESTL_HD void run_passes_tc(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw,
+                           SIDX sidx, const TcCtx& ctx);
+
+// run_passes (FP32) or run_passes_tc (split precision, TC tiles).  The
+// tensor-core table of the tile must be complete: the first call of a
+// TC tile synchronises the CTA before its first pass.
+template <bool TC, class TL, class SIDX>
+ESTL_HD void any_passes(cf32 (&v)[TL::E], int t, int c, const Ptr<cf32>& sm, const Ptr<const cf32>& tw, SIDX sidx,
+                        cf32* tc_area, int split, int tid) {
+  if constexpr (TC) {
+    ESTL_SYNC();
+    run_passes_tc<TL>(v, t, c, sm, tw, sidx, tc_ctx(tc_area, split, tid));
+  } else {
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
   }
 }
 

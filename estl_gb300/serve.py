@@ -24,14 +24,17 @@ class Server:
         return t.value
 
     def submit_conv(self, signal, filt, out, flags=0):
-        """signal, filt, out: contiguous float32 numpy arrays."""
+        """signal, filt, out: contiguous float32 numpy arrays; flags: CONV_* bits,
+        plus conv_precision(PREC_SPLIT_*) for the tensor-core FFT stages."""
         r = ServeRequest(REQ_CONV, 0, int(flags), 0, 0, signal.size, filt.size, signal.ctypes.data, filt.ctypes.data,
                          out.ctypes.data)
         return self._submit(r, (signal, filt, out))
 
-    def submit_fft(self, x, out, direction=-1):
-        """x, out: contiguous complex64 numpy arrays of one power-of-two length."""
-        r = ServeRequest(REQ_FFT, int(direction), 0, 0, x.size, 0, 0, x.ctypes.data, None, out.ctypes.data)
+    def submit_fft(self, x, out, direction=-1, precision=0):
+        """x, out: contiguous complex64 numpy arrays of one power-of-two length;
+        precision: PREC_FP32 or a PREC_SPLIT_* tensor-core form."""
+        r = ServeRequest(REQ_FFT, int(direction), int(precision) << 8, 0, x.size, 0, 0, x.ctypes.data, None,
+                         out.ctypes.data)
         return self._submit(r, (x, out))
 
     def poll(self, ticket, timeout_ms=60000):

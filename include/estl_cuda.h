@@ -209,6 +209,9 @@ estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direction, const 
  * (:141-143), L samples kept (:146-148).  n may be at most 2^22. */
 #define ESTL_CONV_CORRELATE 1
 #define ESTL_CONV_REFERENCE_COMPAT 2
+/* Split precision of the convolution's FFT stages (ESTL_PREC_SPLIT_*), or'd
+ * into the flags; 0 = FP32. */
+#define ESTL_CONV_PRECISION(p) ((p) << 8)
 
 /* One request of a batched convolution.  Offsets are in floats into the
  * caller's packed signal / filter / output arrays. */
@@ -292,7 +295,7 @@ typedef struct estl_serve_config {
 typedef struct estl_serve_request {
   int kind;                  /* ESTL_REQ_FFT or ESTL_REQ_CONV */
   int direction;             /* FFT: ESTL_FORWARD / ESTL_BACKWARD */
-  int flags;                 /* CONV: ESTL_CONV_* */
+  int flags;                 /* CONV: ESTL_CONV_*; both kinds: ESTL_CONV_PRECISION(ESTL_PREC_*) */
   int reserved;
   int64_t n;                 /* FFT: length (power of two <= 2^24) */
   int64_t signal_len;        /* CONV */

@@ -169,6 +169,12 @@ void run_fibers(int nt, const std::function<void(int)>& body) {
 
 template <class Fn, class Args>
 bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
+  // the device limit on dynamic shared memory per CTA (227 KB on sm_103a)
+  if (smem_elems * (long long)sizeof(cf32) > 227LL * 1024) {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    if (g_msg.empty()) g_msg = "kernel needs " + std::to_string(smem_elems * sizeof(cf32)) + " bytes of shared memory";
+    return false;
+  }
   // shared memory base 256-byte aligned, like the device's dynamic shared memory
   std::vector<cf32> smem_store((size_t)std::max<long long>(smem_elems, 1) + 32);
   cf32* smem_base = reinterpret_cast<cf32*>(((uintptr_t)smem_store.data() + 255) & ~(uintptr_t)255);
@@ -215,11 +221,12 @@ struct EmuConvKernel {
   int kind, logm, loge, logr, logc, nt;
   long long smem;
   ConvFn fn;
+  int tc;
 };
 
 template <class K>
-EmuConvKernel mkc(int kind, int m, int e, int r, int c) {
-  return EmuConvKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run};
+EmuConvKernel mkc(int kind, int m, int e, int r, int c, int tc = 0) {
+  return EmuConvKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, tc};
 }
 
 const std::vector<EmuConvKernel>& emu_conv_kernels() {
@@ -235,6 +242,21 @@ const std::vector<EmuConvKernel>& emu_conv_kernels() {
   k.push_back(mkc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C)); \
   k.push_back(mkc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));
 #define ESTL_XC_OUT(M, E, R, C) k.push_back(mkc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C));
+#include "conv_list.inc"
+#define ESTL_XC_SINGLE(M, E, R, C)                                                                       \
+  if constexpr (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog) {                                            \
+    k.push_back(mkc<SpecSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(         \
+        CK_SPEC_SINGLE, M, E, R, C, 1));                                                                   \
+    k.push_back(mkc<ConvSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(         \
+        CK_CONV_SINGLE, M, E, R, C, 1));                                                                   \
+  }
+#define ESTL_XC_COL(M, E, R, C)                                                 \
+  k.push_back(mkc<ConvColKernel<M, E, R, C, true>>(CK_COL_FILTER, M, E, R, C, 1)); \
+  k.push_back(mkc<ConvColKernel<M, E, R, C, true>>(CK_COL_SIGNAL, M, E, R, C, 1));
+#define ESTL_XC_ROW(M, E, R, C)                                               \
+  k.push_back(mkc<SpecRowKernel<M, E, R, C, true>>(CK_SPEC_ROW, M, E, R, C, 1)); \
+  k.push_back(mkc<ConvMidKernel<M, E, R, C, true>>(CK_MID, M, E, R, C, 1));
+#define ESTL_XC_OUT(M, E, R, C) k.push_back(mkc<ConvOutKernel<M, E, R, C, true>>(CK_OUT, M, E, R, C, 1));
 #include "conv_list.inc"
     return k;
   }();
@@ -460,7 +482,9 @@ int emu_conv_run(const long long* reqs, int count, int flags, int shared, const 
   for (const ConvLaunch& l : L.launches) {
     const EmuConvKernel* k = nullptr;
     for (const EmuConvKernel& c : emu_conv_kernels())
-      if (c.kind == l.kind && c.logm == l.logm && c.loge == l.loge && c.logr == l.logr && c.logc == l.logc) k = &c;
+      if (c.kind == l.kind && c.logm == l.logm && c.loge == l.loge && c.logr == l.logr && c.logc == l.logc &&
+          c.tc == l.tc)
+        k = &c;
     if (!k) {
       set_err(err, errlen, "no emulated convolution kernel for a launch");
       return 3;
@@ -483,6 +507,7 @@ int emu_conv_run(const long long* reqs, int count, int flags, int shared, const 
     a.s2 = Ptr<cf32>{s2.data() + (l.kind >= CK_COL_FILTER ? l.s_off : 0), l.kind >= CK_COL_FILTER ? l.row_count * N : 0};
     a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
     a.logn = l.logn;
+    a.split = l.tc ? L.split : SPLIT_NONE;
     if (!run_generic(k->nt, k->smem, k->fn, a, l.grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
       set_err(err, errlen, g_msg);

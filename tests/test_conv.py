@@ -105,6 +105,21 @@ def test_emulated_shared_filter(emu):
         assert rel(out[i * (L + K - 1):(i + 1) * (L + K - 1)], ref) < TOL
 
 
+SPLIT_TOL = {1: TOL, 2: 2e-5, 3: TOL}
+
+
+@pytest.mark.parametrize("split", [1, 2, 3])
+def test_emulated_split_precision(emu, split):
+    """Convolutions whose FFT stages run the split-precision tensor-core tiles
+    (precision in bits 8-9 of the flags): fp16 hi+lo and bf16 hi+mid+lo keep
+    the 1e-6 target, bf16 hi+lo (16 significant bits) stays within 2e-5."""
+    reqs, sig, filt, olen = make_requests(SHAPES_EMU, 11)
+    out = emu_conv(emu, reqs, sig, filt, olen, flags=split << 8)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < SPLIT_TOL[split], (split, L, K)
+
+
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
@@ -184,3 +199,14 @@ def test_gpu_conv_plan(engine, L, K, count):
             assert rel(out[i * olen:(i + 1) * olen], ref) < TOL
     finally:
         Lb.estl_conv_plan_destroy(plan)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("split", [1, 2, 3])
+def test_gpu_split_precision(engine, split):
+    shapes = SHAPES_EMU + [(1 << 16, 4096), ((1 << 20) - 7, 4096)]
+    reqs, sig, filt, olen = make_requests(shapes, 12)
+    out = gpu_conv_batch(engine, reqs, sig, filt, olen, flags=split << 8)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < SPLIT_TOL[split], (split, L, K)

@@ -29,16 +29,16 @@ def conv_requests(count, seed):
     return reqs
 
 
-def run_mixed(server, convs, ffts):
+def run_mixed(server, convs, ffts, precision=0):
     tickets = []
     outs = []
     for s, f in convs:
         out = np.full(s.size + f.size - 1, np.nan, np.float32)
-        tickets.append(server.submit_conv(s, f, out))
+        tickets.append(server.submit_conv(s, f, out, flags=precision << 8))
         outs.append(out)
     for x, d in ffts:
         out = np.full_like(x, np.nan)
-        tickets.append(server.submit_fft(x, out, d))
+        tickets.append(server.submit_fft(x, out, d, precision=precision))
         outs.append(out)
     results = [server.poll(t) for t in tickets]
     return outs, results
@@ -65,6 +65,35 @@ def test_mixed_requests_against_oracle(engine):
     assert all(r.status == 0 and r.latency_us > 0 for r in results)
     assert stats["completed"] == len(results) and stats["batches"] >= 3
     assert max(r.batch_requests for r in results) > 1
+
+
+def test_split_precision_requests(engine):
+    """The batched split-precision form (fp16 hi+lo tensor-core FFT stages) of
+    the served convolution and FFT requests: same accuracy targets as FP32
+    (1e-6 for convolutions, 2e-6 for transforms), and the same result alone
+    and in the mix."""
+    from estl_gb300 import PREC_SPLIT_FP16
+    from estl_gb300.serve import Server
+    convs = conv_requests(30, 4)
+    rng = np.random.default_rng(5)
+    ffts = [((rng.standard_normal(1 << l) + 1j * rng.standard_normal(1 << l)).astype(np.complex64), -1)
+            for l in (8, 13, 16, 20)]
+    srv = Server(max_inflight_batches=4, max_batch_requests=16)
+    try:
+        outs, results = run_mixed(srv, convs, ffts, precision=PREC_SPLIT_FP16)
+    finally:
+        srv.stop()
+    for (s, f), out in zip(convs, outs[:len(convs)]):
+        assert rel(out, oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))) < 1e-6
+    for (x, d), out in zip(ffts, outs[len(convs):]):
+        assert oracle.rel_l2(out[None], oracle.fft(x[None], d))[0] < 2e-6
+    assert all(r.status == 0 for r in results)
+    srv = Server(max_inflight_batches=1, max_batch_requests=1)
+    try:
+        alone, _ = run_mixed(srv, [convs[11]], [], precision=PREC_SPLIT_FP16)
+    finally:
+        srv.stop()
+    assert np.array_equal(alone[0], outs[11])
 
 
 def test_same_result_alone_and_in_the_mix(engine):
