@@ -514,11 +514,13 @@ def main():
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_region")  # ncu --nvtx-include "timed_region/" selects these launches
     e0.record(stream)
     for _ in range(args.steps):
         step(per_n)
     e1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     barrier()
     clk = clocks.stop()
     total_ms = e0.elapsed_time(e1)

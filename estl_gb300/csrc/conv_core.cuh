@@ -75,7 +75,7 @@ struct ConvSingleKernel {
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
-  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MINB = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -159,7 +159,7 @@ struct ConvColKernel {
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
-  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MINB = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return TL::pad(m) * C + c; }
   };
@@ -206,7 +206,7 @@ struct SpecRowKernel {
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
-  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MINB = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };
@@ -306,7 +306,7 @@ struct ConvOutKernel {
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
-  static constexpr int MINB = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MINB = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   struct Sidx {
     ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
   };

@@ -437,7 +437,7 @@ struct SingleKernel {
   static constexpr int EXCH = (TL::P > 1 || TC) ? C * CS : 0;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;  // 16-byte aligned tensor-core area
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
-  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MIN_BLOCKS = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
@@ -496,7 +496,7 @@ struct ColKernel {
   static constexpr int EXCH = (TL::P > 1 || TC) ? TL::MP * C : 0;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
-  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MIN_BLOCKS = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
@@ -581,7 +581,7 @@ struct RowKernel {
   static constexpr int EXCH = (TL::P > 1 || TC) ? TL::MP * C : 0;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
-  static constexpr int MIN_BLOCKS = TC ? 1 : min_blocks(NT, TL::E);
+  static constexpr int MIN_BLOCKS = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
 
@@ -623,6 +623,54 @@ struct RowKernel {
     const Ptr<cf32> in{const_cast<cf32*>(a.in.p) + f * N, N};
     ESTL_CHECK(f * N + N, a.in.n + 1, "row pass input range");
     body(in, a.out.sub(f * N, N), k2_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
+  }
+};
+
+// Four-step row pass for tiles of many rows (the persistent kernels, whose
+// row and column tiles share one thread count): threads are mapped row-fastest
+// (unit-stride loads of whole rows), and the results are staged in shared
+// memory and stored column-fastest so that every store moves a run of C
+// elements.  The C <= 8 tiles of the two-launch four-step use RowKernel.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct RemapRowKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, C);
+  static constexpr int SMEM_ELEMS = C * CS;
+  static constexpr int MIN_BLOCKS = min_blocks(NT, TL::E);
+  static_assert(NT <= 1024, "too many threads");
+  static_assert(NT % C == 0 && (NT / C) * TL::E >= TL::M, "store remap must cover the tile");
+
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+
+  // Rows k2_0 .. k2_0 + C - 1 of one transform's scratch `in` (N elements)
+  // -> the transform's output `out` (N elements, X[k2 + N2 k1]).
+  ESTL_HD static void body(const Ptr<cf32>& in, const Ptr<cf32>& out, int k2_0, int logn, int tid, cf32* smraw,
+                           const Ptr<const cf32>& bank, float sgn) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int logn2 = logn - LOGM;
+    const Ptr<const cf32> tw = bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, SMEM_ELEMS};
+    const Sidx sidx{};
+    cf32 v[TL::E];
+    const Ptr<cf32> row = in.sub((long long)(k2_0 + c) * TL::M, TL::M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = ldcg(row, t + TL::T * j);
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k1 = t2 + TL::T * j;
+      stcs(out, k2_0 + c2 + (k1 << logn2), conj_if(sm[sidx(c2, k1)], sgn));
+    }
   }
 };
 

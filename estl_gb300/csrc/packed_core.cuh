@@ -43,9 +43,9 @@ using PCol6 = ColKernel<6, 4, 4, 6>;
 using PCol7 = ColKernel<7, 4, 4, 5>;
 using PCol8 = ColKernel<8, 4, 4, 4>;
 using PCol9 = ColKernel<9, 4, 4, 3>;
-using PRow7 = RowKernel<7, 4, 4, 5>;
-using PRow8 = RowKernel<8, 4, 4, 4>;
-using PRow9 = RowKernel<9, 4, 4, 3>;
+using PRow7 = RemapRowKernel<7, 4, 4, 5>;
+using PRow8 = RemapRowKernel<8, 4, 4, 4>;
+using PRow9 = RemapRowKernel<9, 4, 4, 3>;
 
 ESTL_CX long long cmax(long long a, long long b) { return a > b ? a : b; }
 // Dynamic shared memory of the packed kernel: the largest tile of every class.

@@ -36,10 +36,15 @@ std::vector<TileCfg> build_configs() {
 // Single kernel: 16 elements per thread and about 256 threads per CTA up to
 // 2^12; 32 elements per thread (256 / 512 threads, one transform per CTA)
 // for 2^13 and 2^14.
-// Four-step: N2 = 2^floor(log2 N / 2) column DFTs; column tiles as wide as
-// 512 threads allow; row tiles of 8 rows (N1 <= 2^9) or 4 rows (larger);
-// chunks of 2^26 elements.
+// Four-step (lengths without a tuned entry): N2 = 2^floor(log2 N / 2) column
+// DFTs; column tiles as wide as 512 threads allow; row tiles of 8 rows
+// (N1 <= 2^9) or 4 rows (larger); chunks of 2^27 elements (1 GiB scratch).
 const TileCfg* default_single(int logm) {
+  // autotuner winners on a GB300 (1 GiB batches): log2 M -> (log2 E, log2 C)
+  static const int tuned[][3] = {{10, 4, 1}, {11, 4, 0}, {12, 5, 0}, {13, 5, 0}, {14, 5, 0}};
+  for (const auto& t : tuned)
+    if (t[0] == logm)
+      if (const TileCfg* c = find_tile(STEP_SINGLE, logm, t[1], 4, t[2])) return c;
   const TileCfg* best = nullptr;
   const int want_e = logm >= 13 ? 5 : std::min(4, logm);
   for (const TileCfg& c : tile_configs()) {
@@ -216,14 +221,27 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     return true;
   }
 
-  // four-step
-  int logn2 = choice.logn2 >= 0 ? choice.logn2 : logn / 2;
+  // four-step.  Defaults: the autotuner's winners on a GB300 for 1 GiB
+  // batches, log2 N -> (log2 N2, column log2 E / log2 C, row log2 E / log2 C);
+  // other lengths split N2 = 2^floor(log2 N / 2).
+  static const int tuned4[][6] = {{15, 7, 4, 5, 4, 3},  {16, 7, 4, 5, 4, 2},  {17, 8, 4, 4, 4, 2},
+                                  {18, 9, 4, 4, 4, 2},  {19, 10, 4, 3, 4, 2}, {20, 9, 4, 4, 4, 2},
+                                  {21, 10, 4, 3, 4, 2}, {22, 10, 4, 3, 4, 2}, {23, 11, 5, 3, 5, 2},
+                                  {24, 12, 5, 2, 5, 2}};
+  const int* td = nullptr;
+  if (!tc && choice.logn2 < 0 && choice.col_loge < 0 && choice.row_loge < 0)
+    for (const auto& t : tuned4)
+      if (t[0] == logn) td = t;
+  int logn2 = choice.logn2 >= 0 ? choice.logn2 : (td ? td[1] : logn / 2);
   int logn1 = logn - logn2;
   const TileCfg* col = nullptr;
   const TileCfg* row = nullptr;
   if (tc) {
     col = find_tc(STEP_COL, logn2, choice.col_logc);
     row = find_tc(STEP_ROW, logn1, choice.row_logc);
+  } else if (td) {
+    col = find_tile(STEP_COL, logn2, td[2], 4, td[3]);
+    row = find_tile(STEP_ROW, logn1, td[4], 4, td[5]);
   } else {
     if (choice.col_loge >= 0)
       col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
@@ -242,7 +260,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     set_err(err, "four-step chunk wider than the transform (N1 = 2^%lld, N2 = 2^%lld)", logn1, logn2);
     return false;
   }
-  long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (1LL << 26) / n);
+  long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (1LL << 27) / n);
   chunk = std::min(chunk, batch);
   p.scratch_elems = chunk * n;
   for (long long b0 = 0; b0 < batch; b0 += chunk) {

@@ -37,7 +37,7 @@ std::vector<StreamDesc>& stream_table() {
   static std::vector<StreamDesc> t = [] {
     std::vector<StreamDesc> v;
 #define ESTL_XS(LOGN, CM, CE, CC, RM, RE, RC) \
-  v.push_back(sdesc<ColKernel<CM, CE, 4, CC>, RowKernel<RM, RE, 4, RC>>(LOGN));
+  v.push_back(sdesc<ColKernel<CM, CE, 4, CC>, RemapRowKernel<RM, RE, 4, RC>>(LOGN));
 #include "stream_list.inc"
     return v;
   }();

@@ -281,7 +281,7 @@ const std::vector<EmuStreamKernel>& emu_stream_kernels() {
   static const std::vector<EmuStreamKernel> v = [] {
     std::vector<EmuStreamKernel> k;
 #define ESTL_XS(LOGN, CM, CE, CC, RM, RE, RC) \
-  k.push_back(mks<ColKernel<CM, CE, 4, CC>, RowKernel<RM, RE, 4, RC>>(LOGN));
+  k.push_back(mks<ColKernel<CM, CE, 4, CC>, RemapRowKernel<RM, RE, 4, RC>>(LOGN));
 #include "stream_list.inc"
     return k;
   }();

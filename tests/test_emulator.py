@@ -140,9 +140,11 @@ def test_plan_shapes(emu):
     assert d["hbm_passes"] == 1 and d["launches"] == 1 and d["kernels"][0]["kind"] == "single"
     d = describe(emu, 1 << 20, 128)
     assert d["hbm_passes"] == 2 and d["kernels"][0]["kind"] == "col" and d["kernels"][1]["kind"] == "row"
-    assert d["scratch_bytes"] <= 512 << 20
-    d = describe(emu, 1 << 24, 8)
-    assert d["launches"] == 4  # 512 MiB scratch = four 2^24-point transforms per chunk, 2 launches per chunk
+    assert d["scratch_bytes"] <= 1 << 30
+    d = describe(emu, 1 << 24, 16)
+    assert d["launches"] == 4  # 1 GiB scratch = eight 2^24-point transforms per chunk, 2 launches per chunk
+    # the tuned default of 2^24: 2^12 x 2^12 with 32-element column and row tiles of 4 columns / rows
+    assert [(k["logm"], k["loge"], k["logc"]) for k in d["kernels"]] == [(12, 5, 2), (12, 5, 2)]
 
 
 def test_rejects_bad_sizes(emu):
