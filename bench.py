@@ -413,6 +413,49 @@ def bench_split_precision(estl, torch):
     return out
 
 
+def bench_fft2d(estl, torch):
+    """2D transforms (FFT2D<D>, FFT.h:54-84): 1 GiB of ydim x xdim arrays,
+    forward + backward per step; rel-L2 of the first array against numpy's FP64
+    fft2.  Two HBM passes (rows, then columns in place)."""
+    import numpy as np
+    out = {"workload": "C2C FP32 2D forward + backward, 2^27 complex64 per direction, uniform[-1,1) seed 6",
+           "method": "CUDA events over 5 steps after 2 warm-up steps; inputs larger than L2"}
+    st = torch.cuda.Stream()
+    for xdim, ydim in ((4096, 4096), (1024, 1024), (16384, 256)):
+        batch = (1 << 27) // (xdim * ydim)
+        g = torch.Generator(device="cuda").manual_seed(6)
+        x = torch.view_as_complex((torch.rand((xdim * ydim * batch, 2), device="cuda", generator=g) * 2 - 1).contiguous())
+        y, z = torch.empty_like(x), torch.empty_like(x)
+        f = estl.Plan2D(xdim, ydim, batch, estl.FORWARD)
+        b = estl.Plan2D(xdim, ydim, batch, estl.BACKWARD)
+        for _ in range(2):
+            f.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+            b.execute_ptr(y.data_ptr(), z.data_ptr(), st.cuda_stream)
+        st.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(5):
+            f.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+            b.execute_ptr(y.data_ptr(), z.data_ptr(), st.cuda_stream)
+        e1.record(st)
+        st.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        x0 = x[: xdim * ydim].view(ydim, xdim).cpu().numpy().astype(np.complex128)
+        ref = np.fft.fft2(x0)
+        y0 = y[: xdim * ydim].view(ydim, xdim).cpu().numpy().astype(np.complex128)
+        err = float(np.sqrt(np.sum(np.abs(y0 - ref) ** 2) / np.sum(np.abs(ref) ** 2)))
+        rt = float(np.sqrt(np.sum(np.abs(z[: xdim * ydim].view(ydim, xdim).cpu().numpy() / (xdim * ydim) - x0) ** 2) /
+                           np.sum(np.abs(x0) ** 2)))
+        d = f.describe()
+        out[f"{xdim}x{ydim}"] = {"batch": batch, "ms_fwd_bwd": round(ms, 3),
+                                  "gbs": round(2 * 16 * xdim * ydim * batch / (ms * 1e-3) / 1e9, 1),
+                                  "hbm_passes": d["hbm_passes"], "rel_l2_fwd": float(f"{err:.3e}"),
+                                  "rel_l2_roundtrip": float(f"{rt:.3e}"), "kernels": d["kernels"]}
+        f.close()
+        b.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -616,7 +659,8 @@ def main():
     configs = {}
     if rank == 0 and not args.no_configs:
         for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
-                        ("split_precision", bench_split_precision), ("served_conv", bench_served_conv)):
+                        ("split_precision", bench_split_precision), ("fft2d", bench_fft2d),
+                        ("served_conv", bench_served_conv)):
             try:
                 configs[key] = fn(estl, torch)
             except Exception as ex:  # reported, never silently dropped

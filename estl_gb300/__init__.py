@@ -128,7 +128,7 @@ class Plan:
         check(lib().estl_execute_host(self._h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(out.ctypes.data)))
         return out
 
-    KERNEL_KINDS = ("single", "col", "row", "copy", "stream")
+    KERNEL_KINDS = ("single", "col", "row", "copy", "stream", "column")
 
     def set_profiling(self, enable=True):
         """Bracket every launch with CUDA events (per-kernel timers)."""
@@ -153,6 +153,19 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Plan2D(Plan):
+    """`batch` 2D transforms of ydim rows by xdim columns (row-major, x fastest):
+    the layout of ESTL's FFT2D<D>.  Powers of two, ydim <= 2^12, FP32."""
+
+    def __init__(self, xdim, ydim, batch=1, direction=FORWARD):
+        _ensure_init()
+        self.xdim, self.ydim = int(xdim), int(ydim)
+        self.n, self.batch, self.direction = self.xdim * self.ydim, int(batch), int(direction)
+        h = ctypes.c_void_p()
+        check(lib().estl_plan2d_create(self.xdim, self.ydim, self.batch, self.direction, PREC_FP32, ctypes.byref(h)))
+        self._h = h
 
 
 _plan_cache = {}

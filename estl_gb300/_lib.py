@@ -52,6 +52,7 @@ SIGNATURES = {
     "estl_max_batch": (_I64, [_I64]),
     "estl_plan_create": (_INT, [_I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
     "estl_plan_create_ex": (_INT, [_I64, _I64, _INT, _INT, _P, ctypes.POINTER(_P)]),
+    "estl_plan2d_create": (_INT, [_I64, _I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
     "estl_plan_destroy": (_INT, [_P]),
     "estl_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_plan_launches": (_I64, [_P]),

@@ -384,6 +384,8 @@ estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int pre
   return plan_create_impl(n, batch, direction, precision, options, plan);
 }
 
+static estl_status plan_finish(std::unique_ptr<estl_plan_s> p, int direction, estl_plan* plan);
+
 static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int precision,
                                     const estl_plan_options* opt, estl_plan* plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "plan output pointer is NULL");
@@ -428,6 +430,12 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
     dflt.split = precision;
     if (!make_plan(n, batch, dflt, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   }
+  return plan_finish(std::move(p), direction, plan);
+}
+
+// Device buffers, work list and ordering event of a plan whose layout is set.
+static estl_status plan_finish(std::unique_ptr<estl_plan_s> p, int direction, estl_plan* plan) {
+  estl_status s;
   p->direction = direction;
   p->sgn = direction == ESTL_FORWARD ? 1.f : -1.f;
   p->scratch_bytes = (size_t)p->layout.scratch_elems * sizeof(cf32);
@@ -454,6 +462,25 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
   }
   *plan = out;
   return ESTL_OK;
+}
+
+estl_status estl_plan2d_create(int64_t xdim, int64_t ydim, int64_t batch, int direction, int precision,
+                               estl_plan* plan) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "plan output pointer is NULL");
+  *plan = nullptr;
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  if (direction != ESTL_FORWARD && direction != ESTL_BACKWARD)
+    return fail(ESTL_INVALID_ARG, "direction must be ESTL_FORWARD (-1) or ESTL_BACKWARD (+1), got %d", direction);
+  if (precision != ESTL_PREC_FP32) return fail(ESTL_INVALID_ARG, "2D transforms run in FP32 (precision %d)", precision);
+  PlanChoice choice;
+  if (xdim > 0 && batch > 0 && ydim > 0) tuner_lookup(xdim, ydim * batch, &choice);  // the row FFTs' tuned plan
+  std::unique_ptr<estl_plan_s> p(new estl_plan_s);
+  std::string err;
+  if (!make_plan2d(xdim, ydim, batch, choice, &p->layout, &err) &&
+      !make_plan2d(xdim, ydim, batch, PlanChoice{}, &p->layout, &err))
+    return fail(xdim < 1 || ydim < 1 || batch < 1 ? ESTL_INVALID_ARG : ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  return plan_finish(std::move(p), direction, plan);
 }
 
 estl_status estl_plan_destroy(estl_plan plan) {
@@ -589,10 +616,9 @@ static estl_status host_pipeline_setup(estl_plan p) {
   long long chunk = std::max(1LL, (64LL << 20) / (8 * n));
   chunk = std::min(chunk, batch);
   std::string err;
-  if (!make_plan(n, chunk, p->layout.choice, &p->host_plan_full, &err))
-    return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  if (!make_plan_like(p->layout, chunk, &p->host_plan_full, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   long long tail = batch % chunk;
-  if (tail && !make_plan(n, tail, p->layout.choice, &p->host_plan_tail, &err))
+  if (tail && !make_plan_like(p->layout, tail, &p->host_plan_tail, &err))
     return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   if ((size_t)p->host_plan_full.scratch_elems * sizeof(cf32) > p->scratch_bytes)
     return fail(ESTL_DEVICE_ERROR, "chunk plan needs more scratch than the plan holds");

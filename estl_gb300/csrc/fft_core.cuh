@@ -488,7 +488,9 @@ struct SingleKernel {
 // columns n1 of one transform and runs their N2-point DFTs (M = N2), then
 // multiplies by w_N^{n1 k2} and writes S[k2 * N1 + n1].  Thread mapping is
 // column-fastest so both the loads and the stores move runs of C elements.
-template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
+// TW = false: the plain strided column FFT of a 2D transform (no four-step
+// twiddle, conjugated store of the inverse), in place on a [rows][N1] array.
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false, bool TW = true>
 struct ColKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
@@ -528,7 +530,12 @@ struct ColKernel {
     } else {
       run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     }
-    store_twiddled(v, out, n1, t, logn, bank);
+    if constexpr (TW) {
+      store_twiddled(v, out, n1, t, logn, bank);
+    } else {
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << logn1) + n1] = conj_if(v[j], sgn);
+    }
   }
 
   // Four-step twiddle and store: S[k2 * N1 + n1] = y[k2] * w_N^{n1 k2} for

@@ -8,7 +8,8 @@
 
 namespace estl {
 
-enum KernelKind { KIND_SINGLE = 0, KIND_COL = 1, KIND_ROW = 2 };
+// equal to the planner's StepKind values
+enum KernelKind { KIND_SINGLE = 0, KIND_COL = 1, KIND_ROW = 2, KIND_COLUMN = 5 };
 
 struct KernelDesc {
   int kind;
@@ -40,6 +41,7 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_PIPE_SINGLE(M, E, R, C) make_desc<PipeSingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C, 1)
 #define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
 #define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
+#define ESTL_COLUMN(M, E, C) make_desc<ColKernel<M, E, 4, C, false, false>>(KIND_COLUMN, M, E, 4, C)
 #define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
 #define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)
 #define ESTL_TC_ROW(M, C) make_desc<RowKernel<M, 4, 4, C, true>>(KIND_ROW, M, 4, 4, C, 0, 1)

@@ -24,6 +24,7 @@ static const KernelDesc kTable[] = {
 #define ESTL_X_COL(M, E, R, C) ESTL_COL(M, E, R, C),
 #define ESTL_X_PIPE_COL(M, E, R, C) ESTL_PIPE_COL(M, E, R, C),
 #define ESTL_X_TC_COL(M, C) ESTL_TC_COL(M, C),
+#define ESTL_X_COLUMN(M, E, C) ESTL_COLUMN(M, E, C),
 #include "kernel_list.inc"
 };
 

@@ -24,6 +24,7 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) v.push_back(cfg_of<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_COLUMN(M, E, C) v.push_back(cfg_of<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_ROW(M, C) v.push_back(cfg_of<RowKernel<M, 4, 4, C, true>>(STEP_ROW, M, 4, 4, C, 0, 1));
@@ -280,6 +281,56 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   return true;
 }
 
+bool make_plan2d(long long xdim, long long ydim, long long batch, const PlanChoice& choice, Plan1D* out,
+                 std::string* err) {
+  const int logx = ilog2_exact(xdim), logy = ilog2_exact(ydim);
+  if (logx < 0 || logy < 0) {
+    set_err(err, "2D dimensions must be powers of two (got %lld x %lld)", xdim, ydim);
+    return false;
+  }
+  if (logy > kColumnMaxLog || logx + logy > kPlan2dMaxLog) {
+    set_err(err, "2D transform needs ydim <= 2^12 and xdim * ydim <= 2^26 (got 2^%lld rows, 2^%lld points)", logy,
+            logx + logy);
+    return false;
+  }
+  if (choice.split != 0) {
+    set_err(err, "2D transforms run in FP32 (split precision %lld requested)", choice.split);
+    return false;
+  }
+  if (batch < 1) {
+    set_err(err, "batch must be >= 1 (got %lld)", batch);
+    return false;
+  }
+  Plan1D p;
+  if (!make_plan(xdim, ydim * batch, choice, &p, err)) return false;  // the row FFTs
+  if (logy > 0) {
+    const TileCfg* col = nullptr;
+    for (const TileCfg& c : tile_configs())
+      if (c.kind == STEP_COLUMN && c.logm == logy && c.logc <= logx && (!col || c.logc > col->logc)) col = &c;
+    if (!col) {
+      set_err(err, "no column tile instantiated for ydim = 2^%lld", logy);
+      return false;
+    }
+    const long long total = xdim * ydim * batch;
+    Step s{STEP_COLUMN, col->logm, col->loge, col->logr, col->logc, batch << (logx - col->logc), BUF_OUT, BUF_OUT,
+           0, total, 0, total, batch, logx + logy};
+    p.steps.push_back(s);
+    p.hbm_passes += 1;
+  }
+  p.n = xdim * ydim;
+  p.batch = batch;
+  p.logn = logx + logy;
+  p.xdim = xdim;
+  p.ydim = ydim;
+  *out = p;
+  return true;
+}
+
+bool make_plan_like(const Plan1D& base, long long batch, Plan1D* out, std::string* err) {
+  if (base.xdim > 0) return make_plan2d(base.xdim, base.ydim, batch, base.choice, out, err);
+  return make_plan(base.n, batch, base.choice, out, err);
+}
+
 std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
   std::vector<PlanChoice> out;
   int logn = ilog2_exact(n);
@@ -340,20 +391,26 @@ std::string Plan1D::describe() const {
   char buf[512];
   static const char* splits[] = {"fp32", "fp16x2", "bf16x2", "bf16x3"};
   std::snprintf(buf, sizeof buf,
-                "{\"n\": %lld, \"batch\": %lld, \"precision\": \"%s\", \"hbm_passes\": %d, \"launches\": %zu, "
-                "\"scratch_bytes\": %lld, \"kernels\": [",
-                n, batch, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes, steps.size(),
-                scratch_elems * 8);
+                "{\"n\": %lld, \"batch\": %lld, \"xdim\": %lld, \"ydim\": %lld, \"precision\": \"%s\", "
+                "\"hbm_passes\": %d, \"launches\": %zu, \"scratch_bytes\": %lld, \"kernels\": [",
+                n, batch, xdim, ydim, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes,
+                steps.size(), scratch_elems * 8);
   s += buf;
-  const char* names[] = {"single", "col", "row", "copy", "stream"};
+  const char* names[] = {"single", "col", "row", "copy", "stream", "column"};
+  // the first two steps (one chunk), and for 2D plans the column step
+  std::vector<size_t> idx;
+  for (size_t i = 0; i < steps.size() && i < 2; ++i)
+    if (!(xdim > 0 && steps[i].kind == STEP_COLUMN)) idx.push_back(i);
+  if (xdim > 0 && !steps.empty() && steps.back().kind == STEP_COLUMN) idx.push_back(steps.size() - 1);
   int shown = 0;
-  for (size_t i = 0; i < steps.size() && shown < 2; ++i, ++shown) {
+  for (size_t i : idx) {
     const Step& st = steps[i];
     std::snprintf(buf, sizeof buf,
                   "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"tiles\": %lld, \"pipe\": %d, "
                   "\"tc\": %d}",
                   shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe, st.tc);
     s += buf;
+    ++shown;
   }
   s += "]}";
   return s;

@@ -16,8 +16,10 @@
 
 namespace estl {
 
-enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_STREAM = 4 };
-constexpr int kStepKinds = 5;
+// STEP_COLUMN: the column pass of a 2D transform (strided column DFTs, no
+// four-step twiddle), in place on the output.
+enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_STREAM = 4, STEP_COLUMN = 5 };
+constexpr int kStepKinds = 6;
 enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_SCRATCH = 2 };
 
 struct TileCfg {
@@ -75,6 +77,7 @@ struct PlanChoice {
 struct Plan1D {
   long long n = 0, batch = 0;
   int logn = 0;
+  long long xdim = 0, ydim = 0;  // 2D plans (make_plan2d): n = xdim * ydim; 0 for 1D
   PlanChoice choice;
   std::vector<Step> steps;
   long long scratch_elems = 0;
@@ -91,6 +94,17 @@ constexpr int kMaxLogN = 24;
 // Returns false (with *err set) when n is not a power of two in [1, 2^24] or
 // the choice names no instantiated kernel.
 bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* out, std::string* err);
+
+// 2D transforms of ydim rows by xdim columns (row-major, x fastest), the
+// layout of ESTL's FFT2D<D> (FFT.h:54-84): xdim-point row FFTs (any 1D plan),
+// then ydim-point column FFTs in place (ydim <= 2^12, xdim * ydim <= 2^26).
+constexpr int kColumnMaxLog = 12;
+constexpr int kPlan2dMaxLog = 26;
+bool make_plan2d(long long xdim, long long ydim, long long batch, const PlanChoice& choice, Plan1D* out,
+                 std::string* err);
+
+// The plan of the same transform (1D or 2D) for another batch count.
+bool make_plan_like(const Plan1D& base, long long batch, Plan1D* out, std::string* err);
 
 // Candidate choices for (n, batch), default first (autotuner search space).
 std::vector<PlanChoice> plan_candidates(long long n, long long batch);

@@ -124,6 +124,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
     if (describe.find("\"row\"") != std::string::npos) kinds.push_back(2);
     if (describe.find("\"copy\"") != std::string::npos) kinds.push_back(3);
     if (describe.find("\"stream\"") != std::string::npos) kinds.push_back(4);
+    if (describe.find("\"column\"") != std::string::npos) kinds.push_back(5);
     kernelTimers.resize(kinds.size());
     const size_t bytes = sizeof(D) * 2 * (size_t)this->size * this->batchCount;
     registered = estl_host_register(arrays->in->getData(), bytes) == ESTL_OK &&
@@ -139,7 +140,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
   }
 
   virtual std::string getKernelInfo(int kernel) {
-    static const char* names[] = {"tile", "column", "row", "copy", "streamed four-step"};
+    static const char* names[] = {"tile", "column", "row", "copy", "streamed four-step", "2D column"};
     return (kernel >= 0 && kernel < (int)kinds.size()) ? names[kinds[kernel]] : "";
   }
 
@@ -176,6 +177,40 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
   std::string describe;
   std::vector<int> kinds;
   double lastMs[ESTL_KERNEL_KINDS];
+};
+
+/* FFT2D_CUDA<D> is an FFT2D<D> (FFT.h:54-84): the same `data` array of
+ * xDim * yDim Complex<D> (row-major, x fastest) and the same in-place
+ * execute(), which the reference runs as one FFT object per row and per
+ * column with per-element copies.  Here execute() is one 2D plan
+ * (estl_plan2d_create): row FFTs and column FFTs on the device, the array
+ * copied in and out once.  Convolution2D_FFT (Convolution.h:102-104) builds
+ * its three FFT2D objects this way when it constructs FFT2D_CUDA instead. */
+template <class D>
+class FFT2D_CUDA : public FFT2D<D> {
+ public:
+  FFT2D_CUDA(int iXDim, int iYDim, bool iForward = true)
+      : FFT2D<D>(iXDim, iYDim, NULL, iForward), plan(NULL), out((size_t)iXDim * iYDim) {
+    typedef char only_float_is_supported[(sizeof(D) == sizeof(float) && sizeof(Complex<D>) == 2 * sizeof(D)) ? 1 : -1];
+    (void)sizeof(only_float_is_supported);
+    GpuAlgorithm::ensureInit();
+    estlCheck(estl_plan2d_create(iXDim, iYDim, 1, iForward ? ESTL_FORWARD : ESTL_BACKWARD, ESTL_PREC_FP32, &plan),
+              "estl_plan2d_create");
+  }
+
+  virtual void execute() {
+    estlCheck(estl_execute_host(plan, reinterpret_cast<const float*>(this->data), reinterpret_cast<float*>(&out[0])),
+              "estl_execute_host");
+    for (size_t q = 0; q < out.size(); ++q) this->data[q] = out[q];
+  }
+
+  virtual ~FFT2D_CUDA() {
+    if (plan) estl_plan_destroy(plan);
+  }
+
+ private:
+  estl_plan plan;
+  std::vector<Complex<D> > out;
 };
 
 #endif  // FFT_CUDA_H

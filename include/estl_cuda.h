@@ -113,6 +113,16 @@ typedef struct estl_plan_options {
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
                                 const estl_plan_options* options, estl_plan* plan);
 
+/* 2D transforms: `batch` arrays of ydim rows by xdim columns, row-major (x
+ * fastest), the layout of ESTL's FFT2D<D> (FFT.h:54-84), which runs xdim-point
+ * FFTs over the rows and then ydim-point FFTs over the columns, in place.
+ * Here: one row pass (any 1D plan of xdim, batched over ydim * batch rows)
+ * and one column pass in place on the output.  Powers of two, ydim <= 2^12,
+ * xdim * ydim <= 2^26, FP32.  Executed with estl_execute / estl_execute_host
+ * like a 1D plan of n = xdim * ydim. */
+estl_status estl_plan2d_create(int64_t xdim, int64_t ydim, int64_t batch, int direction, int precision,
+                               estl_plan* plan);
+
 /* Free the plan and its device buffers (FFT_OpenCL_Contiguous.h:186-191). */
 estl_status estl_plan_destroy(estl_plan plan);
 
@@ -156,11 +166,11 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out);
 estl_status estl_plan_set_profiling(estl_plan plan, int enable);
 
 /* Per kernel kind (index 0 single-tile, 1 column pass, 2 row pass, 3 device
- * copy, 4 streamed four-step): launches, summed device milliseconds and
+ * copy, 4 streamed four-step, 5 2D column pass): launches, summed device milliseconds and
  * summed algorithmic bytes (16 bytes per complex element read and written).
  * Waits for the profiled launches to finish.  Arrays have ESTL_KERNEL_KINDS
  * entries; any may be NULL. */
-#define ESTL_KERNEL_KINDS 5
+#define ESTL_KERNEL_KINDS 6
 estl_status estl_plan_kernel_stats(estl_plan plan, int64_t* launches, double* total_ms, double* bytes);
 
 /* Page-lock / unlock host memory for estl_execute_host. */

@@ -57,8 +57,8 @@ class FFT2D {
   FFT2D(int x, int y, FFTFactory<D>* f, bool fwd = true) : xDim(x), yDim(y), fftFactory(f), forward(fwd) {
     data = new Complex<D>[(size_t)x * y];
   }
-  ~FFT2D() { delete[] data; }
-  void execute() {
+  virtual ~FFT2D() { delete[] data; }
+  virtual void execute() {
     FFT<D>* fx = fftFactory->newFFT(xDim, forward);
     for (int y = 0; y < yDim; ++y) {
       for (int x = 0; x < xDim; ++x) fx->setData(x, data[y * xDim + x]);

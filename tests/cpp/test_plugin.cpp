@@ -87,7 +87,8 @@ static void known_answer_sweep(FFTFactory<D>* f, int max_b, int max_m) {
 
 static void fft2d_against_direct(FFTFactory<D>* f, int mx, int my) {
   int X = 1 << mx, Y = 1 << my;
-  FFT2D<D> t(X, Y, f);
+  FFT2D<D>* tp = f ? new FFT2D<D>(X, Y, f) : new FFT2D_CUDA<D>(X, Y);
+  FFT2D<D>& t = *tp;
   std::vector<C> in((size_t)X * Y);
   unsigned s = 12345;
   for (int q = 0; q < X * Y; ++q) {
@@ -111,7 +112,8 @@ static void fft2d_against_direct(FFTFactory<D>* f, int mx, int my) {
         }
       check_close(t.data[(size_t)ky * X + kx], C((D)sr, (D)si), (double)X * Y, "2D");
     }
-  printf("FFT2D %dx%d checked against a direct DFT\n", X, Y);
+  printf("%s %dx%d checked against a direct DFT\n", f ? "FFT2D" : "FFT2D_CUDA", X, Y);
+  delete tp;
 }
 
 static void backward_every_batch(FFTFactory<D>* f, int m, int B) {
@@ -146,6 +148,8 @@ int main(int argc, char** argv) {
       backward_every_batch(factories[i], 10, 8);
       backward_every_batch(factories[i], 17, 3);
     }
+    fft2d_against_direct(NULL, 3, 4);
+    fft2d_against_direct(NULL, 6, 5);
   } catch (std::exception& e) {
     printf("exception: %s\n", e.what());
     return 2;

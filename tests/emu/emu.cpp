@@ -75,6 +75,7 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) k.push_back(mk<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_COLUMN(M, E, C) k.push_back(mk<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_ROW(M, C) k.push_back(mk<RowKernel<M, 4, 4, C, true>>(STEP_ROW, M, 4, 4, C, 0, 1));
@@ -318,6 +319,8 @@ extern "C" {
 // choice: 12 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
+static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen);
+
 int emu_plan_run(long long n, long long batch, const int* choice, int sign, const float* in, float* out, char* err,
                  int errlen) {
   Plan1D p;
@@ -326,6 +329,23 @@ int emu_plan_run(long long n, long long batch, const int* choice, int sign, cons
     set_err(err, errlen, e);
     return 2;
   }
+  return run_plan(p, sign, in, out, err, errlen);
+}
+
+// 2D plan (make_plan2d) of batch arrays of ydim rows by xdim columns.
+int emu_plan2d_run(long long xdim, long long ydim, long long batch, int sign, const float* in, float* out, char* err,
+                   int errlen) {
+  Plan1D p;
+  std::string e;
+  if (!make_plan2d(xdim, ydim, batch, PlanChoice{}, &p, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  return run_plan(p, sign, in, out, err, errlen);
+}
+
+static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen) {
+  const long long n = p.n, batch = p.batch;
   {
     std::lock_guard<std::mutex> g(g_msg_mu);
     g_msg.clear();
