@@ -15,7 +15,8 @@ created for (size, batchCount, forward) and executed repeatedly.
 import ctypes
 import json
 
-from ._lib import (BACKWARD, FORWARD, PREC_FP32, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, PREC_SPLIT_FP16, EstlError,
+from ._lib import (BACKWARD, FORWARD, LAYOUT_BLOCK_PLANAR, LAYOUT_INTERLEAVED, LAYOUT_SPLIT, PREC_FP32,
+                   PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, PREC_SPLIT_FP16, EstlError,
                    PlanOptions, check, lib)
 
 __all__ = ["init", "shutdown", "Plan", "fft", "autotune", "max_batch", "memory_usage", "EstlError",
@@ -121,6 +122,25 @@ class Plan:
         if out is None:
             out = torch.empty_like(x)
         self.execute_ptr(x.data_ptr(), out.data_ptr(), _stream_handle(stream))
+        return out
+
+    def execute_layout(self, x, layout, out=None, stream=None):
+        """x: float32 CUDA tensor holding the batch in `layout` (LAYOUT_BLOCK_PLANAR /
+        LAYOUT_SPLIT / LAYOUT_INTERLEAVED), layout_floats(layout, n * batch) floats."""
+        import torch
+        floats = int(lib().estl_layout_floats(int(layout), self.n * self.batch))
+        if x.dtype != torch.float32 or not x.is_cuda or not x.is_contiguous() or x.numel() < floats:
+            raise EstlError(1, f"input must be a contiguous float32 CUDA tensor of >= {floats} floats")
+        if out is None:
+            out = torch.zeros(floats, dtype=torch.float32, device=x.device)
+        check(lib().estl_execute_layout(self._h, int(layout), ctypes.c_void_p(x.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(_stream_handle(stream))))
+        return out
+
+    def execute_host_layout(self, x, out, layout):
+        """Host float32 numpy arrays in `layout` (see execute_layout)."""
+        check(lib().estl_execute_host_layout(self._h, int(layout), ctypes.c_void_p(x.ctypes.data),
+                                             ctypes.c_void_p(out.ctypes.data)))
         return out
 
     def execute_host(self, x, out):

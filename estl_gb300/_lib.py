@@ -23,6 +23,9 @@ STATUS = {
 
 FORWARD = -1
 BACKWARD = +1
+LAYOUT_INTERLEAVED = 0
+LAYOUT_BLOCK_PLANAR = 1  # 32 real parts then 32 imaginary parts per block (PlannarizedDataInterface)
+LAYOUT_SPLIT = 2         # all real parts, then all imaginary parts
 PREC_FP32 = 0
 PREC_SPLIT_FP16 = 1    # fp16 hi+lo tensor-core radix-16 stages (butterflies scaled by powers of two)
 PREC_SPLIT_BF16 = 2    # bf16 hi+lo
@@ -53,6 +56,9 @@ SIGNATURES = {
     "estl_plan_create": (_INT, [_I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
     "estl_plan_create_ex": (_INT, [_I64, _I64, _INT, _INT, _P, ctypes.POINTER(_P)]),
     "estl_plan2d_create": (_INT, [_I64, _I64, _I64, _INT, _INT, ctypes.POINTER(_P)]),
+    "estl_layout_floats": (_I64, [_INT, _I64]),
+    "estl_execute_layout": (_INT, [_P, _INT, _P, _P, _P]),
+    "estl_execute_host_layout": (_INT, [_P, _INT, _P, _P]),
     "estl_plan_destroy": (_INT, [_P]),
     "estl_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_plan_launches": (_I64, [_P]),

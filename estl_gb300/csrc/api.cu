@@ -241,6 +241,14 @@ struct estl_plan_s {
   void* host_aux[2] = {nullptr, nullptr};  // streamed plans: work lists of the chunk plans
   size_t host_aux_bytes[2] = {0, 0};
   StreamAux host_saux[2] = {};
+  // other host layouts (estl_execute_layout / estl_execute_host_layout):
+  // interleaved staging of the device path, raw-layout staging of the host path
+  cf32* lay_in = nullptr;
+  cf32* lay_out = nullptr;
+  size_t lay_bytes = 0;
+  float* hlay_in[2] = {nullptr, nullptr};
+  float* hlay_out[2] = {nullptr, nullptr};
+  size_t hlay_bytes = 0;
   // per-launch profiling (estl_plan_set_profiling)
   bool profiling = false;
   struct Rec {
@@ -262,6 +270,12 @@ static void plan_release(estl_plan p) {
   dev_free(p->scratch, p->scratch_bytes);
   dev_free(p->aux, p->aux_bytes);
   for (int s = 0; s < 2; ++s) dev_free(p->host_aux[s], p->host_aux_bytes[s]);
+  dev_free(p->lay_in, p->lay_bytes);
+  dev_free(p->lay_out, p->lay_bytes);
+  for (int s = 0; s < 2; ++s) {
+    dev_free(p->hlay_in[s], p->hlay_bytes);
+    dev_free(p->hlay_out[s], p->hlay_bytes);
+  }
   for (int s = 0; s < 2; ++s) {
     dev_free(p->din[s], p->stage_bytes);
     dev_free(p->dout[s], p->stage_bytes);
@@ -531,6 +545,61 @@ static estl_status check_buffers(const void* in, const void* out) {
   return ESTL_OK;
 }
 
+// ---- other host layouts ---------------------------------------------------
+// ESTL_LAYOUT_BLOCK_PLANAR: complex element i has its real part at float
+// ((i >> 5) << 6) | (i & 31) and its imaginary part 32 floats later
+// (PlannarizedComplexArray<5, D>, Complex.h:34-48,97-130).
+// ESTL_LAYOUT_SPLIT: all real parts, then all imaginary parts
+// (ComplexArray(n, plannar = true), Complex.h:156-192).
+__device__ __forceinline__ long long layout_pos(long long i, int elem, int layout, long long total) {
+  if (layout == ESTL_LAYOUT_BLOCK_PLANAR) return ((i >> 5) << 6) | ((long long)elem << 5) | (i & 31);
+  return (long long)elem * total + i;
+}
+
+__global__ void layout_in_kernel(const float* __restrict__ in, cf32* __restrict__ out, long long total, int layout) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x)
+    out[i] = cf32{in[layout_pos(i, 0, layout, total)], in[layout_pos(i, 1, layout, total)]};
+}
+
+// Writes every element; in the last 32-element block of a block-planar array
+// the real slots past the end are zeroed (those imaginary slots lie past the
+// array's last used float and are not touched).
+__global__ void layout_out_kernel(const cf32* __restrict__ in, float* __restrict__ out, long long total, int layout) {
+  const long long end = layout == ESTL_LAYOUT_BLOCK_PLANAR ? ((total + 31) & ~31LL) : total;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < end; i += (long long)gridDim.x * blockDim.x) {
+    if (i < total) {
+      const cf32 v = in[i];
+      out[layout_pos(i, 0, layout, total)] = v.x;
+      out[layout_pos(i, 1, layout, total)] = v.y;
+    } else {
+      out[layout_pos(i, 0, layout, total)] = 0.f;
+    }
+  }
+}
+
+// Floats of a host array in `layout` holding `total` complex elements: up to
+// and including the last float any element uses.
+static long long layout_floats(int layout, long long total) {
+  if (total <= 0) return 0;
+  if (layout == ESTL_LAYOUT_BLOCK_PLANAR) return (((total - 1) >> 5) << 6) + 32 + ((total - 1) & 31) + 1;
+  return 2 * total;
+}
+
+static int layout_grid(long long total) {
+  const long long blocks = (total + 255) / 256;
+  return (int)std::max(1LL, std::min<long long>(blocks, 152LL * 16));
+}
+
+static estl_status launch_layout_in(int layout, const float* src, cf32* dst, long long total, cudaStream_t st) {
+  layout_in_kernel<<<layout_grid(total), 256, 0, st>>>(src, dst, total, layout);
+  return check_cuda(cudaGetLastError(), "layout conversion (in)");
+}
+
+static estl_status launch_layout_out(int layout, const cf32* src, float* dst, long long total, cudaStream_t st) {
+  layout_out_kernel<<<layout_grid(total), 256, 0, st>>>(src, dst, total, layout);
+  return check_cuda(cudaGetLastError(), "layout conversion (out)");
+}
+
 static estl_status pool_event(estl_plan p, cudaEvent_t* e) {
   if (!p->event_pool.empty()) {
     *e = p->event_pool.back();
@@ -580,12 +649,25 @@ static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const Stre
   return ESTL_OK;
 }
 
+// Conversions of the other host layouts around a plan: `src` (layout) ->
+// the plan's interleaved input, its interleaved output -> `dst` (layout).
+struct LayoutIO {
+  int layout;
+  const float* src;
+  float* dst;
+  long long total;  // complex elements
+};
+
 static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, const LayoutIO* io = nullptr) {
   std::lock_guard<std::mutex> g(plan->mu);
   estl_status s;
   if (plan->done_recorded) {
     s = check_cuda(cudaStreamWaitEvent(stream, plan->done, 0), "cudaStreamWaitEvent");
+    if (s != ESTL_OK) return s;
+  }
+  if (io) {
+    s = launch_layout_in(io->layout, io->src, const_cast<cf32*>(in), io->total, stream);
     if (s != ESTL_OK) return s;
   }
   if (plan->profiling)
@@ -593,6 +675,10 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const Strea
   else
     s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream, aux);
   if (s != ESTL_OK) return s;
+  if (io) {
+    s = launch_layout_out(io->layout, out, io->dst, io->total, stream);
+    if (s != ESTL_OK) return s;
+  }
   s = check_cuda(cudaEventRecord(plan->done, stream), "cudaEventRecord");
   if (s != ESTL_OK) return s;
   plan->done_recorded = true;
@@ -685,6 +771,108 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
     if ((s = check_cuda(cudaEventRecord(plan->ev_d2h[k], sd), "record")) != ESTL_OK) return s;
   }
   return check_cuda(cudaStreamSynchronize(sd), "cudaStreamSynchronize");
+}
+
+estl_status estl_execute_layout(estl_plan plan, int layout, const float* d_in, float* d_out, void* stream) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  if (layout == ESTL_LAYOUT_INTERLEAVED) return estl_execute(plan, d_in, d_out, stream);
+  if (layout != ESTL_LAYOUT_BLOCK_PLANAR && layout != ESTL_LAYOUT_SPLIT)
+    return fail(ESTL_INVALID_ARG, "unknown layout %d", layout);
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  if (!d_in || !d_out || ((uintptr_t)d_in & 3) || ((uintptr_t)d_out & 3) || d_in == d_out)
+    return fail(ESTL_INVALID_ARG, "need distinct, 4-byte aligned device buffers");
+  const long long total = plan->layout.n * plan->layout.batch;
+  {
+    std::lock_guard<std::mutex> g(plan->mu);
+    if (!plan->lay_in) {
+      const size_t bytes = (size_t)total * sizeof(cf32);
+      s = dev_alloc((void**)&plan->lay_in, bytes, "layout staging");
+      if (s == ESTL_OK) s = dev_alloc((void**)&plan->lay_out, bytes, "layout staging");
+      if (s != ESTL_OK) {
+        dev_free(plan->lay_in, bytes);
+        plan->lay_in = nullptr;
+        return s;
+      }
+      plan->lay_bytes = bytes;
+    }
+  }
+  LayoutIO io{layout, d_in, d_out, total};
+  return run_plan_on(plan, plan->layout, &plan->saux, plan->lay_in, plan->lay_out, (cudaStream_t)stream, &io);
+}
+
+estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_in, float* h_out) {
+  if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  if (layout == ESTL_LAYOUT_INTERLEAVED) return estl_execute_host(plan, h_in, h_out);
+  if (layout != ESTL_LAYOUT_BLOCK_PLANAR && layout != ESTL_LAYOUT_SPLIT)
+    return fail(ESTL_INVALID_ARG, "unknown layout %d", layout);
+  estl_status s = require_init();
+  if (s != ESTL_OK) return s;
+  if (!h_in || !h_out || h_in == h_out) return fail(ESTL_INVALID_ARG, "need distinct host buffers");
+  s = host_pipeline_setup(plan);
+  if (s != ESTL_OK) return s;
+  const long long n = plan->layout.n, batch = plan->layout.batch, chunk = plan->host_chunk, total = n * batch;
+  if (!plan->hlay_in[0]) {
+    // raw-layout staging of one chunk (chunk * n is 0 mod 32 or the whole batch, so
+    // every block-planar chunk starts on a 32-element block)
+    const size_t bytes = (size_t)std::max(layout_floats(ESTL_LAYOUT_BLOCK_PLANAR, chunk * n), 2 * chunk * n) * 4;
+    for (int k = 0; k < 2 && s == ESTL_OK; ++k) {
+      s = dev_alloc((void**)&plan->hlay_in[k], bytes, "layout staging");
+      if (s == ESTL_OK) s = dev_alloc((void**)&plan->hlay_out[k], bytes, "layout staging");
+    }
+    plan->hlay_bytes = bytes;
+    if (s != ESTL_OK) return s;
+  }
+  const long long nchunks = (batch + chunk - 1) / chunk;
+  cudaStream_t sh = plan->st[0], sc = plan->st[1], sd = plan->st[2];
+  for (long long i = 0; i < nchunks; ++i) {
+    const int k = (int)(i & 1);
+    const long long b0 = i * chunk, cnt = std::min(chunk, batch - b0), e0 = b0 * n, ce = cnt * n;
+    const Plan1D& lay = cnt == chunk ? plan->host_plan_full : plan->host_plan_tail;
+    const StreamAux* aux = cnt == chunk ? &plan->host_saux[0] : &plan->host_saux[1];
+    if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sh, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
+    if (layout == ESTL_LAYOUT_BLOCK_PLANAR) {
+      s = check_cuda(cudaMemcpyAsync(plan->hlay_in[k], h_in + 2 * e0, (size_t)layout_floats(layout, ce) * 4,
+                                     cudaMemcpyHostToDevice, sh),
+                     "cudaMemcpyAsync(H2D)");
+    } else {  // split: the chunk's real parts, then its imaginary parts
+      s = check_cuda(cudaMemcpyAsync(plan->hlay_in[k], h_in + e0, (size_t)ce * 4, cudaMemcpyHostToDevice, sh),
+                     "cudaMemcpyAsync(H2D)");
+      if (s == ESTL_OK)
+        s = check_cuda(cudaMemcpyAsync(plan->hlay_in[k] + ce, h_in + total + e0, (size_t)ce * 4,
+                                       cudaMemcpyHostToDevice, sh),
+                       "cudaMemcpyAsync(H2D)");
+    }
+    if (s != ESTL_OK) return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_h2d[k], sh), "record")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_h2d[k], 0), "wait")) != ESTL_OK) return s;
+    if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_d2h[k], 0), "wait")) != ESTL_OK) return s;
+    LayoutIO io{layout, plan->hlay_in[k], plan->hlay_out[k], ce};
+    if ((s = run_plan_on(plan, lay, aux, plan->din[k], plan->dout[k], sc, &io)) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_comp[k], sc), "record")) != ESTL_OK) return s;
+    if ((s = check_cuda(cudaStreamWaitEvent(sd, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
+    if (layout == ESTL_LAYOUT_BLOCK_PLANAR) {
+      s = check_cuda(cudaMemcpyAsync(h_out + 2 * e0, plan->hlay_out[k], (size_t)layout_floats(layout, ce) * 4,
+                                     cudaMemcpyDeviceToHost, sd),
+                     "cudaMemcpyAsync(D2H)");
+    } else {
+      s = check_cuda(cudaMemcpyAsync(h_out + e0, plan->hlay_out[k], (size_t)ce * 4, cudaMemcpyDeviceToHost, sd),
+                     "cudaMemcpyAsync(D2H)");
+      if (s == ESTL_OK)
+        s = check_cuda(cudaMemcpyAsync(h_out + total + e0, plan->hlay_out[k] + ce, (size_t)ce * 4,
+                                       cudaMemcpyDeviceToHost, sd),
+                       "cudaMemcpyAsync(D2H)");
+    }
+    if (s != ESTL_OK) return s;
+    if ((s = check_cuda(cudaEventRecord(plan->ev_d2h[k], sd), "record")) != ESTL_OK) return s;
+  }
+  return check_cuda(cudaStreamSynchronize(sd), "cudaStreamSynchronize");
+}
+
+int64_t estl_layout_floats(int layout, int64_t total) {
+  if (layout == ESTL_LAYOUT_INTERLEAVED || layout == ESTL_LAYOUT_SPLIT) return total > 0 ? 2 * total : 0;
+  if (layout == ESTL_LAYOUT_BLOCK_PLANAR) return layout_floats(layout, total);
+  return -1;
 }
 
 estl_status estl_plan_set_profiling(estl_plan plan, int enable) {

@@ -92,10 +92,29 @@ class GpuAlgorithm {
   }
 };
 
+/* Host layout of a DataInterface type: SplitInterleavedDataInterface(n,
+ * false) is interleaved (the FFT_FFTW3 layout, FFT_FFTW3.h:24);
+ * PlannarizedDataInterface is block-planar (the FFT_OpenCL_Contiguous
+ * layout, FFT_OpenCL_Contiguous.h:28). */
+template <class DI>
+struct EstlLayoutOf {
+  enum { value = ESTL_LAYOUT_INTERLEAVED };
+  static DI* make(int n) { return new DI(n, false); }
+};
 template <class D>
+struct EstlLayoutOf<PlannarizedDataInterface<D> > {
+  enum { value = ESTL_LAYOUT_BLOCK_PLANAR };
+  static PlannarizedDataInterface<D>* make(int n) { return new PlannarizedDataInterface<D>(n); }
+};
+
+/* FFT_CUDA<D> keeps FFT_FFTW3's interleaved host arrays;
+ * FFT_CUDA<D, PlannarizedDataInterface<D> > keeps FFT_OpenCL_Contiguous's
+ * block-planar ones, so it replaces that backend with the same dataInterface
+ * type. */
+template <class D, class DI = SplitInterleavedDataInterface<D> >
 class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
  public:
-  typedef SplitInterleavedDataInterface<D> DataInterfaceType;
+  typedef DI DataInterfaceType;
 
   static streng getName() { return "GB300 CUDA FFT"; }
 
@@ -110,7 +129,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
       : FFT<D>(n, iBatchCount), plan(NULL), registered(false) {
     typedef char only_float_is_supported[(sizeof(D) == sizeof(float)) ? 1 : -1];
     (void)sizeof(only_float_is_supported);
-    this->dataInterface = arrays = new DataInterfaceType(this->batchCount * this->size, false);
+    this->dataInterface = arrays = EstlLayoutOf<DI>::make(this->batchCount * this->size);
     ensureInit();
     estlCheck(estl_plan_create(n, iBatchCount, forward ? ESTL_FORWARD : ESTL_BACKWARD, ESTL_PREC_FP32, &plan),
               "estl_plan_create");
@@ -126,7 +145,8 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
     if (describe.find("\"stream\"") != std::string::npos) kinds.push_back(4);
     if (describe.find("\"column\"") != std::string::npos) kinds.push_back(5);
     kernelTimers.resize(kinds.size());
-    const size_t bytes = sizeof(D) * 2 * (size_t)this->size * this->batchCount;
+    const size_t bytes =
+        sizeof(D) * (size_t)estl_layout_floats(EstlLayoutOf<DI>::value, (int64_t)this->size * this->batchCount);
     registered = estl_host_register(arrays->in->getData(), bytes) == ESTL_OK &&
                  estl_host_register(arrays->out->getData(), bytes) == ESTL_OK;
     for (int k = 0; k < ESTL_KERNEL_KINDS; ++k) lastMs[k] = 0;
@@ -146,7 +166,8 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
 
   /* FFT<D>::execute: the result is in the data interface's output array. */
   virtual void execute() {
-    estlCheck(estl_execute_host(plan, arrays->in->getData(), arrays->out->getData()), "estl_execute_host");
+    estlCheck(estl_execute_host_layout(plan, EstlLayoutOf<DI>::value, arrays->in->getData(), arrays->out->getData()),
+              "estl_execute_host_layout");
     int64_t launches[ESTL_KERNEL_KINDS];
     double ms[ESTL_KERNEL_KINDS], bytes[ESTL_KERNEL_KINDS];
     estlCheck(estl_plan_kernel_stats(plan, launches, ms, bytes), "estl_plan_kernel_stats");

@@ -157,6 +157,26 @@ estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* st
  * full bandwidth; pageable memory works but is slower. */
 estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out);
 
+/* Other host layouts of the complex data (the reference's DataInterface
+ * classes, DataInterface.h:26-45):
+ *   ESTL_LAYOUT_INTERLEAVED   re, im pairs (SplitInterleavedDataInterface(n, false));
+ *   ESTL_LAYOUT_BLOCK_PLANAR  blocks of 32 real parts then 32 imaginary parts
+ *                             (PlannarizedDataInterface, the layout of
+ *                             FFT_OpenCL_Contiguous, FFT_OpenCL_Contiguous.h:28);
+ *   ESTL_LAYOUT_SPLIT         all real parts, then all imaginary parts
+ *                             (SplitInterleavedDataInterface(n, true)).
+ * The whole batch (n * batch elements) is one array in the layout; arrays
+ * hold estl_layout_floats(layout, n * batch) floats.  The data is converted
+ * on the device around the plan's kernels.  estl_execute_layout allocates two
+ * interleaved staging buffers of n * batch complex on its first call;
+ * estl_execute_host_layout converts per chunk of its host pipeline. */
+#define ESTL_LAYOUT_INTERLEAVED 0
+#define ESTL_LAYOUT_BLOCK_PLANAR 1
+#define ESTL_LAYOUT_SPLIT 2
+int64_t estl_layout_floats(int layout, int64_t total);
+estl_status estl_execute_layout(estl_plan plan, int layout, const float* d_in, float* d_out, void* stream);
+estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_in, float* h_out);
+
 /* Per-launch device timing, the counterpart of OpenCLAlgorithm's
  * kernelTimers / timerComputation (uOpenCL.h:281-282) that
  * FFT_OpenCL_Contiguous::execute fills from event profiling

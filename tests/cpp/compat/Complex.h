@@ -53,6 +53,28 @@ class Complex {
   R r, i;
 };
 
+/* Block-planar complex array: element i's real part at float
+ * ((i >> 5) << 6) | (i & 31), its imaginary part 32 floats later
+ * (interface of PlannarizedComplexArray<5, D>). */
+template <int LEVEL, class D>
+class PlannarizedComplexArray {
+ public:
+  explicit PlannarizedComplexArray(int n) : size(n), data(new AlignedArray<D>(2 * (((n + (1 << LEVEL) - 1) >> LEVEL) << LEVEL))) {}
+  ~PlannarizedComplexArray() { delete data; }
+  D* getData() { return &(*data)[0]; }
+  int getSize() const { return size; }
+  void setElement(int k, Complex<D> v) {
+    (*data)[pos(k, 0)] = v.getReal();
+    (*data)[pos(k, 1)] = v.getImaginary();
+  }
+  Complex<D> getElement(int k) { return Complex<D>((*data)[pos(k, 0)], (*data)[pos(k, 1)]); }
+
+ private:
+  static int pos(int k, int e) { return ((k >> LEVEL) << (LEVEL + 1)) | (e << LEVEL) | (k & ((1 << LEVEL) - 1)); }
+  int size;
+  AlignedArray<D>* data;
+};
+
 /* Interleaved (planar = false) or fully planar complex array. */
 template <class D>
 class ComplexArray {

@@ -40,4 +40,13 @@ class SplitInterleavedDataInterface : public ArrayDataInterface<D, ComplexArray<
   }
 };
 
+template <class D>
+class PlannarizedDataInterface : public ArrayDataInterface<D, PlannarizedComplexArray<5, D> > {
+ public:
+  explicit PlannarizedDataInterface(int n) : ArrayDataInterface<D, PlannarizedComplexArray<5, D> >(n) {
+    this->in = new PlannarizedComplexArray<5, D>(n);
+    this->out = new PlannarizedComplexArray<5, D>(n);
+  }
+};
+
 #endif

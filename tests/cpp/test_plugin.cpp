@@ -140,6 +140,8 @@ int main(int argc, char** argv) {
   int max_m = argc > 2 ? atoi(argv[2]) : 16;
   std::vector<FFTFactory<D>*> factories;
   factories.push_back(new FFTFactorySpecific<FFT_CUDA<D> >());
+  // the FFT_OpenCL_Contiguous host layout (PlannarizedDataInterface, block-planar)
+  factories.push_back(new FFTFactorySpecific<FFT_CUDA<D, PlannarizedDataInterface<D> > >());
   try {
     for (size_t i = 0; i < factories.size(); ++i) {
       known_answer_sweep(factories[i], max_b, max_m);
