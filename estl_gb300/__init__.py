@@ -129,6 +129,8 @@ class Plan:
         LAYOUT_SPLIT / LAYOUT_INTERLEAVED), layout_floats(layout, n * batch) floats."""
         import torch
         floats = int(lib().estl_layout_floats(int(layout), self.n * self.batch))
+        if floats < 0:
+            raise EstlError(1, f"unknown layout {layout}")
         if x.dtype != torch.float32 or not x.is_cuda or not x.is_contiguous() or x.numel() < floats:
             raise EstlError(1, f"input must be a contiguous float32 CUDA tensor of >= {floats} floats")
         if out is None:

@@ -9,6 +9,7 @@
 #include <unordered_set>
 #include <vector>
 
+#include "bluestein_core.cuh"
 #include "engine.h"
 #include "kernels.cuh"
 #include "tuner.h"
@@ -249,6 +250,12 @@ struct estl_plan_s {
   float* hlay_in[2] = {nullptr, nullptr};
   float* hlay_out[2] = {nullptr, nullptr};
   size_t hlay_bytes = 0;
+  // Bluestein plans: chirp (N), scaled kernel spectrum (M), two work buffers
+  cf32* blue_chirp = nullptr;
+  cf32* blue_spec = nullptr;
+  cf32* blue_a = nullptr;
+  cf32* blue_c = nullptr;
+  size_t blue_chirp_bytes = 0, blue_spec_bytes = 0, blue_work_bytes = 0;
   // per-launch profiling (estl_plan_set_profiling)
   bool profiling = false;
   struct Rec {
@@ -270,6 +277,10 @@ static void plan_release(estl_plan p) {
   dev_free(p->scratch, p->scratch_bytes);
   dev_free(p->aux, p->aux_bytes);
   for (int s = 0; s < 2; ++s) dev_free(p->host_aux[s], p->host_aux_bytes[s]);
+  dev_free(p->blue_chirp, p->blue_chirp_bytes);
+  dev_free(p->blue_spec, p->blue_spec_bytes);
+  dev_free(p->blue_a, p->blue_work_bytes);
+  dev_free(p->blue_c, p->blue_work_bytes);
   dev_free(p->lay_in, p->lay_bytes);
   dev_free(p->lay_out, p->lay_bytes);
   for (int s = 0; s < 2; ++s) {
@@ -400,6 +411,103 @@ estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int pre
 
 static estl_status plan_finish(std::unique_ptr<estl_plan_s> p, int direction, estl_plan* plan);
 
+// ---- Bluestein plans (bluestein_core.cuh) ---------------------------------
+static int flat_grid(long long total) {
+  const long long blocks = (total + 255) / 256;
+  return (int)std::max(1LL, std::min<long long>(blocks, 152LL * 16));
+}
+
+__global__ void blue_chirp_kernel(cf32* chirp, long long N) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+    chirp[i] = bluestein_chirp(i, N);
+}
+
+__global__ void blue_kernel_kernel(const cf32* chirp, cf32* b, long long N, long long M) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+    b[i] = bluestein_kernel_elem(chirp, i, N, M);
+}
+
+__global__ void blue_scale_kernel(cf32* v, long long M, float s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+    v[i] = cf32{v[i].x * s, v[i].y * s};
+}
+
+// a[b][m] for `count` transforms of length N into rows of length M
+__global__ void blue_pre_kernel(const cf32* __restrict__ x, cf32* __restrict__ a, const cf32* __restrict__ chirp,
+                                long long N, int logm, long long count, float sgn) {
+  const long long total = count << logm, mask = (1LL << logm) - 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x)
+    a[i] = bluestein_pre(x + (i >> logm) * N, chirp, i & mask, N, sgn);
+}
+
+__global__ void blue_mul_kernel(cf32* c, const cf32* __restrict__ spec, int logm, long long count) {
+  const long long total = count << logm, mask = (1LL << logm) - 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x)
+    c[i] = cmul(c[i], spec[i & mask]);
+}
+
+__global__ void blue_post_kernel(const cf32* __restrict__ c, cf32* __restrict__ y, const cf32* __restrict__ chirp,
+                                 long long N, int logm, long long count, float sgn) {
+  const long long total = count * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i / N, k = i - b * N;
+    y[i] = bluestein_post(c + (b << logm), chirp, k, sgn);
+  }
+}
+
+// Chirp, the kernel spectrum FFT_M(b) / M and the work buffers of a plan.
+static estl_status bluestein_setup(estl_plan_s* p) {
+  const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
+  p->blue_chirp_bytes = (size_t)N * sizeof(cf32);
+  p->blue_spec_bytes = (size_t)M * sizeof(cf32);
+  p->blue_work_bytes = (size_t)(cmax * M) * sizeof(cf32);
+  estl_status s = dev_alloc((void**)&p->blue_chirp, p->blue_chirp_bytes, "Bluestein chirp");
+  if (s == ESTL_OK) s = dev_alloc((void**)&p->blue_spec, p->blue_spec_bytes, "Bluestein spectrum");
+  if (s == ESTL_OK) s = dev_alloc((void**)&p->blue_a, p->blue_work_bytes, "Bluestein work");
+  if (s == ESTL_OK) s = dev_alloc((void**)&p->blue_c, p->blue_work_bytes, "Bluestein work");
+  if (s != ESTL_OK) return s;
+  Plan1D one;
+  std::string err;
+  if (!make_plan(M, 1, PlanChoice{}, &one, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+  if ((size_t)one.scratch_elems * sizeof(cf32) > p->scratch_bytes)
+    return fail(ESTL_DEVICE_ERROR, "Bluestein set-up needs more scratch than the plan holds");
+  cudaStream_t st = 0;  // legacy default stream: ordered with every blocking stream
+  blue_chirp_kernel<<<flat_grid(N), 256, 0, st>>>(p->blue_chirp, N);
+  blue_kernel_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_chirp, p->blue_a, N, M);
+  s = check_cuda(cudaGetLastError(), "Bluestein set-up");
+  if (s == ESTL_OK) s = launch_steps(one, p->blue_a, p->blue_spec, p->scratch, 1.f, st, nullptr);
+  if (s != ESTL_OK) return s;
+  blue_scale_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_spec, M, 1.f / (float)M);
+  s = check_cuda(cudaGetLastError(), "Bluestein set-up");
+  if (s == ESTL_OK) s = check_cuda(cudaStreamSynchronize(st), "Bluestein set-up");
+  return s;
+}
+
+// `count` transforms of a Bluestein plan: pre-multiply, M-point FFT, spectrum
+// multiply, M-point inverse FFT, post-multiply, in chunks of blue_chunk.
+static estl_status run_bluestein(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
+  const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
+  const int logm = ilog2_exact(M);
+  for (long long b0 = 0; b0 < count; b0 += cmax) {
+    const long long c = std::min(cmax, count - b0);
+    Plan1D inner;
+    std::string err;
+    if (!make_plan(M, c, PlanChoice{}, &inner, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+    blue_pre_kernel<<<flat_grid(c * M), 256, 0, st>>>(in + b0 * N, p->blue_a, p->blue_chirp, N, logm, c, p->sgn);
+    estl_status s = check_cuda(cudaGetLastError(), "Bluestein pre-multiply");
+    if (s == ESTL_OK) s = launch_steps(inner, p->blue_a, p->blue_c, p->scratch, 1.f, st, nullptr);
+    if (s != ESTL_OK) return s;
+    blue_mul_kernel<<<flat_grid(c * M), 256, 0, st>>>(p->blue_c, p->blue_spec, logm, c);
+    s = check_cuda(cudaGetLastError(), "Bluestein spectrum multiply");
+    if (s == ESTL_OK) s = launch_steps(inner, p->blue_c, p->blue_a, p->scratch, -1.f, st, nullptr);
+    if (s != ESTL_OK) return s;
+    blue_post_kernel<<<flat_grid(c * N), 256, 0, st>>>(p->blue_a, out + b0 * N, p->blue_chirp, N, logm, c, p->sgn);
+    s = check_cuda(cudaGetLastError(), "Bluestein post-multiply");
+    if (s != ESTL_OK) return s;
+  }
+  return ESTL_OK;
+}
+
 static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int precision,
                                     const estl_plan_options* opt, estl_plan* plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "plan output pointer is NULL");
@@ -412,8 +520,18 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
     return fail(ESTL_INVALID_ARG, "unknown precision %d", precision);
   if (batch < 1) return fail(ESTL_INVALID_ARG, "batch must be >= 1 (got %lld)", (long long)batch);
   int logn = ilog2_exact(n);
+  if (logn < 0 && n > 2) {
+    // any other length: Bluestein over power-of-two FFTs (FP32, planner defaults)
+    if (precision != ESTL_PREC_FP32)
+      return fail(ESTL_INVALID_ARG, "lengths that are not powers of two run in FP32 (precision %d)", precision);
+    if (opt && opt->mode != 0) return fail(ESTL_INVALID_ARG, "plan options apply to power-of-two lengths");
+    std::unique_ptr<estl_plan_s> p(new estl_plan_s);
+    std::string err;
+    if (!make_plan_bluestein(n, batch, &p->layout, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+    return plan_finish(std::move(p), direction, plan);
+  }
   if (logn < 0 || logn > kMaxLogN)
-    return fail(ESTL_UNSUPPORTED_SIZE, "transform length %lld is not a power of two in [1, 2^%d]", (long long)n,
+    return fail(ESTL_UNSUPPORTED_SIZE, "transform length %lld must be at least 1 and at most 2^%d", (long long)n,
                 kMaxLogN);
   PlanChoice choice;
   if (opt && opt->mode != 0) {
@@ -455,6 +573,13 @@ static estl_status plan_finish(std::unique_ptr<estl_plan_s> p, int direction, es
   p->scratch_bytes = (size_t)p->layout.scratch_elems * sizeof(cf32);
   s = dev_alloc((void**)&p->scratch, p->scratch_bytes, "plan scratch");
   if (s != ESTL_OK) return s;
+  if (p->layout.blue_m > 0) {
+    s = bluestein_setup(p.get());
+    if (s != ESTL_OK) {
+      plan_release(p.release());
+      return s;
+    }
+  }
   p->aux_bytes = stream_aux_bytes(p->layout);
   if (p->aux_bytes) {
     s = dev_alloc(&p->aux, p->aux_bytes, "stream work list");
@@ -670,7 +795,9 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const Strea
     s = launch_layout_in(io->layout, io->src, const_cast<cf32*>(in), io->total, stream);
     if (s != ESTL_OK) return s;
   }
-  if (plan->profiling)
+  if (layout.blue_m > 0)
+    s = run_bluestein(plan, layout.batch, in, out, stream);
+  else if (plan->profiling)
     s = launch_profiled(plan, layout, aux, in, out, stream);
   else
     s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream, aux);

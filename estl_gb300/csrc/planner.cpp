@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdio>
 
+#include "bluestein_core.cuh"
 #include "fft_core.cuh"
 #include "pipe_core.cuh"
 
@@ -326,7 +327,34 @@ bool make_plan2d(long long xdim, long long ydim, long long batch, const PlanChoi
   return true;
 }
 
+bool make_plan_bluestein(long long n, long long batch, Plan1D* out, std::string* err) {
+  if (n < 3 || ilog2_exact(n) >= 0 || n > (1LL << (kBluesteinMaxLogM - 1))) {
+    set_err(err, "Bluestein plans take lengths that are not powers of two, 2 < n <= 2^%lld (got %lld)",
+            (long long)(kBluesteinMaxLogM - 1), n);
+    return false;
+  }
+  if (batch < 1) {
+    set_err(err, "batch must be >= 1 (got %lld)", batch);
+    return false;
+  }
+  const long long m = bluestein_m(n);
+  Plan1D inner;
+  const long long chunk = std::min(batch, std::max(1LL, (1LL << 26) / m));
+  if (!make_plan(m, chunk, PlanChoice{}, &inner, err)) return false;
+  Plan1D p;
+  p.n = n;
+  p.batch = batch;
+  p.logn = 0;
+  p.blue_m = m;
+  p.blue_chunk = chunk;
+  p.scratch_elems = inner.scratch_elems;
+  p.hbm_passes = 2 * inner.hbm_passes + 3;  // pre-multiply, two M-point FFTs, spectrum multiply, post-multiply
+  *out = p;
+  return true;
+}
+
 bool make_plan_like(const Plan1D& base, long long batch, Plan1D* out, std::string* err) {
+  if (base.blue_m > 0) return make_plan_bluestein(base.n, batch, out, err);
   if (base.xdim > 0) return make_plan2d(base.xdim, base.ydim, batch, base.choice, out, err);
   return make_plan(base.n, batch, base.choice, out, err);
 }
@@ -391,9 +419,9 @@ std::string Plan1D::describe() const {
   char buf[512];
   static const char* splits[] = {"fp32", "fp16x2", "bf16x2", "bf16x3"};
   std::snprintf(buf, sizeof buf,
-                "{\"n\": %lld, \"batch\": %lld, \"xdim\": %lld, \"ydim\": %lld, \"precision\": \"%s\", "
+                "{\"n\": %lld, \"batch\": %lld, \"bluestein_m\": %lld, \"xdim\": %lld, \"ydim\": %lld, \"precision\": \"%s\", "
                 "\"hbm_passes\": %d, \"launches\": %zu, \"scratch_bytes\": %lld, \"kernels\": [",
-                n, batch, xdim, ydim, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes,
+                n, batch, blue_m, xdim, ydim, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes,
                 steps.size(), scratch_elems * 8);
   s += buf;
   const char* names[] = {"single", "col", "row", "copy", "stream", "column"};

@@ -78,6 +78,8 @@ struct Plan1D {
   long long n = 0, batch = 0;
   int logn = 0;
   long long xdim = 0, ydim = 0;  // 2D plans (make_plan2d): n = xdim * ydim; 0 for 1D
+  long long blue_m = 0;          // Bluestein plans (make_plan_bluestein): the FFT length M; 0 otherwise
+  long long blue_chunk = 0;      // Bluestein: transforms per pass through the M-point FFTs
   PlanChoice choice;
   std::vector<Step> steps;
   long long scratch_elems = 0;
@@ -103,7 +105,13 @@ constexpr int kPlan2dMaxLog = 26;
 bool make_plan2d(long long xdim, long long ydim, long long batch, const PlanChoice& choice, Plan1D* out,
                  std::string* err);
 
-// The plan of the same transform (1D or 2D) for another batch count.
+// Transforms of a length N that is not a power of two (2 < N <= 2^23):
+// Bluestein's algorithm over M = 2^ceil(log2(2N - 1)) point FFT plans
+// (bluestein_core.cuh).  The plan holds no steps; scratch_elems is the
+// scratch of its M-point plan for blue_chunk transforms.
+bool make_plan_bluestein(long long n, long long batch, Plan1D* out, std::string* err);
+
+// The plan of the same transform (1D, 2D or Bluestein) for another batch count.
 bool make_plan_like(const Plan1D& base, long long batch, Plan1D* out, std::string* err);
 
 // Candidate choices for (n, batch), default first (autotuner search space).

@@ -43,6 +43,9 @@ def emu():
     lib.emu_plan2d_run.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, P, P,
                                    ctypes.c_char_p, ctypes.c_int]
     lib.emu_plan2d_run.restype = ctypes.c_int
+    lib.emu_bluestein_run.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, P, P, ctypes.c_char_p,
+                                      ctypes.c_int]
+    lib.emu_bluestein_run.restype = ctypes.c_int
     lib.emu_plan_describe.argtypes = [ctypes.c_longlong, ctypes.c_longlong, P, ctypes.c_char_p, ctypes.c_int]
     lib.emu_plan_candidates.argtypes = [ctypes.c_longlong, ctypes.c_longlong, P, ctypes.c_int]
     lib.emu_conv_run.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, ctypes.c_char_p, ctypes.c_int]

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "bluestein_core.cuh"
 #include "conv_plan.h"
 #include "fft_core.cuh"
 #include "packed_core.cuh"
@@ -342,6 +343,52 @@ int emu_plan2d_run(long long xdim, long long ydim, long long batch, int sign, co
     return 2;
   }
   return run_plan(p, sign, in, out, err, errlen);
+}
+
+// Bluestein plan (make_plan_bluestein) of a length that is not a power of
+// two: the same element functions as the GPU kernels (bluestein_core.cuh)
+// around emulated power-of-two FFT plans.
+int emu_bluestein_run(long long n, long long batch, int sign, const float* in, float* out, char* err, int errlen) {
+  Plan1D p;
+  std::string e;
+  if (!make_plan_bluestein(n, batch, &p, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  const long long M = p.blue_m;
+  const float sgn = sign < 0 ? 1.f : -1.f;
+  std::vector<cf32> chirp(n), b(M), spec(M);
+  for (long long i = 0; i < n; ++i) chirp[i] = bluestein_chirp(i, n);
+  for (long long m = 0; m < M; ++m) b[m] = bluestein_kernel_elem(chirp.data(), m, n, M);
+  Plan1D one;
+  if (!make_plan(M, 1, PlanChoice{}, &one, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  int rc = run_plan(one, -1, reinterpret_cast<const float*>(b.data()), reinterpret_cast<float*>(spec.data()), err, errlen);
+  if (rc) return rc;
+  for (cf32& v : spec) v = cf32{v.x / (float)M, v.y / (float)M};
+  const cf32* x = reinterpret_cast<const cf32*>(in);
+  cf32* y = reinterpret_cast<cf32*>(out);
+  for (long long b0 = 0; b0 < batch; b0 += p.blue_chunk) {
+    const long long c = std::min(p.blue_chunk, batch - b0);
+    Plan1D inner;
+    if (!make_plan(M, c, PlanChoice{}, &inner, &e)) {
+      set_err(err, errlen, e);
+      return 2;
+    }
+    std::vector<cf32> a(c * M), cc(c * M);
+    for (long long t = 0; t < c; ++t)
+      for (long long m = 0; m < M; ++m) a[t * M + m] = bluestein_pre(x + (b0 + t) * n, chirp.data(), m, n, sgn);
+    rc = run_plan(inner, -1, reinterpret_cast<const float*>(a.data()), reinterpret_cast<float*>(cc.data()), err, errlen);
+    if (rc) return rc;
+    for (long long i = 0; i < c * M; ++i) cc[i] = cmul(cc[i], spec[i % M]);
+    rc = run_plan(inner, +1, reinterpret_cast<const float*>(cc.data()), reinterpret_cast<float*>(a.data()), err, errlen);
+    if (rc) return rc;
+    for (long long t = 0; t < c; ++t)
+      for (long long k = 0; k < n; ++k) y[(b0 + t) * n + k] = bluestein_post(a.data() + t * M, chirp.data(), k, sgn);
+  }
+  return 0;
 }
 
 static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen) {

@@ -150,7 +150,7 @@ def test_errors(engine):
     import torch
     from estl_gb300 import EstlError
     with pytest.raises(EstlError) as e:
-        engine.Plan(12, 1)
+        engine.Plan((1 << 23) + 3, 1)  # beyond the Bluestein limit for other lengths
     assert e.value.name == "ESTL_UNSUPPORTED_SIZE"
     with pytest.raises(EstlError) as e:
         engine.Plan(1 << 25, 1)
