@@ -456,6 +456,39 @@ def bench_fft2d(estl, torch):
     return out
 
 
+def bench_bluestein(estl, torch):
+    """Lengths that are not powers of two (Bluestein over power-of-two plans):
+    C2C FP32 forward, about 2^26 elements per size, uniform[-1,1) seed 7;
+    rel-L2 of the first transforms against numpy's FP64 FFT."""
+    import numpy as np
+    out = {"workload": "C2C FP32 forward, N in {1000, 12288, 1000000}, batch = 2^26 // N, uniform[-1,1) seed 7",
+           "bytes_counted": "16 B per element (compulsory read + write)"}
+    st = torch.cuda.Stream()
+    for n in (1000, 12288, 1000000):
+        batch = (1 << 26) // n
+        g = torch.Generator(device="cuda").manual_seed(7)
+        x = torch.view_as_complex((torch.rand((n * batch, 2), device="cuda", generator=g) * 2 - 1).contiguous())
+        y = torch.empty_like(x)
+        p = estl.Plan(n, batch, estl.FORWARD)
+        for _ in range(2):
+            p.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+        st.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(5):
+            p.execute_ptr(x.data_ptr(), y.data_ptr(), st.cuda_stream)
+        e1.record(st)
+        st.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        rows = max(1, min(batch, (1 << 21) // n))
+        x0 = x[: rows * n].view(rows, n).cpu().numpy().astype(np.complex128)
+        err = float(rel_l2_rows(y[: rows * n].view(rows, n).cpu().numpy(), np.fft.fft(x0, axis=-1)).max())
+        out[str(n)] = {"batch": batch, "bluestein_m": p.describe()["bluestein_m"], "ms": round(ms, 3),
+                       "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": float(f"{err:.3e}")}
+        p.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -659,7 +692,7 @@ def main():
     configs = {}
     if rank == 0 and not args.no_configs:
         for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
-                        ("split_precision", bench_split_precision), ("fft2d", bench_fft2d),
+                        ("split_precision", bench_split_precision), ("fft2d", bench_fft2d), ("bluestein", bench_bluestein),
                         ("served_conv", bench_served_conv)):
             try:
                 configs[key] = fn(estl, torch)
