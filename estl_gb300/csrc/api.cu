@@ -186,7 +186,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     }
     // pipelined kernels move 16-byte chunks: they need 16-byte aligned data
     const bool aligned = !(((uintptr_t)(src + st.src_off) | (uintptr_t)(dst + st.dst_off)) & 15);
-    const int pipe = (st.pipe && aligned) ? 1 : 0;
+    const int pipe = aligned ? st.pipe : 0;
     const KernelDesc* d = nullptr;
     int resident = 0;
     estl_status s = lookup_kernel(st, pipe, &d, &resident);
@@ -203,6 +203,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.sgn = sgn;
     a.grid = grid;
     a.split = st.tc ? plan.choice.split : SPLIT_NONE;
+    a.err = E.dev_err;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel");
@@ -340,6 +341,14 @@ estl_status estl_init(int device, size_t hbm_budget_bytes) {
     return s;
   }
   E.bank = (cf32*)b;
+  {
+    void* w = nullptr;
+    s = dev_alloc(&w, 256, "error word");
+    if (s != ESTL_OK) return s;
+    E.dev_err = (long long*)w;
+    s = check_cuda(cudaMemset(E.dev_err, 0, sizeof(long long)), "cudaMemset(error word)");
+    if (s != ESTL_OK) return s;
+  }
   bank_init_kernel<<<(unsigned)((kBankSize + 255) / 256), 256>>>(E.bank);
   s = check_cuda(cudaGetLastError(), "bank_init_kernel launch");
   if (s == ESTL_OK) s = check_cuda(cudaDeviceSynchronize(), "bank_init_kernel");
@@ -365,6 +374,8 @@ estl_status estl_shutdown(void) {
   cudaDeviceSynchronize();
   dev_free(E.bank, kBankSize * sizeof(cf32));
   E.bank = nullptr;
+  dev_free(E.dev_err, 256);
+  E.dev_err = nullptr;
   E.inited = false;
   return ESTL_OK;
 }
@@ -657,6 +668,13 @@ estl_status estl_plan_check(estl_plan plan) {
       cudaMemset(a->error, 0, sizeof(int));
       return fail(ESTL_TIMEOUT, "a dependency wait of the streamed kernel gave up");
     }
+  }
+  long long e = 0;
+  s = check_cuda(cudaMemcpy(&e, engine().dev_err, sizeof(e), cudaMemcpyDeviceToHost), "cudaMemcpy(error word)");
+  if (s != ESTL_OK) return s;
+  if (e) {
+    cudaMemset(engine().dev_err, 0, sizeof(long long));
+    return fail(ESTL_TIMEOUT, "a bulk-load wait gave up (tile %lld)", e - 1);
   }
   return ESTL_OK;
 }

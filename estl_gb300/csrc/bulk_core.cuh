@@ -1,0 +1,192 @@
+// bulk_core.cuh — four-step row pass with bulk asynchronous tile loads.
+//
+// The plain tile kernels load their tile with per-thread global loads, then
+// compute, then store; with 1-2 CTAs per SM the SM is idle on memory during
+// compute.  BulkRowKernel is persistent: each CTA owns two shared-memory
+// stages, and one thread issues the next tiles' rows as bulk asynchronous
+// copies (cp.async.bulk, global -> shared, completion counted in bytes on an
+// mbarrier) while the CTA computes the current tile.  A stage is first the
+// landing zone of its tile's rows (row c at c * RS, RS = M + 16/C so that the
+// column-fastest reads are conflict-free), then, once every thread holds its
+// elements in registers, the Stockham exchange buffer of that tile.  The
+// next load into the stage is issued after the tile's last exchange.
+//
+//   tile k:  wait(stage k%2) -> registers -> passes (exchange in the stage)
+//            -> issue tile k+2 into stage k%2 -> stores (C-wide runs)
+//
+// Waits are bounded: after kBulkSpinLimit polls the kernel records the tile in
+// an error word and returns.  The emulator runs the same code with the copies
+// as bounds-checked memcpys at issue time.
+#pragma once
+#include <stdint.h>
+
+#include <cstring>
+
+#include "fft_core.cuh"
+
+namespace estl {
+
+constexpr long long kBulkSpinLimit = 1LL << 22;
+
+#if defined(__CUDA_ARCH__)
+ESTL_HD uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+#endif
+
+ESTL_HD void mbar_init(uint64_t* bar, int count) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+#else
+  *bar = 0;
+  (void)count;
+#endif
+}
+
+ESTL_HD void bulk_fence_init() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+#endif
+}
+
+// Orders this thread's (and, after a barrier, the CTA's) generic-proxy accesses
+// of shared memory before later async-proxy (bulk copy) writes.
+ESTL_HD void bulk_fence_proxy() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+#endif
+}
+
+ESTL_HD void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+#else
+  (void)bar;
+  (void)bytes;
+#endif
+}
+
+// Bulk copy of `n` complex elements from global `src` to shared `dst` (both
+// 16-byte aligned, n even), counted on `bar`.
+ESTL_HD void bulk_load(const Ptr<cf32>& dst, long long didx, const Ptr<const cf32>& src, long long sidx, int n,
+                       uint64_t* bar) {
+  ESTL_CHECK(didx + n - 1, dst.n, "bulk copy shared destination");
+  ESTL_CHECK(sidx + n - 1, src.n, "bulk copy global source");
+  ESTL_CHECK((long long)(((uintptr_t)(dst.p + didx)) & 15), 1, "bulk copy shared alignment (16 B)");
+  ESTL_CHECK((long long)(((uintptr_t)(src.p + sidx)) & 15), 1, "bulk copy global alignment (16 B)");
+#if defined(__CUDA_ARCH__)
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(dst.p + didx)),
+      "l"(src.p + sidx), "r"((uint32_t)(n * sizeof(cf32))), "r"(smem_u32(bar))
+      : "memory");
+#else
+  std::memcpy(dst.p + didx, src.p + sidx, (size_t)n * sizeof(cf32));
+  (void)bar;
+#endif
+}
+
+// Bounded wait for phase `parity` of `bar`; false if the limit ran out.
+ESTL_HD bool mbar_wait(uint64_t* bar, uint32_t parity) {
+#if defined(__CUDA_ARCH__)
+  for (long long it = 0; it < kBulkSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+#else
+  (void)bar;
+  (void)parity;
+  return true;  // the emulator's copies complete at issue
+#endif
+}
+
+// CTA-wide OR (a barrier): every thread leaves a failed wait together.
+ESTL_HD bool cta_any(bool x) {
+#if defined(__CUDA_ARCH__)
+  return __syncthreads_or(x ? 1 : 0) != 0;
+#else
+  ESTL_SYNC();
+  return x;  // the emulator's waits never fail
+#endif
+}
+
+// Row pass of the four-step (as RowKernel: C rows k2_0.. of one transform's
+// scratch -> X[k2 + N2 k1], column-fastest threads), persistent over tiles.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct BulkRowKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  using Base = RowKernel<LOGM, LOGE, LOGR, LOGC>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static_assert(C >= 2 && C <= 8, "landing rows 16-byte aligned and conflict-free for 2 <= C <= 8");
+  static constexpr int RS = TL::M + 16 / C;  // landing row stride (elements, even)
+  static constexpr int EXCH = TL::MP * C;    // exchange layout of RowKernel (pad(m) * C + c)
+  static constexpr int STAGE = ((EXCH > C * RS ? EXCH : C * RS) + 1) & ~1;
+  static constexpr int SMEM_ELEMS = 2 * STAGE + 2;  // two stages, then two 8-byte mbarriers
+  // CTAs per SM that shared memory allows: the registers are sized for those
+  static constexpr int SMEM_BLOCKS = (227 * 1024) / (SMEM_ELEMS * 8 + 1024);
+  static constexpr int MIN_BLOCKS =
+      SMEM_BLOCKS < 1 ? 1 : (SMEM_BLOCKS < min_blocks(NT, TL::E) ? SMEM_BLOCKS : min_blocks(NT, TL::E));
+  static_assert(TL::M % 2 == 0, "rows of an even number of elements (16-byte copies)");
+
+  ESTL_HD static long long ntiles(const TileArgs& a) { return a.rows << (a.logn - LOGM - LOGC); }
+
+  // thread 0: the C rows of `tile` into stage `s`
+  ESTL_HD static void issue(const TileArgs& a, long long tile, const Ptr<cf32>& stage, uint64_t* bar) {
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = tile / nblk;
+    const int k2_0 = (int)(tile - f * nblk) * C;
+    const long long N = 1LL << a.logn;
+    bulk_fence_proxy();
+    mbar_expect_tx(bar, (uint32_t)(C * TL::M * sizeof(cf32)));
+    for (int c = 0; c < C; ++c) bulk_load(stage, (long long)c * RS, a.in, f * N + (long long)(k2_0 + c) * TL::M, TL::M, bar);
+  }
+
+  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
+    const long long nt = ntiles(a), grid = a.grid;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + 2 * STAGE);
+    const int c = tid & (C - 1);
+    const int t = tid >> LOGC;
+    const int logn2 = a.logn - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long N = 1LL << a.logn;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    if (tid == 0) {
+      mbar_init(&bar[0], 1);
+      mbar_init(&bar[1], 1);
+      bulk_fence_init();
+      if (cta < nt) issue(a, cta, Ptr<cf32>{smraw, STAGE}, &bar[0]);
+      if (cta + grid < nt) issue(a, cta + grid, Ptr<cf32>{smraw + STAGE, STAGE}, &bar[1]);
+    }
+    ESTL_SYNC();
+    long long k = 0;
+    for (long long tile = cta; tile < nt; tile += grid, ++k) {
+      const int s = (int)(k & 1);
+      const Ptr<cf32> stage{smraw + s * STAGE, STAGE};
+      if (cta_any(!mbar_wait(&bar[s], (uint32_t)((k >> 1) & 1)))) {
+        if (tid == 0 && a.err) atomic_max_ll(a.err, tile + 1);
+        return;
+      }
+      cf32 v[TL::E];
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = stage[c * RS + t + TL::T * j];
+      ESTL_SYNC();  // the stage becomes the exchange buffer
+      run_passes<TL, 0>(v, t, c, stage, tw, typename Base::Sidx{});
+      ESTL_SYNC();  // every exchange read of this stage is done
+      if (tid == 0 && tile + 2 * grid < nt) issue(a, tile + 2 * grid, stage, &bar[s]);
+      const long long f = tile / nblk;
+      const int k2_0 = (int)(tile - f * nblk) * C;
+      const Ptr<cf32> out = a.out.sub(f * N, N);
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) stcs(out, k2_0 + c + ((t + TL::T * j) << logn2), conj_if(v[j], a.sgn));
+    }
+  }
+};
+
+}  // namespace estl

@@ -28,6 +28,7 @@ struct Engine {
   size_t budget = 0;
   std::atomic<size_t> used{0};
   cf32* bank = nullptr;  // twiddle bank, kBankSize entries
+  long long* dev_err = nullptr;  // bulk-load kernels' wait-timeout word (TileArgs::err)
   int num_sms = 0;
 };
 

@@ -419,7 +419,16 @@ struct TileArgs {
   float sgn;       // +1 forward; -1 = backward via conj(FFT(conj(x)))
   long long grid;  // CTAs launched (grid-stride kernels of pipe_core.cuh)
   int split;       // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
+  long long* err;  // bulk-load kernels: 1 + the tile whose bounded wait gave up (0 = none)
 };
+
+ESTL_HD void atomic_max_ll(long long* p, long long v) {
+#if defined(__CUDA_ARCH__)
+  atomicMax(p, v);
+#else
+  if (*p < v) *p = v;
+#endif
+}
 
 ESTL_HD cf32 conj_if(cf32 v, float sgn) { return {v.x, v.y * sgn}; }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "fft_core.cuh"
+#include "bulk_core.cuh"
 #include "pipe_core.cuh"
 
 namespace estl {
@@ -17,7 +18,7 @@ struct KernelDesc {
   int nthreads;
   int smem_bytes;
   const void* fn;
-  int pipe;  // grid-stride, cp.async double-buffered variant (pipe_core.cuh)
+  int pipe;  // 1: grid-stride cp.async double-buffered variant (pipe_core.cuh); 2: bulk-load ring (bulk_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
 };
 
@@ -41,6 +42,7 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_PIPE_SINGLE(M, E, R, C) make_desc<PipeSingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C, 1)
 #define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
 #define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
+#define ESTL_BULK_ROW(M, E, R, C) make_desc<BulkRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 2)
 #define ESTL_COLUMN(M, E, C) make_desc<ColKernel<M, E, 4, C, false, false>>(KIND_COLUMN, M, E, 4, C)
 #define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
 #define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)

@@ -143,6 +143,7 @@ extern "C" estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direct
     a.sgn = direction == ESTL_FORWARD ? 1.f : -1.f;
     a.grid = step.grid;
     a.split = SPLIT_NONE;
+    a.err = nullptr;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)step.grid), dim3(d->nthreads), args, d->smem_bytes, st),
                    "cudaLaunchKernel");

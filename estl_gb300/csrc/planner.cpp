@@ -6,6 +6,7 @@
 
 #include "bluestein_core.cuh"
 #include "fft_core.cuh"
+#include "bulk_core.cuh"
 #include "pipe_core.cuh"
 
 namespace estl {
@@ -25,6 +26,7 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) v.push_back(cfg_of<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_BULK_ROW(M, E, R, C) v.push_back(cfg_of<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_COLUMN(M, E, C) v.push_back(cfg_of<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -110,7 +112,8 @@ static const TileCfg* find_tc(int kind, int logm, int logc) {
 // Whether a step of this configuration runs as its pipelined variant.
 static int use_pipe(const PlanChoice& ch, const TileCfg* c) {
   if (ch.pipe == 0) return 0;
-  return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, 1) ? 1 : 0;
+  const int want = ch.pipe == 2 ? 2 : 1;
+  return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, want) ? want : 0;
 }
 
 int ilog2_exact(long long n) {
@@ -393,7 +396,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
         for (const TileCfg& r : tile_configs()) {
           if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe || r.tc) continue;
           for (long long chunk : {0LL, 16LL << 20, 128LL << 20}) {
-           for (int pipe : {0, 1}) {
+           for (int pipe : {0, 1, 2}) {
             PlanChoice ch;
             ch.mode = 2;
             ch.logn2 = logn2;

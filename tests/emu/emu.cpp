@@ -24,6 +24,7 @@
 #include "conv_plan.h"
 #include "fft_core.cuh"
 #include "packed_core.cuh"
+#include "bulk_core.cuh"
 #include "pipe_core.cuh"
 #include "stream_core.cuh"
 #include "planner.h"
@@ -76,6 +77,7 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_PIPE_SINGLE(M, E, R, C) k.push_back(mk<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
 #define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
+#define ESTL_X_BULK_ROW(M, E, R, C) k.push_back(mk<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_COLUMN(M, E, C) k.push_back(mk<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -479,6 +481,7 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
     const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
     a.grid = grid;
     a.split = st.tc ? p.choice.split : SPLIT_NONE;
+    a.err = nullptr;
     if (!run_kernel(*k, a, grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
       set_err(err, errlen, g_msg);

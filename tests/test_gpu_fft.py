@@ -177,3 +177,25 @@ def test_autotune_keeps_results(engine, tmp_path, monkeypatch):
     x = uniform_c64((batch, n), 5)
     y = engine.Plan(n, batch, -1).execute(torch.from_numpy(x).cuda()).cpu().numpy()
     assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < 2e-6
+
+
+@pytest.mark.parametrize("logn,split,row_e,row_c", [(16, 8, 4, 3), (18, 9, 4, 2), (19, 9, 4, 2), (20, 10, 4, 2),
+                                                    (21, 10, 4, 1), (22, 11, 4, 2), (23, 11, 4, 1), (24, 12, 4, 1)])
+def test_bulk_load_row_tiles(engine, logn, split, row_e, row_c):
+    """The persistent row pass with bulk asynchronous tile loads (pipelined = 2,
+    bulk_core.cuh) against the oracle, both directions, and its wait-timeout
+    word clear afterwards."""
+    import torch
+    n = 1 << logn
+    batch = max(2, (1 << 23) // n)
+    x = uniform_c64((batch, n), 700 + logn)
+    xd = torch.from_numpy(x).cuda()
+    row_m = logn - split
+    for direction in (-1, +1):
+        p = engine.Plan(n, batch, direction, mode="four_step",
+                        tiles={"split_log2": split, "row_loge": row_e, "row_logc": row_c, "pipelined": 2})
+        d = p.describe()
+        assert d["kernels"][1]["kind"] == "row" and d["kernels"][1]["pipe"] == 2 and d["kernels"][1]["logm"] == row_m
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
