@@ -227,12 +227,12 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   }
 
   // four-step.  Defaults: the autotuner's winners on a GB300 for 1 GiB
-  // batches, log2 N -> (log2 N2, column log2 E / log2 C, row log2 E / log2 C);
-  // other lengths split N2 = 2^floor(log2 N / 2).
-  static const int tuned4[][6] = {{15, 7, 4, 5, 4, 3},  {16, 7, 4, 5, 4, 2},  {17, 8, 4, 4, 4, 2},
-                                  {18, 9, 4, 4, 4, 2},  {19, 10, 4, 3, 4, 2}, {20, 9, 4, 4, 4, 2},
-                                  {21, 10, 4, 3, 4, 2}, {22, 10, 4, 3, 4, 2}, {23, 11, 5, 3, 5, 2},
-                                  {24, 12, 5, 2, 5, 2}};
+  // batches, log2 N -> (log2 N2, column log2 E / log2 C, row log2 E / log2 C,
+  // row pass with bulk tile loads); other lengths split N2 = 2^floor(log2 N / 2).
+  static const int tuned4[][7] = {{15, 7, 4, 5, 4, 3, 0},  {16, 7, 4, 5, 4, 2, 2},  {17, 8, 4, 4, 4, 2, 2},
+                                  {18, 9, 4, 4, 4, 2, 2},  {19, 10, 4, 3, 4, 2, 2}, {20, 9, 4, 4, 4, 2, 2},
+                                  {21, 10, 4, 3, 4, 2, 2}, {22, 10, 4, 3, 4, 2, 0}, {23, 11, 5, 3, 5, 2, 0},
+                                  {24, 12, 5, 2, 5, 2, 0}};
   const int* td = nullptr;
   if (!tc && choice.logn2 < 0 && choice.col_loge < 0 && choice.row_loge < 0)
     for (const auto& t : tuned4)
@@ -276,6 +276,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
            0, cnt * n, b0 * n, cnt * n, cnt, logn};
     a.pipe = tc ? 0 : use_pipe(choice, col);
     b.pipe = tc ? 0 : use_pipe(choice, row);
+    if (td && choice.pipe == 0 && td[6] && find_tile(STEP_ROW, row->logm, row->loge, row->logr, row->logc, td[6]))
+      b.pipe = td[6];
     a.tc = b.tc = tc ? 1 : 0;
     p.steps.push_back(a);
     p.steps.push_back(b);
