@@ -165,6 +165,43 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
               st.logm, st.loge, st.logc);
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (no -lcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The column pass's view of its input: rows * 2^logm rows of N1 = 2^(logn -
+// logm) complex (as 2 N1 floats, pitch N1 * 8 bytes); boxes of C complex x
+// min(2^logm, 256) rows.
+static estl_status encode_column_map(CUtensorMap* map, const cf32* base, const Step& st) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return fail(ESTL_DEVICE_ERROR, "cuTensorMapEncodeTiled is not available from the driver");
+  const long long n1 = 1LL << (st.logn - st.logm);
+  const long long height = st.rows << st.logm;
+  if (height > (1LL << 31)) return fail(ESTL_UNSUPPORTED_SIZE, "tensor map of %lld rows", height);
+  const cuuint64_t dims[2] = {(cuuint64_t)(2 * n1), (cuuint64_t)height};
+  const cuuint64_t strides[1] = {(cuuint64_t)(n1 * sizeof(cf32))};
+  const cuuint32_t box[2] = {(cuuint32_t)(2 << st.logc), (cuuint32_t)std::min(1 << st.logm, 256)};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<cf32*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ESTL_DEVICE_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ESTL_OK;
+}
+
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
                          cudaStream_t stream, const StreamAux* aux) {
   Engine& E = engine();
@@ -204,7 +241,12 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.grid = grid;
     a.split = st.tc ? plan.choice.split : SPLIT_NONE;
     a.err = E.dev_err;
-    void* args[] = {&a};
+    alignas(64) CUtensorMap map;
+    if (d->tmap) {
+      s = encode_column_map(&map, src + st.src_off, st);
+      if (s != ESTL_OK) return s;
+    }
+    void* args[] = {&a, &map};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel");
     if (s != ESTL_OK) return s;

@@ -420,6 +420,7 @@ struct TileArgs {
   long long grid;  // CTAs launched (grid-stride kernels of pipe_core.cuh)
   int split;       // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
   long long* err;  // bulk-load kernels: 1 + the tile whose bounded wait gave up (0 = none)
+  const void* tmap = nullptr;  // tensor-map kernels: the CUtensorMap kernel parameter of the input
 };
 
 ESTL_HD void atomic_max_ll(long long* p, long long v) {

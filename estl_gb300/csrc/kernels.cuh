@@ -1,6 +1,7 @@
 // kernels.cuh — __global__ wrappers and the kernel registry entries for the
 // tile FFT kernels of fft_core.cuh.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fft_core.cuh"
@@ -20,6 +21,7 @@ struct KernelDesc {
   const void* fn;
   int pipe;  // 1: grid-stride cp.async double-buffered variant (pipe_core.cuh); 2: bulk-load ring (bulk_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
+  int tmap;  // launched with a 2D tensor map of its input as a second parameter (tma_tile_kernel)
 };
 
 template <class K>
@@ -28,10 +30,25 @@ __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tile_kernel(TileArgs a) 
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
 }
 
+// Kernels whose tile loads are tensor copies: the map lives in parameter space
+// for the whole launch, and the tile code finds it through TileArgs::tmap.
+template <class K>
+__global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tma_tile_kernel(TileArgs a, const __grid_constant__ CUtensorMap map) {
+  extern __shared__ float2 estl_smem[];
+  a.tmap = &map;
+  K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
+}
+
 template <class K>
 KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0) {
   return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
-                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe, tc};
+                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe, tc, 0};
+}
+
+template <class K>
+KernelDesc make_tma_desc(int kind, int logm, int loge, int logr, int logc) {
+  return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
+                    reinterpret_cast<const void*>(&tma_tile_kernel<K>), 2, 0, 1};
 }
 
 constexpr long long kMaxSmemBytes = 227 * 1024;
@@ -43,6 +60,7 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
 #define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
 #define ESTL_BULK_ROW(M, E, R, C) make_desc<BulkRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 2)
+#define ESTL_BULK_COL(M, E, R, C) make_tma_desc<BulkColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
 #define ESTL_COLUMN(M, E, C) make_desc<ColKernel<M, E, 4, C, false, false>>(KIND_COLUMN, M, E, 4, C)
 #define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
 #define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)

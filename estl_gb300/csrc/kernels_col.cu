@@ -14,6 +14,8 @@
   static_assert(ColKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
 #define ESTL_X_TC_ROW(M, C) \
   static_assert(RowKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
+#define ESTL_X_BULK_COL(M, E, R, C) \
+  static_assert(BulkColKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-copy tile too large");
 namespace estl {
 #include "kernel_list.inc"
 }
@@ -23,6 +25,7 @@ namespace estl {
 static const KernelDesc kTable[] = {
 #define ESTL_X_COL(M, E, R, C) ESTL_COL(M, E, R, C),
 #define ESTL_X_PIPE_COL(M, E, R, C) ESTL_PIPE_COL(M, E, R, C),
+#define ESTL_X_BULK_COL(M, E, R, C) ESTL_BULK_COL(M, E, R, C),
 #define ESTL_X_TC_COL(M, C) ESTL_TC_COL(M, C),
 #define ESTL_X_COLUMN(M, E, C) ESTL_COLUMN(M, E, C),
 #include "kernel_list.inc"

@@ -27,6 +27,7 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) v.push_back(cfg_of<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
+#define ESTL_X_BULK_COL(M, E, R, C) v.push_back(cfg_of<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_COLUMN(M, E, C) v.push_back(cfg_of<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));

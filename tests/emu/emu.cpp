@@ -78,6 +78,7 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
 #define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) k.push_back(mk<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
+#define ESTL_X_BULK_COL(M, E, R, C) k.push_back(mk<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_COLUMN(M, E, C) k.push_back(mk<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));

@@ -166,3 +166,22 @@ def test_twiddle_bank_accuracy(emu):
         exact = np.exp(-2j * np.pi * j / (1 << k))
         got = bank[(1 << k) + j]
         assert np.abs(got - exact).max() < 6e-8
+
+
+@pytest.mark.parametrize("col", [(7, 4, 5), (8, 4, 3), (9, 4, 4), (10, 4, 2), (11, 4, 2), (12, 4, 1)])
+def test_tensor_copy_column_tiles(emu, col):
+    """The persistent column pass whose tiles arrive as 2D tensor copies
+    (bulk_core.cuh BulkColKernel, pipelined = 2): the emulated boxes check the
+    16-byte x offset, the 128-byte shared-memory alignment and the source
+    bounds of every box; two CTAs loop over the tiles through both stages."""
+    logm, loge, logc = col
+    logn = logm + 9
+    n = 1 << logn
+    choice = [2, -1, -1, logm, loge, logc, 4, 2, 0, 0, 2]
+    d = describe(emu, n, 2, choice)
+    assert d["kernels"][0]["kind"] == "col" and d["kernels"][0]["pipe"] == 2
+    x = rand_c64((2, n), 90 + logm)
+    for sign in (-1, +1):
+        rc, msg, y = emu_run(emu, n, 2, x, sign, choice)
+        assert rc == 0, msg
+        assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL

@@ -199,3 +199,27 @@ def test_bulk_load_row_tiles(engine, logn, split, row_e, row_c):
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("logn,col", [(16, (7, 4, 5)), (17, (8, 4, 4)), (17, (8, 4, 3)), (18, (9, 4, 3)),
+                                      (20, (9, 4, 4)), (19, (10, 4, 2)), (21, (10, 4, 3)), (22, (11, 4, 2)),
+                                      (24, (12, 4, 1))])
+def test_tensor_copy_column_tiles(engine, logn, col):
+    """The persistent column pass whose strided tiles arrive as 2D tensor
+    copies (pipelined = 2, bulk_core.cuh BulkColKernel) against the oracle,
+    both directions, and its wait-timeout word clear afterwards."""
+    import torch
+    logm, loge, logc = col
+    n = 1 << logn
+    batch = max(2, (1 << 23) // n)
+    x = uniform_c64((batch, n), 800 + logn)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, batch, direction, mode="four_step",
+                        tiles={"split_log2": logm, "col_loge": loge, "col_logc": logc, "row_loge": 4, "row_logc": 2,
+                               "pipelined": 2})
+        d = p.describe()
+        assert d["kernels"][0]["kind"] == "col" and d["kernels"][0]["pipe"] == 2 and d["kernels"][0]["logm"] == logm
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
