@@ -53,6 +53,8 @@ def compact_choice(c):
     """Short text form of an autotuner plan choice."""
     if c["mode"] == 1:
         return f"single {c['single_loge']}.{c['single_logc']}"
+    if c["mode"] == 4:
+        return f"three-pass R 2^{c['logn2']} Q 2^{c.get('logn3', -1)} chunk {c['chunk']} pipe {c['pipe']}"
     kind = "stream" if c["mode"] == 3 else "four-step"
     return (f"{kind} col {c['logn2']}.{c['col_loge']}.{c['col_logc']} row {c['row_loge']}.{c['row_logc']} "
             f"chunk {c['chunk']} lag {c['lag']} pipe {c['pipe']}")

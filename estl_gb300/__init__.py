@@ -68,14 +68,14 @@ def _stream_handle(stream):
 class Plan:
     """`batch` transforms of length n, forward (-1) or backward (+1)."""
 
-    MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3}
+    MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3, "three_pass": 4}
 
     TILE_FIELDS = ("split_log2", "single_loge", "single_logc", "col_loge", "col_logc", "row_loge", "row_logc",
-                   "pipelined")
+                   "pipelined", "split2_log2")
 
     def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0, tiles=None):
         """tiles: optional dict of estl_plan_options tile fields (split_log2, col_loge, ...; modes
-        single / four_step), missing ones left to the planner."""
+        single / four_step / three_pass), missing ones left to the planner."""
         _ensure_init()
         self.n, self.batch, self.direction = int(n), int(batch), int(direction)
         h = ctypes.c_void_p()

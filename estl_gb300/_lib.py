@@ -121,13 +121,14 @@ REQ_CONV = 1
 
 
 class PlanOptions(ctypes.Structure):
-    """estl_plan_options: mode 0 auto, 1 single tile, 2 four-step, 3 streamed four-step;
-    explicit_tiles != 0 fixes the tile kernels (-1 fields: planner's choice)."""
+    """estl_plan_options: mode 0 auto, 1 single tile, 2 four-step, 3 streamed four-step,
+    4 three-pass; explicit_tiles != 0 fixes the tile kernels (-1 fields: planner's choice)."""
     _fields_ = [("mode", ctypes.c_int), ("lag", ctypes.c_int), ("chunk", ctypes.c_int64),
                 ("explicit_tiles", ctypes.c_int), ("split_log2", ctypes.c_int),
                 ("single_loge", ctypes.c_int), ("single_logc", ctypes.c_int),
                 ("col_loge", ctypes.c_int), ("col_logc", ctypes.c_int),
-                ("row_loge", ctypes.c_int), ("row_logc", ctypes.c_int), ("pipelined", ctypes.c_int)]
+                ("row_loge", ctypes.c_int), ("row_logc", ctypes.c_int), ("pipelined", ctypes.c_int),
+                ("split2_log2", ctypes.c_int)]
 
 
 class ConvRequest(ctypes.Structure):

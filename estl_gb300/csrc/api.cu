@@ -241,6 +241,8 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.grid = grid;
     a.split = st.tc ? plan.choice.split : SPLIT_NONE;
     a.err = E.dev_err;
+    a.ologr = st.ologr;
+    if (st.ologr) a.sgn = 1.f;  // middle pass of three: its input is conjugated already
     alignas(64) CUtensorMap map;
     if (d->tmap) {
       s = encode_column_map(&map, src + st.src_off, st);
@@ -456,7 +458,7 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
                                 const estl_plan_options* options, estl_plan* plan) {
-  if (options && (options->mode < 0 || options->mode > 3 || options->lag < 0 || options->chunk < 0))
+  if (options && (options->mode < 0 || options->mode > 4 || options->lag < 0 || options->chunk < 0))
     return fail(ESTL_INVALID_ARG, "bad plan options (mode %d, lag %d, chunk %lld)", options->mode, options->lag,
                 (long long)options->chunk);
   return plan_create_impl(n, batch, direction, precision, options, plan);
@@ -600,6 +602,7 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
       choice.row_loge = opt->row_loge;
       choice.row_logc = opt->row_logc;
       choice.pipe = opt->pipelined < 0 ? 0 : opt->pipelined;
+      choice.logn3 = opt->split2_log2;
     }
   } else {
     if (precision == ESTL_PREC_FP32) tuner_lookup(n, batch, &choice);

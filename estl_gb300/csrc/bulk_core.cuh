@@ -295,7 +295,6 @@ struct BulkColKernel {
     const int t = tid >> LOGC;
     const int logn1 = a.logn - LOGM;
     const int nblk = 1 << (logn1 - LOGC);
-    const long long N = 1LL << a.logn;
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
     if (tid == 0) {
       mbar_init(&bar[0], 1);
@@ -322,7 +321,7 @@ struct BulkColKernel {
       if (tid == 0 && tile + 2 * grid < nt) issue(a, tile + 2 * grid, stage.p, &bar[s]);
       const long long f = tile / nblk;
       const int n1 = (int)(tile - f * nblk) * C + c;
-      Base::store_twiddled(v, a.out.sub(f * N, N), n1, t, a.logn, a.bank);
+      Base::store_twiddled(v, Base::out_of(a.out, f, a.logn, a.ologr), n1, t, a.logn, a.bank, a.ologr);
     }
   }
 };

@@ -421,6 +421,7 @@ struct TileArgs {
   int split;       // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
   long long* err;  // bulk-load kernels: 1 + the tile whose bounded wait gave up (0 = none)
   const void* tmap = nullptr;  // tensor-map kernels: the CUtensorMap kernel parameter of the input
+  int ologr = 0;  // column tiles: interleaved output of a three-pass plan's middle pass (planner.h Step::ologr)
 };
 
 ESTL_HD void atomic_max_ll(long long* p, long long v) {
@@ -519,7 +520,8 @@ struct ColKernel {
   // Columns n1_0 .. n1_0 + C - 1 of one transform: in = the transform
   // (N elements), out = its scratch (N elements, S[k2*N1 + n1]).
   ESTL_HD static void body(const Ptr<const cf32>& in, const Ptr<cf32>& out, int n1_0, int logn, int tid,
-                           cf32* smraw, const Ptr<const cf32>& bank, float sgn, int split = SPLIT_NONE) {
+                           cf32* smraw, const Ptr<const cf32>& bank, float sgn, int split = SPLIT_NONE,
+                           int ologr = 0) {
     const int c = tid & (C - 1);
     const int t = tid >> LOGC;
     const int logn1 = logn - LOGM;
@@ -541,7 +543,7 @@ struct ColKernel {
       run_passes<TL, 0>(v, t, c, sm, tw, Sidx{});
     }
     if constexpr (TW) {
-      store_twiddled(v, out, n1, t, logn, bank);
+      store_twiddled(v, out, n1, t, logn, bank, ologr);
     } else {
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << logn1) + n1] = conj_if(v[j], sgn);
@@ -554,7 +556,7 @@ struct ColKernel {
   // four for W, W^2, W^4, W^8, and the other powers by products (instead of a
   // scattered two-level lookup per element).
   ESTL_HD static void store_twiddled(cf32 (&v)[TL::E], const Ptr<cf32>& out, int n1, int t, int logn,
-                                     const Ptr<const cf32>& bank) {
+                                     const Ptr<const cf32>& bank, int ologr = 0) {
     static_assert(TL::E == 16 || TL::E == 32, "column tiles hold 16 or 32 elements per thread");
     const int logn1 = logn - LOGM;
     const int logq = LOGE + logn1;  // W = w_{2^logq}^{n1}
@@ -570,8 +572,20 @@ struct ColKernel {
       for (int j = 16; j < 32; ++j) v[j] = cmul(v[j], base16);
       apply_powers16(v + 16, w1, w2, w4, w8);
     }
+    const int oshift = logn1 + ologr;  // output row pitch: N1, or 2^ologr N1 (three-pass middle pass)
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << logn1) + n1] = v[j];
+    for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << oshift) + n1] = v[j];
+  }
+
+  // Output of transform f of the step: its own N elements, or (three-pass
+  // middle pass, ologr > 0) rows interleaved 2^ologr apart with transform
+  // f = b 2^ologr + k3 starting at b N 2^ologr + k3 N1.
+  ESTL_HD static Ptr<cf32> out_of(const Ptr<cf32>& out, long long f, int logn, int ologr) {
+    const long long N = 1LL << logn;
+    if (!ologr) return out.sub(f * N, N);
+    const long long r = f & ((1LL << ologr) - 1);
+    const long long off = ((f >> ologr) << (logn + ologr)) + (r << (logn - LOGM));
+    return out.sub(off, (N << ologr) - (r << (logn - LOGM)));
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
@@ -580,7 +594,8 @@ struct ColKernel {
     const int nblk = (1 << logn1) >> LOGC;
     const long long f = cta / nblk;
     const int n1_0 = (int)(cta - f * nblk) * C;
-    body(a.in.sub(f * N, N), a.out.sub(f * N, N), n1_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
+    body(a.in.sub(f * N, N), out_of(a.out, f, a.logn, a.ologr), n1_0, a.logn, tid, smraw, a.bank, a.sgn, a.split,
+         a.ologr);
   }
 };
 

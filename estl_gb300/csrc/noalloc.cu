@@ -126,6 +126,8 @@ extern "C" estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direct
   const cf32* in = static_cast<const cf32*>(d_in);
   cf32* out = static_cast<cf32*>(d_out);
   for (const Step& step : plan.steps) {
+    if (step.src == BUF_OUT || step.ologr)
+      return fail(ESTL_UNSUPPORTED_SIZE, "estl_execute_noalloc: plans of three passes are not supported");
     const KernelDesc* d = find_desc(step);
     if (!d) return fail(ESTL_UNSUPPORTED_SIZE, "estl_execute_noalloc: no kernel for a plan step");
     s = check_cuda(cudaFuncSetAttribute(d->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->smem_bytes),

@@ -200,6 +200,66 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     return true;
   }
 
+  if (mode == 4) {
+    // three passes, N = R * Q * P (x[n1 + P n2 + PQ n3]):
+    //   A  column DFTs of length R over the PQ columns, four-step twiddle
+    //      w_N^{n' k3} (n' = n1 + P n2)             in      -> out (temporary)
+    //   B  per (b, k3): column DFTs of length Q over the P columns, twiddle
+    //      w_{PQ}^{n1 k2}, stored as rows k3 + R k2   out     -> scratch
+    //   C  row DFTs of length P, X[k3 + R k2 + RQ k1]  scratch -> out
+    // Every pass moves C-wide runs of 2^7..2^9-point tiles.
+    if (tc) {
+      set_err(err, "split precision runs the single / four-step tiles (mode %lld)", choice.mode);
+      return false;
+    }
+    const int lr = choice.logn2 > 0 ? choice.logn2 : (logn + 2) / 3;
+    const int lq = choice.logn3 > 0 ? choice.logn3 : (logn - lr + 1) / 2;
+    const int lp = logn - lr - lq;
+    if (lr < 7 || lr > 9 || lq < 7 || lq > 9 || lp < 7 || lp > 9) {
+      set_err(err, "three-pass plan needs three DFT lengths of 2^7..2^9 (log2 N = %lld)", logn);
+      return false;
+    }
+    static const int col_c[10] = {0, 0, 0, 0, 0, 0, 0, 5, 4, 3}, row_c[10] = {0, 0, 0, 0, 0, 0, 0, 4, 3, 2};
+    auto col_for = [&](int m) -> const TileCfg* {
+      if (choice.col_loge >= 0)
+        if (const TileCfg* c = find_tile(STEP_COL, m, choice.col_loge, 4, choice.col_logc)) return c;
+      return find_tile(STEP_COL, m, 4, 4, col_c[m]);
+    };
+    const TileCfg* ca = col_for(lr);
+    const TileCfg* cb = col_for(lq);
+    const TileCfg* r = choice.row_loge >= 0 ? find_tile(STEP_ROW, lp, choice.row_loge, 4, choice.row_logc) : nullptr;
+    if (!r) r = find_tile(STEP_ROW, lp, 4, 4, row_c[lp]);
+    if (!ca || !cb || !r || cb->logc > lp || ca->logc > lq + lp || r->logc > lr + lq) {
+      set_err(err, "no three-pass tiles instantiated for log2 N = %lld with first column DFTs of 2^%lld", logn, lr);
+      return false;
+    }
+    long long chunk = choice.chunk > 0 ? choice.chunk : std::max(1LL, (1LL << 27) / n);
+    chunk = std::min(chunk, batch);
+    p.scratch_elems = chunk * n;
+    // pipelined = 2: the bulk-load variants; other values run the plain tiles
+    PlanChoice pc = choice;
+    if (pc.pipe != 2) pc.pipe = 0;
+    for (long long b0 = 0; b0 < batch; b0 += chunk) {
+      const long long cnt = std::min(chunk, batch - b0);
+      Step a{STEP_COL, ca->logm, ca->loge, ca->logr, ca->logc, cnt << (logn - lr - ca->logc), BUF_IN, BUF_OUT,
+             b0 * n, cnt * n, b0 * n, cnt * n, cnt, logn};
+      Step b{STEP_COL, cb->logm, cb->loge, cb->logr, cb->logc, (cnt << lr) << (lp - cb->logc), BUF_OUT, BUF_SCRATCH,
+             b0 * n, cnt * n, 0, cnt * n, cnt << lr, lq + lp};
+      Step c{STEP_ROW, r->logm, r->loge, r->logr, r->logc, cnt << (logn - lp - r->logc), BUF_SCRATCH, BUF_OUT,
+             0, cnt * n, b0 * n, cnt * n, cnt, logn};
+      b.ologr = lr;
+      a.pipe = use_pipe(pc, ca);
+      b.pipe = use_pipe(pc, cb);
+      c.pipe = use_pipe(pc, r);
+      p.steps.push_back(a);
+      p.steps.push_back(b);
+      p.steps.push_back(c);
+    }
+    p.hbm_passes = 3;
+    *out = p;
+    return true;
+  }
+
   if (mode == 1) {
     if (logn > kSingleMaxLog) {
       set_err(err, "single-kernel plan needs log2 n <= %lld (got %lld)", kSingleMaxLog, logn);
@@ -229,10 +289,11 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
 
   // four-step.  Defaults: the autotuner's winners on a GB300 for 1 GiB
   // batches, log2 N -> (log2 N2, column log2 E / log2 C, row log2 E / log2 C,
-  // row pass with bulk tile loads); other lengths split N2 = 2^floor(log2 N / 2).
+  // pipelined: 2 = the bulk-load variants where they exist); other lengths
+  // split N2 = 2^floor(log2 N / 2).
   static const int tuned4[][7] = {{15, 7, 4, 5, 4, 3, 0},  {16, 7, 4, 5, 4, 2, 2},  {17, 8, 4, 4, 4, 2, 2},
-                                  {18, 9, 4, 4, 4, 2, 2},  {19, 10, 4, 3, 4, 2, 2}, {20, 9, 4, 4, 4, 2, 2},
-                                  {21, 10, 4, 3, 4, 2, 2}, {22, 10, 4, 3, 4, 2, 0}, {23, 11, 5, 3, 5, 2, 0},
+                                  {18, 9, 4, 3, 4, 2, 2},  {19, 10, 4, 3, 4, 2, 2}, {20, 10, 4, 2, 4, 2, 2},
+                                  {21, 10, 4, 3, 4, 2, 2}, {22, 11, 4, 2, 4, 2, 2}, {23, 11, 4, 2, 4, 2, 2},
                                   {24, 12, 5, 2, 5, 2, 0}};
   const int* td = nullptr;
   if (!tc && choice.logn2 < 0 && choice.col_loge < 0 && choice.row_loge < 0)
@@ -275,10 +336,10 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
            b0 * n, cnt * n, 0, cnt * n, cnt, logn};
     Step b{STEP_ROW, row->logm, row->loge, row->logr, row->logc, cnt << (logn2 - row->logc), BUF_SCRATCH, BUF_OUT,
            0, cnt * n, b0 * n, cnt * n, cnt, logn};
-    a.pipe = tc ? 0 : use_pipe(choice, col);
-    b.pipe = tc ? 0 : use_pipe(choice, row);
-    if (td && choice.pipe == 0 && td[6] && find_tile(STEP_ROW, row->logm, row->loge, row->logr, row->logc, td[6]))
-      b.pipe = td[6];
+    PlanChoice pc = choice;
+    if (td && choice.pipe == 0) pc.pipe = td[6];
+    a.pipe = tc ? 0 : use_pipe(pc, col);
+    b.pipe = tc ? 0 : use_pipe(pc, row);
     a.tc = b.tc = tc ? 1 : 0;
     p.steps.push_back(a);
     p.steps.push_back(b);
@@ -390,6 +451,19 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       out.push_back(ch);
     }
   }
+  for (int lr = 7; lr <= 9; ++lr)
+    for (int lq = 7; lq <= 9; ++lq) {
+      const int lp = logn - lr - lq;
+      if (lp < 7 || lp > 9) continue;
+      for (int pipe : {0, 2}) {
+        PlanChoice ch;
+        ch.mode = 4;
+        ch.logn2 = lr;
+        ch.logn3 = lq;
+        ch.pipe = pipe;
+        out.push_back(ch);
+      }
+    }
   if (logn >= 14) {
     for (int logn2 = 7; logn2 <= 12; ++logn2) {
       int logn1 = logn - logn2;
@@ -433,7 +507,7 @@ std::string Plan1D::describe() const {
   const char* names[] = {"single", "col", "row", "copy", "stream", "column"};
   // the first two steps (one chunk), and for 2D plans the column step
   std::vector<size_t> idx;
-  for (size_t i = 0; i < steps.size() && i < 2; ++i)
+  for (size_t i = 0; i < steps.size() && i < (size_t)(hbm_passes == 3 ? 3 : 2); ++i)
     if (!(xdim > 0 && steps[i].kind == STEP_COLUMN)) idx.push_back(i);
   if (xdim > 0 && !steps.empty() && steps.back().kind == STEP_COLUMN) idx.push_back(steps.size() - 1);
   int shown = 0;

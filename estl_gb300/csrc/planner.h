@@ -52,6 +52,11 @@ struct Step {
   int pipe = 0;
   // tensor-core variant (radix-16 passes as split-precision GEMMs)
   int tc = 0;
+  // middle pass of a three-pass plan (STEP_COL): its input is already
+  // conjugated for a backward transform (no conjugation on load), and inner
+  // transform f = b * 2^ologr + k3 stores column output k2 at
+  // b * N + k3 * N1 + k2 * 2^ologr * N1 (N1 = 2^(logn - logm)).
+  int ologr = 0;
 };
 
 // Streamed four-step configuration of a length (stream_list.inc), or nullptr.
@@ -63,9 +68,10 @@ const StreamCfg* find_stream_cfg(int logn);
 // Tunable plan parameters (what the autotuner searches).  Zero / -1 fields
 // mean "planner default".
 struct PlanChoice {
-  int mode = 0;  // 0 default, 1 single kernel, 2 four-step, 3 streamed four-step
+  int mode = 0;  // 0 default, 1 single kernel, 2 four-step, 3 streamed four-step, 4 three-pass
   int single_loge = -1, single_logc = -1;
-  int logn2 = -1;  // four-step: log2 N2 (column DFT length)
+  int logn2 = -1;  // four-step: log2 N2 (column DFT length); three-pass: log2 R (first column DFTs)
+  int logn3 = -1;  // three-pass: log2 Q (second column DFTs); <= 0 = default
   int col_loge = -1, col_logc = -1;
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)

@@ -73,9 +73,10 @@ std::string choice_to_json(const PlanChoice& c) {
   char buf[400];
   std::snprintf(buf, sizeof buf,
                 "{\"mode\": %d, \"single_loge\": %d, \"single_logc\": %d, \"logn2\": %d, \"col_loge\": %d, "
-                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"lag\": %d, \"pipe\": %d}",
+                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"lag\": %d, \"pipe\": %d, "
+                "\"logn3\": %d}",
                 c.mode, c.single_loge, c.single_logc, c.logn2, c.col_loge, c.col_logc, c.row_loge, c.row_logc, c.chunk,
-                c.lag, c.pipe);
+                c.lag, c.pipe, c.logn3);
   return buf;
 }
 
@@ -102,6 +103,7 @@ void tuner_load_cache() {
     e.choice.chunk = json_int(line, "chunk", 0);
     e.choice.lag = (int)json_int(line, "lag", 0);
     e.choice.pipe = (int)json_int(line, "pipe", 0);
+    e.choice.logn3 = (int)json_int(line, "logn3", -1);
     g_cache[{gpu, n, bb}] = e;  // later lines win
   }
 }

@@ -89,15 +89,21 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
  * (tuning cache, else defaults), 1 single-tile kernel (n <= 2^14),
  * 2 four-step as a column launch and a row launch per chunk of transforms
  * (two HBM round trips), 3 streamed four-step: one persistent launch whose
- * column and row tiles share a scratch ring small enough to stay in L2.
+ * column and row tiles share a scratch ring small enough to stay in L2,
+ * 4 three-pass (N = R * Q * P, 2^21 <= N <= 2^24, each of R, Q, P in
+ * 2^7..2^9): two column launches and a row launch per chunk, three HBM round
+ * trips of wide runs instead of two of narrow ones.
  * lag (mode 3): transforms between a column tile and the row tiles that read
  * it (0 = default).  chunk (mode 2): transforms per launch pair (0 = default).
  * explicit_tiles != 0 (modes 1 and 2) also fixes the tile kernels, each field
  * -1 for the planner's choice: split_log2 = log2 N2 of N = N1 * N2 (the column
  * DFT length), *_loge = log2 elements per thread, *_logc = log2 transforms
  * (single) or columns / rows (four-step) per CTA, pipelined = 1 for the
- * cp.async double-buffered variant where one exists.  A zero-initialised
- * struct with mode = 0 is the automatic plan. */
+ * cp.async double-buffered variant where one exists, 2 for the persistent
+ * bulk-load variants (row tiles by bulk copies, column tiles by 2D tensor
+ * copies).  Mode 4 reads split_log2 as log2 R and split2_log2 as log2 Q
+ * (0 or -1 = default).  A zero-initialised struct with mode = 0 is the
+ * automatic plan. */
 typedef struct estl_plan_options {
   int mode;
   int lag;
@@ -108,6 +114,7 @@ typedef struct estl_plan_options {
   int col_loge, col_logc;
   int row_loge, row_logc;
   int pipelined;
+  int split2_log2;
 } estl_plan_options;
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,

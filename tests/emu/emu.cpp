@@ -312,6 +312,7 @@ PlanChoice choice_from(const int* f) {
   c.lag = f[9];
   c.pipe = f[10];
   c.split = f[11];
+  c.logn3 = f[12];
   return c;
 }
 
@@ -320,7 +321,7 @@ PlanChoice choice_from(const int* f) {
 extern "C" {
 
 // Runs the plan for (n, batch) on interleaved complex64 host data.
-// choice: 12 ints (PlanChoice fields) or NULL for the planner default.
+// choice: 13 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
 static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen);
@@ -477,6 +478,8 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
     a.logn = st.logn;
     a.logn1 = 0;
     a.sgn = sign < 0 ? 1.f : -1.f;
+    a.ologr = st.ologr;
+    if (st.ologr) a.sgn = 1.f;  // middle pass of three: its input is conjugated already
     // pipelined kernels are grid-stride: emulate one or two CTAs so that every
     // CTA loops over several tiles and uses both tile buffers
     const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
@@ -505,13 +508,13 @@ int emu_plan_describe(long long n, long long batch, const int* choice, char* buf
 }
 
 // Candidate choices of the autotuner for (n, batch): writes up to max rows
-// of 12 ints, returns the number of candidates.
+// of 13 ints, returns the number of candidates.
 int emu_plan_candidates(long long n, long long batch, int* out, int max) {
   std::vector<PlanChoice> c = plan_candidates(n, batch);
   int k = 0;
   for (const PlanChoice& ch : c) {
     if (k >= max) break;
-    int* f = out + 12 * k++;
+    int* f = out + 13 * k++;
     f[0] = ch.mode;
     f[1] = ch.single_loge;
     f[2] = ch.single_logc;
@@ -524,6 +527,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[9] = ch.lag;
     f[10] = ch.pipe;
     f[11] = ch.split;
+    f[12] = ch.logn3;
   }
   return (int)c.size();
 }

@@ -25,12 +25,11 @@ def rand_c64(shape, seed):
 def pad_choice(choice):
     """PlanChoice fields: mode, single_loge, single_logc, logn2, col_loge,
     col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available),
-    split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes)."""
+    split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes),
+    logn3 (three-pass: log2 of the second column DFT length, 0 = default)."""
     c = list(choice)
-    if len(c) < 10:
-        c += [0] * (10 - len(c))
-    if len(c) < 12:
-        c += [0] * (12 - len(c))
+    if len(c) < 13:
+        c += [0] * (13 - len(c))
     return c
 
 
@@ -39,20 +38,20 @@ def emu_run(emu, n, batch, x, sign=-1, choice=None):
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 12)(*pad_choice(choice))
+        ch = (ctypes.c_int * 13)(*pad_choice(choice))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (12 * 4096))()
+    buf = (ctypes.c_int * (13 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[12 * i: 12 * i + 12]) for i in range(min(k, 4096))]
+    return [list(buf[13 * i: 13 * i + 13]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 12)(*pad_choice(choice)) if choice is not None else None
+    ch = (ctypes.c_int * 13)(*pad_choice(choice)) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())
@@ -185,3 +184,21 @@ def test_tensor_copy_column_tiles(emu, col):
         rc, msg, y = emu_run(emu, n, 2, x, sign, choice)
         assert rc == 0, msg
         assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL
+
+
+@pytest.mark.parametrize("logn,lr,lq,pipe", [(21, 7, 7, 0), (21, 7, 7, 2), (22, 8, 7, 2), (22, 7, 8, 0)])
+def test_three_pass(emu, logn, lr, lq, pipe):
+    """Three-pass plan (mode 4): column DFTs of 2^lr and 2^lq, the middle
+    pass storing interleaved rows, then row DFTs; both directions, plain and
+    bulk-load tiles, against the oracle."""
+    n = 1 << logn
+    choice = [4, -1, -1, lr, -1, -1, -1, -1, 0, 0, pipe, 0, lq]
+    d = describe(emu, n, 1, choice)
+    assert d["hbm_passes"] == 3 and [k["kind"] for k in d["kernels"]] == ["col", "col", "row"]
+    assert [k["logm"] for k in d["kernels"]] == [lr, lq, logn - lr - lq]
+    assert all(k["pipe"] == pipe for k in d["kernels"][:2])
+    x = rand_c64((1, n), 60 + logn)
+    for sign in (-1, +1):
+        rc, msg, y = emu_run(emu, n, 1, x, sign, choice)
+        assert rc == 0, msg
+        assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < 2 * logn * 2.0 ** -24

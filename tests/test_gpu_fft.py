@@ -223,3 +223,22 @@ def test_tensor_copy_column_tiles(engine, logn, col):
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("logn,lr,lq,pipe", [(21, 7, 7, 2), (22, 8, 7, 0), (23, 8, 8, 2), (23, 8, 7, 2),
+                                             (24, 8, 8, 0), (24, 8, 8, 2), (24, 9, 8, 2)])
+def test_three_pass(engine, logn, lr, lq, pipe):
+    """Three-pass plans (mode three_pass: column DFTs of 2^lr, column DFTs of
+    2^lq stored as interleaved rows, row DFTs) against the oracle, both
+    directions, with two transforms per launch."""
+    import torch
+    n = 1 << logn
+    x = uniform_c64((2, n), 900 + logn)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, 2, direction, mode="three_pass", tiles={"split_log2": lr, "split2_log2": lq, "pipelined": pipe})
+        d = p.describe()
+        assert d["hbm_passes"] == 3 and [k["logm"] for k in d["kernels"]] == [lr, lq, logn - lr - lq]
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
