@@ -98,6 +98,7 @@ constexpr int kSingleMaxLog = 14;
 constexpr int kTcSingleMaxLog = 13;  // split precision: larger n run four-step
 constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;
+constexpr int kThreePassDefaultLog = 23;  // default plans of N >= 2^23 (FP32) run three passes
 
 // Returns false (with *err set) when n is not a power of two in [1, 2^24] or
 // the choice names no instantiated kernel.

@@ -141,8 +141,12 @@ def test_plan_shapes(emu):
     assert d["hbm_passes"] == 2 and d["kernels"][0]["kind"] == "col" and d["kernels"][1]["kind"] == "row"
     assert d["scratch_bytes"] <= 1 << 30
     d = describe(emu, 1 << 24, 16)
-    assert d["launches"] == 4  # 1 GiB scratch = eight 2^24-point transforms per chunk, 2 launches per chunk
-    # the tuned default of 2^24: 2^12 x 2^12 with 32-element column and row tiles of 4 columns / rows
+    assert d["launches"] == 6  # 1 GiB scratch = eight 2^24-point transforms per chunk, 3 launches per chunk
+    # the default of 2^24: three passes, 2^7 x 2^8 column DFTs and 2^9-point rows, bulk-load tiles
+    assert d["hbm_passes"] == 3
+    assert [(k["kind"], k["logm"], k["pipe"]) for k in d["kernels"]] == [("col", 7, 2), ("col", 8, 2), ("row", 9, 2)]
+    d = describe(emu, 1 << 24, 16, [2, -1, -1, -1, -1, -1, -1, -1])
+    # the tuned four-step of 2^24: 2^12 x 2^12 with 32-element column and row tiles of 4 columns / rows
     assert [(k["logm"], k["loge"], k["logc"]) for k in d["kernels"]] == [(12, 5, 2), (12, 5, 2)]
 
 
