@@ -19,8 +19,8 @@ from ._lib import (BACKWARD, FORWARD, LAYOUT_BLOCK_PLANAR, LAYOUT_INTERLEAVED, L
                    PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, PREC_SPLIT_FP16, EstlError,
                    PlanOptions, check, lib)
 
-__all__ = ["init", "shutdown", "Plan", "fft", "autotune", "max_batch", "memory_usage", "EstlError",
-           "FORWARD", "BACKWARD"]
+__all__ = ["init", "shutdown", "Plan", "Plan2D", "Conv2DPlan", "fft", "autotune", "max_batch", "memory_usage",
+           "EstlError", "FORWARD", "BACKWARD", "CONV_CORRELATE", "CONV_REFERENCE_COMPAT"]
 
 _initialised = False
 
@@ -188,6 +188,66 @@ class Plan2D(Plan):
         h = ctypes.c_void_p()
         check(lib().estl_plan2d_create(self.xdim, self.ydim, self.batch, self.direction, PREC_FP32, ctypes.byref(h)))
         self._h = h
+
+
+CONV_CORRELATE = 1
+CONV_REFERENCE_COMPAT = 2
+
+
+class Conv2DPlan:
+    """2D FFT convolution of `count` real images (height x width, row-major)
+    with one real filter (kheight x kwidth), after Convolution2D_FFT::convolve
+    (Convolution.h:95-148).  flags: CONV_CORRELATE, CONV_REFERENCE_COMPAT (the
+    reference's centred, K^[0]-normalised height x width result; default: the
+    full linear convolution)."""
+
+    def __init__(self, width, height, kwidth, kheight, count=1, flags=0):
+        _ensure_init()
+        self.width, self.height, self.kwidth, self.kheight = int(width), int(height), int(kwidth), int(kheight)
+        self.count, self.flags = int(count), int(flags)
+        ow, oh = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().estl_conv2d_output_size(self.width, self.height, self.kwidth, self.kheight, self.flags,
+                                            ctypes.byref(ow), ctypes.byref(oh)))
+        self.out_width, self.out_height = ow.value, oh.value
+        h = ctypes.c_void_p()
+        check(lib().estl_conv2d_plan_create(self.width, self.height, self.kwidth, self.kheight, self.count,
+                                            self.flags, ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def _check_tensor(x, numel, what):
+        import torch
+        if x.dtype != torch.float32 or not x.is_cuda or not x.is_contiguous() or x.numel() != numel:
+            raise EstlError(1, f"{what} must be a contiguous float32 CUDA tensor of {numel} elements")
+
+    def set_filter(self, k, stream=None):
+        """k: float32 CUDA tensor of kheight * kwidth elements."""
+        self._check_tensor(k, self.kwidth * self.kheight, "filter")
+        check(lib().estl_conv2d_plan_set_filter(self._h, ctypes.c_void_p(k.data_ptr()), _stream_handle(stream)))
+
+    def execute(self, images, out=None, stream=None):
+        """images: float32 CUDA tensor of count * height * width elements; returns
+        (count, out_height, out_width)."""
+        import torch
+        self._check_tensor(images, self.count * self.width * self.height, "images")
+        if out is None:
+            out = torch.empty((self.count, self.out_height, self.out_width), dtype=torch.float32,
+                              device=images.device)
+        self._check_tensor(out, self.count * self.out_width * self.out_height, "out")
+        check(lib().estl_conv2d_plan_execute(self._h, ctypes.c_void_p(images.data_ptr()),
+                                             ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().estl_conv2d_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _plan_cache = {}

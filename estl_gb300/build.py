@@ -25,6 +25,7 @@ SOURCES = [
     "noalloc.cu",
     "conv_plan.cpp",
     "conv.cu",
+    "conv2d.cu",
     "packed_plan.cpp",
     "packed.cu",
     "serve.cu",

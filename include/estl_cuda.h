@@ -283,6 +283,31 @@ estl_status estl_conv_plan_execute(estl_conv_plan plan, const float* d_signals, 
 int64_t estl_conv_plan_launches(estl_conv_plan plan);
 estl_status estl_conv_plan_destroy(estl_conv_plan plan);
 
+/* ---- 2D FFT convolution (Convolution2D_FFT::convolve, Convolution.h:95-148) ----
+ * `count` real images of height x width floats (row-major, x fastest, packed
+ * back-to-back) convolved with one real filter of kheight x kwidth floats:
+ * both zero-padded to Pw x Ph = nextPow2(width + kwidth - 1) x
+ * nextPow2(height + kheight - 1) (:96-97), 2D FFTs, pointwise product
+ * (conj of the filter spectrum with ESTL_CONV_CORRELATE, :125-137), inverse
+ * 2D FFT scaled by 1 / (Pw Ph).  Default output: the full linear convolution,
+ * (height + kheight - 1) x (width + kwidth - 1) per image.  With
+ * ESTL_CONV_REFERENCE_COMPAT the reference's own result: the filter centred
+ * by ((kwidth + 1) / 2, (kheight + 1) / 2) cyclically (:113-120), divided by
+ * Pw Ph K^[0] (:141-143), height x width kept (:146-148).  FP32; Pw <= 2^14,
+ * Ph <= 2^12, Pw Ph <= 2^26.  Three launches per execute (row FFTs of the
+ * padded rows, column FFT x spectrum x inverse column FFT, inverse row FFTs
+ * with the real crop); the filter spectrum is computed once per
+ * estl_conv2d_plan_set_filter.  Stream ordered. */
+estl_status estl_conv2d_output_size(int64_t width, int64_t height, int64_t kwidth, int64_t kheight, int flags,
+                                    int64_t* out_width, int64_t* out_height);
+typedef struct estl_conv2d_plan_s* estl_conv2d_plan;
+estl_status estl_conv2d_plan_create(int64_t width, int64_t height, int64_t kwidth, int64_t kheight, int64_t count,
+                                    int flags, estl_conv2d_plan* plan);
+estl_status estl_conv2d_plan_set_filter(estl_conv2d_plan plan, const float* d_filter, void* stream);
+estl_status estl_conv2d_plan_execute(estl_conv2d_plan plan, const float* d_images, float* d_out, void* stream);
+int64_t estl_conv2d_plan_launches(estl_conv2d_plan plan);
+estl_status estl_conv2d_plan_destroy(estl_conv2d_plan plan);
+
 /* ---- Uneven batches: packed transforms of mixed lengths ----
  * count transforms, transform i of length sizes[i] (a power of two in
  * [2, 2^18]) at complex-element offset offsets[i] of both the input and the

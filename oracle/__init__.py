@@ -4,10 +4,10 @@ The checker for the FFT engine, never the product: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline`` leg and
 the ``--impl reference`` arm) may import it.
 
-* ``fft`` / ``dft_ld`` / ``conv_fft`` / ``conv_direct``: FP64 restatement of the
-  reference's CPU transform (``FFT_FFTW3.h:23-31``, plan semantics of
-  ``fftwf_plan_many_dft``) and of its FFT convolution (``Convolution.h:95-148``),
-  in ``oracle.c``.
+* ``fft`` / ``dft_ld`` / ``conv_fft`` / ``conv_direct`` / ``conv2d_fft`` /
+  ``conv2d_direct``: FP64 restatement of the reference's CPU transform
+  (``FFT_FFTW3.h:23-31``, plan semantics of ``fftwf_plan_many_dft``) and of its
+  FFT convolution (``Convolution.h:95-148``, in 1D and in 2D), in ``oracle.c``.
 * ``ref_contiguous_fft``: FP32 restatement of the reference's own GPU
   algorithm (``FFT_OpenCL_Contiguous.h:144-184``), in ``ref_contiguous.c``;
   timed as the CPU baseline.
@@ -55,6 +55,9 @@ def _load():
         lib.oracle_conv_direct.argtypes = [P, I64, P, I64, P]
         lib.oracle_conv_fft.argtypes = [P, I64, P, I64, P, ctypes.c_int]
         lib.oracle_conv_fft.restype = ctypes.c_int
+        lib.oracle_conv2d_fft.argtypes = [P, I64, I64, P, I64, I64, P, ctypes.c_int, ctypes.c_int]
+        lib.oracle_conv2d_fft.restype = ctypes.c_int
+        lib.oracle_conv2d_direct.argtypes = [P, I64, I64, P, I64, I64, P]
         lib.ref_contiguous_fft.argtypes = [P, P, P, I64, I64, ctypes.c_int, ctypes.c_int]
         lib.ref_contiguous_fft.restype = ctypes.c_int
         _lib = lib
@@ -106,6 +109,32 @@ def conv_fft(a, b, correlate=False):
     b = np.ascontiguousarray(b, dtype=np.float64)
     out = np.empty(a.size + b.size - 1)
     _load().oracle_conv_fft(_ptr(a), a.size, _ptr(b), b.size, _ptr(out), int(bool(correlate)))
+    return out
+
+
+def conv2d_fft(a, k, correlate=False, compat=False):
+    """FP64 2D FFT convolution of a real image (h, w) with a real kernel
+    (kh, kw), after Convolution2D_FFT::convolve (Convolution.h:95-148):
+    compat=False gives the full linear convolution (h+kh-1, w+kw-1) / 1;
+    compat=True the reference's centred, K^[0]-normalised (h, w) result."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    h, w = a.shape
+    kh, kw = k.shape
+    shape = (h, w) if compat else (h + kh - 1, w + kw - 1)
+    out = np.empty(shape)
+    _load().oracle_conv2d_fft(_ptr(a), h, w, _ptr(k), kh, kw, _ptr(out), int(bool(correlate)), int(bool(compat)))
+    return out
+
+
+def conv2d_direct(a, k):
+    """Long-double direct 2D linear convolution, shape (h+kh-1, w+kw-1)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    h, w = a.shape
+    kh, kw = k.shape
+    out = np.empty((h + kh - 1, w + kw - 1))
+    _load().oracle_conv2d_direct(_ptr(a), h, w, _ptr(k), kh, kw, _ptr(out))
     return out
 
 

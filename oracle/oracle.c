@@ -225,3 +225,82 @@ int oracle_conv_fft(const double* a, int64_t la, const double* b, int64_t lb, do
   free(B);
   return 0;
 }
+
+/* 2D FFT of an h x w complex array in place (rows, then columns), FP64. */
+static void fft2d(c64* A, int64_t h, int64_t w, int sign) {
+  oracle_fft((double*)A, (double*)A, w, h, sign, 1);
+  c64* col = (c64*)malloc((size_t)h * sizeof(c64));
+  for (int64_t x = 0; x < w; x++) {
+    for (int64_t y = 0; y < h; y++) col[y] = A[y * w + x];
+    oracle_fft((double*)col, (double*)col, h, 1, sign, 1);
+    for (int64_t y = 0; y < h; y++) A[y * w + x] = col[y];
+  }
+  free(col);
+}
+
+/* 2D FFT convolution of a real h x w image with a real kh x kw kernel, after
+ * Convolution2D_FFT::convolve (Convolution.h:95-148), in FP64.  Both padded to
+ * W x H = nextPow2(w + kw - 1) x nextPow2(h + kh - 1) (:96-97), 2D FFTs,
+ * product (with conj of the kernel spectrum when correlate, :125-137),
+ * inverse 2D FFT.
+ *   compat = 0: the kernel at the origin, result / (W H), the full linear
+ *               convolution (h + kh - 1) x (w + kw - 1) kept;
+ *   compat = 1: the reference's own steps: kernel read from
+ *               ((x + (kw+1)/2) mod W, (y + (kh+1)/2) mod H) (:113-120),
+ *               result / (W H K^[0]) (:141-143), h x w kept (:146-148). */
+int oracle_conv2d_fft(const double* a, int64_t h, int64_t w, const double* k, int64_t kh, int64_t kw, double* out,
+                      int correlate, int compat) {
+  int64_t W = 1, H = 1;
+  while (W < w + kw - 1) W *= 2;
+  while (H < h + kh - 1) H *= 2;
+  c64* A = (c64*)calloc((size_t)(W * H), sizeof(c64));
+  c64* K = (c64*)calloc((size_t)(W * H), sizeof(c64));
+  for (int64_t y = 0; y < h; y++)
+    for (int64_t x = 0; x < w; x++) A[y * W + x].re = a[y * w + x];
+  const int64_t xo = compat ? (kw + 1) / 2 : 0, yo = compat ? (kh + 1) / 2 : 0;
+  for (int64_t y = 0; y < H; y++) {
+    const int64_t sy = (y + yo) % H;
+    for (int64_t x = 0; x < W; x++) {
+      const int64_t sx = (x + xo) % W;
+      if (sx < kw && sy < kh) K[y * W + x].re = k[sy * kw + sx];
+    }
+  }
+  fft2d(A, H, W, -1);
+  fft2d(K, H, W, -1);
+  const double k0 = K[0].re;
+  for (int64_t i = 0; i < W * H; i++) {
+    double br = K[i].re, bi = correlate ? -K[i].im : K[i].im;
+    double r = A[i].re * br - A[i].im * bi, im = A[i].re * bi + A[i].im * br;
+    A[i].re = r;
+    A[i].im = im;
+  }
+  fft2d(A, H, W, +1);
+  const double scale = 1.0 / ((double)W * (double)H * (compat ? k0 : 1.0));
+  const int64_t ow = compat ? w : w + kw - 1, oh = compat ? h : h + kh - 1;
+  for (int64_t y = 0; y < oh; y++)
+    for (int64_t x = 0; x < ow; x++) out[y * ow + x] = A[y * W + x].re * scale;
+  free(A);
+  free(K);
+  return 0;
+}
+
+/* Direct 2D linear convolution in long double:
+ * out[y][x] = sum_{r,q} a[y - r][x - q] k[r][q], (h + kh - 1) x (w + kw - 1). */
+void oracle_conv2d_direct(const double* a, int64_t h, int64_t w, const double* k, int64_t kh, int64_t kw,
+                          double* out) {
+  const int64_t ow = w + kw - 1, oh = h + kh - 1;
+  for (int64_t y = 0; y < oh; y++)
+    for (int64_t x = 0; x < ow; x++) {
+      long double s = 0.0L;
+      for (int64_t r = 0; r < kh; r++) {
+        const int64_t ya = y - r;
+        if (ya < 0 || ya >= h) continue;
+        for (int64_t q = 0; q < kw; q++) {
+          const int64_t xa = x - q;
+          if (xa < 0 || xa >= w) continue;
+          s += (long double)a[ya * w + xa] * (long double)k[r * kw + q];
+        }
+      }
+      out[y * ow + x] = (double)s;
+    }
+}

@@ -50,6 +50,9 @@ def emu():
     lib.emu_plan_candidates.argtypes = [ctypes.c_longlong, ctypes.c_longlong, P, ctypes.c_int]
     lib.emu_conv_run.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, ctypes.c_char_p, ctypes.c_int]
     lib.emu_conv_run.restype = ctypes.c_int
+    L = ctypes.c_longlong
+    lib.emu_conv2d_run.argtypes = [L, L, L, L, L, ctypes.c_int, P, P, P, ctypes.c_char_p, ctypes.c_int]
+    lib.emu_conv2d_run.restype = ctypes.c_int
     lib.emu_packed_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_char_p,
                                    ctypes.c_int]
     lib.emu_packed_run.restype = ctypes.c_int

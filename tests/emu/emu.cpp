@@ -25,6 +25,8 @@
 #include "fft_core.cuh"
 #include "packed_core.cuh"
 #include "bulk_core.cuh"
+#include "conv2d_core.cuh"
+#include "estl_cuda.h"
 #include "pipe_core.cuh"
 #include "stream_core.cuh"
 #include "planner.h"
@@ -318,6 +320,39 @@ PlanChoice choice_from(const int* f) {
 
 }  // namespace
 
+namespace {
+struct EmuC2Kernel {
+  int col, logm, loge, logc, nt;
+  long long smem;
+  void (*fn)(const Conv2dArgs&, long long, int, cf32*);
+};
+
+template <class K>
+EmuC2Kernel mk_c2(int col, int m, int e, int c) {
+  return EmuC2Kernel{col, m, e, c, K::NT, K::SMEM_ELEMS, &K::run};
+}
+
+const std::vector<EmuC2Kernel>& emu_c2_kernels() {
+  static const std::vector<EmuC2Kernel> v = [] {
+    std::vector<EmuC2Kernel> k;
+#define ESTL_X_C2ROW(M, E, C) k.push_back(mk_c2<Conv2dRowKernel<M, E, 4, C>>(0, M, E, C));
+#define ESTL_X_C2COL(M, E, C) k.push_back(mk_c2<Conv2dColKernel<M, E, 4, C>>(1, M, E, C));
+#include "conv2d_list.inc"
+    return k;
+  }();
+  return v;
+}
+
+// the tile choice of conv2d.cu: the row tile of the width, the widest column
+// tile no wider than the padded width
+const EmuC2Kernel* emu_c2_pick(int col, int logm, int logw) {
+  const EmuC2Kernel* best = nullptr;
+  for (const EmuC2Kernel& d : emu_c2_kernels())
+    if (d.col == col && d.logm == logm && (!col || d.logc <= logw) && (!best || d.logc > best->logc)) best = &d;
+  return best;
+}
+}  // namespace
+
 extern "C" {
 
 // Runs the plan for (n, batch) on interleaved complex64 host data.
@@ -588,6 +623,55 @@ int emu_conv_run(const long long* reqs, int count, int flags, int shared, const 
       set_err(err, errlen, g_msg);
       return 1;
     }
+  }
+  return 0;
+}
+
+// 2D convolution of count images (h rows of w floats) with one filter (kh
+// rows of kw floats), the launches of conv2d.cu: filter spectrum (row pass,
+// column pass), then row pass, column pass, row pass.  Returns 0 ok, 1
+// out-of-bounds access, 2 size error, 3 missing kernel.
+int emu_conv2d_run(long long w, long long h, long long kw, long long kh, long long count, int flags,
+                   const float* images, const float* filt, float* out, char* err, int errlen) {
+  Conv2dGeom g;
+  const int compat = (flags & ESTL_CONV_REFERENCE_COMPAT) ? 1 : 0;
+  if (count < 1 || !conv2d_geometry(w, h, kw, kh, compat != 0, &g) || !conv2d_supported(g)) {
+    set_err(err, errlen, "2D convolution sizes out of range");
+    return 2;
+  }
+  const EmuC2Kernel* row = emu_c2_pick(0, g.logw, g.logw);
+  const EmuC2Kernel* col = emu_c2_pick(1, g.logh, g.logw);
+  if (!row || !col) {
+    set_err(err, errlen, "no emulated 2D convolution tile");
+    return 3;
+  }
+  {
+    std::lock_guard<std::mutex> gl(g_msg_mu);
+    g_msg.clear();
+  }
+  const long long pts = 1LL << (g.logw + g.logh);
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  std::vector<cf32> spec((size_t)pts, cf32{nan, nan});
+  std::vector<cf32> work((size_t)(count * pts), cf32{nan, nan});
+  auto launch = [&](const EmuC2Kernel* k, const Conv2dArgs& a) {
+    const long long grid = conv2d_grid(k->col != 0, k->logc, a);
+    return grid < 1 || run_generic(k->nt, k->smem, k->fn, a, grid);
+  };
+  Conv2dArgs a = conv2d_filter_args(g, kw, kh, compat, flags & ESTL_CONV_CORRELATE, filt, spec.data(),
+                                    host_bank().data(), kBankSize);
+  bool ok = launch(row, a);
+  a.mode = 1;
+  ok = ok && launch(col, a);
+  Conv2dArgs b = conv2d_exec_args(g, w, h, count, compat, images, work.data(), spec.data(), out, host_bank().data(),
+                                  kBankSize);
+  ok = ok && launch(row, b);
+  ok = ok && launch(col, b);
+  b.mode = 1;
+  ok = ok && launch(row, b);
+  if (!ok) {
+    std::lock_guard<std::mutex> gl(g_msg_mu);
+    set_err(err, errlen, g_msg);
+    return 1;
   }
   return 0;
 }
