@@ -39,8 +39,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other benchmark configurations (4096x256, uneven batch, served convolution)")
+    ap.add_argument("--configs", type=str, default=None,
+                    help="comma-separated subset of the other configurations (plain_4096x256, uneven_8192, "
+                         "split_precision, fft2d, conv2d, conv_pairs, bluestein, served_conv)")
     ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
-    ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream"],
+    ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream", "three_pass"],
                     help="plan mode for every N (auto: autotuned / tuning cache / planner default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner pass that picks each N's plan before the timed region")
@@ -278,6 +281,63 @@ def bench_uneven(estl, torch):
     return res
 
 
+CONV_NO_PAIRING = 4  # ESTL_CONV_NO_PAIRING
+
+
+def bench_conv_pairs(estl, torch):
+    """The real-input specialisation on the device (estl_conv_execute, device
+    buffers, no host copies): batches of one padded length, each request its
+    own filter, two requests per complex transform (default) against one
+    (ESTL_CONV_NO_PAIRING); FP32 and split fp16."""
+    import ctypes
+    import numpy as np
+    from estl_gb300._lib import ConvRequest, check, lib
+    Lb = lib()
+    out = {"workload": "batched 1D FFT convolutions, N(0,1) signals and filters, seed 9, own filter per request",
+           "method": "host clock around 5 blocking estl_conv_execute calls after 2 warm-up calls (request "
+                     "layout, spectra and convolutions included)"}
+    st = torch.cuda.Stream()
+    for L, K, count in ((3000, 100, 8192), (900, 125, 32768), (12000, 385, 2048)):
+        g = torch.Generator(device="cuda").manual_seed(9)
+        sig = torch.randn(L * count, device="cuda", generator=g)
+        filt = torch.randn(K * count, device="cuda", generator=g)
+        o = torch.empty((L + K - 1) * count, device="cuda")
+        arr = (ConvRequest * count)(*[ConvRequest(L, K, i * L, i * K, i * (L + K - 1)) for i in range(count)])
+        res = {}
+        ref = None
+        for name, flags in (("paired", 0), ("unpaired", CONV_NO_PAIRING), ("paired_split_fp16", estl.PREC_SPLIT_FP16 << 8),
+                            ("unpaired_split_fp16", (estl.PREC_SPLIT_FP16 << 8) | CONV_NO_PAIRING)):
+            ws = ctypes.c_size_t()
+            check(Lb.estl_conv_workspace_size(arr, count, flags, ctypes.byref(ws)))
+            wsb = torch.empty(ws.value + 256, dtype=torch.uint8, device="cuda")
+            base = (wsb.data_ptr() + 255) // 256 * 256
+
+            def go():
+                check(Lb.estl_conv_execute(arr, count, flags, ctypes.c_void_p(sig.data_ptr()),
+                                           ctypes.c_void_p(filt.data_ptr()), ctypes.c_void_p(o.data_ptr()),
+                                           ctypes.c_void_p(base), ws.value, ctypes.c_void_p(st.cuda_stream)))
+            for _ in range(2):
+                go()
+            st.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                go()
+            st.synchronize()
+            ms = (time.perf_counter() - t0) / 5 * 1e3
+            if ref is None:
+                s0 = sig[:L].double().cpu().numpy()
+                f0 = filt[:K].double().cpu().numpy()
+                ref = fp64_conv(s0, f0)
+            y = o[:L + K - 1].double().cpu().numpy()
+            err = float(np.sqrt(np.sum((y - ref) ** 2) / np.sum(ref ** 2)))
+            res[name] = {"ms": round(ms, 3), "req_per_s": round(count / (ms * 1e-3), 1), "rel_l2_first": float(f"{err:.3e}")}
+            del wsb
+        res["paired_speedup"] = round(res["unpaired"]["ms"] / res["paired"]["ms"], 2)
+        res["paired_split_fp16_speedup"] = round(res["unpaired_split_fp16"]["ms"] / res["paired_split_fp16"]["ms"], 2)
+        out[f"L{L}_K{K}_x{count}"] = res
+    return out
+
+
 def bench_served_conv(estl, torch, count=600):
     """Served FFT convolution: real signals of length log-uniform 2^8..2^20 with
     filters of length log-uniform 2^4..2^12, both N(0,1), seed 5, pinned host
@@ -332,17 +392,18 @@ def bench_served_conv(estl, torch, count=600):
 
     out = {"workload": f"{count} FFT-convolution requests, signal log-uniform 2^8..2^20, filter 2^4..2^12, "
                        "N(0,1) seed 5, pinned host buffers", "hbm_budget_gib": 64}
-    for name, kw, flags in (("batched", dict(max_inflight_batches=4, max_batch_requests=64), 0),
-                            ("batched_split_fp16", dict(max_inflight_batches=4, max_batch_requests=64),
-                             estl.PREC_SPLIT_FP16 << 8),
-                            ("per_request", dict(max_inflight_batches=1, max_batch_requests=1), 0)):
+    batched = dict(max_inflight_batches=4, max_batch_requests=64)
+    for name, kw, flags, poisson in (("batched", batched, 0, True),
+                                     ("batched_unpaired", batched, CONV_NO_PAIRING, False),
+                                     ("batched_split_fp16", batched, estl.PREC_SPLIT_FP16 << 8, True),
+                                     ("per_request", dict(max_inflight_batches=1, max_batch_requests=1), 0, True)):
         srv = Server(hbm_budget_bytes=64 << 30, **kw)
         run_flags[0] = flags
         try:
             run(srv, None)  # warm-up: plans, kernels, memory pool
             sat = run(srv, None)
             res = {"saturated": sat}
-            for frac in (0.5, 0.9):
+            for frac in ((0.5, 0.9) if poisson else ()):
                 res[f"poisson_{int(frac * 100)}pct"] = dict(run(srv, frac * sat["req_per_s"]),
                                                             rate=round(frac * sat["req_per_s"], 1))
             res["stats"] = {k: v for k, v in srv.stats().items() if k in ("batches", "max_batch_requests",
@@ -359,6 +420,8 @@ def bench_served_conv(estl, torch, count=600):
             out_split_err = max(errs)
     out["batched_vs_per_request"] = round(out["batched"]["saturated"]["req_per_s"] /
                                           out["per_request"]["saturated"]["req_per_s"], 2)
+    out["paired_vs_unpaired"] = round(out["batched"]["saturated"]["req_per_s"] /
+                                      out["batched_unpaired"]["saturated"]["req_per_s"], 2)
     out["batched_split_fp16_vs_per_request_fp32"] = round(out["batched_split_fp16"]["saturated"]["req_per_s"] /
                                                           out["per_request"]["saturated"]["req_per_s"], 2)
     out["batched_split_fp16"]["rel_l2_max_sampled"] = out_split_err
@@ -455,6 +518,67 @@ def bench_fft2d(estl, torch):
                                   "rel_l2_roundtrip": float(f"{rt:.3e}"), "kernels": d["kernels"]}
         f.close()
         b.close()
+    return out
+
+
+def fp64_conv2d(a, k, compat):
+    """numpy FP64 2D FFT convolution: the full linear convolution, or (compat)
+    the kernel-centred result divided by the kernel sum, cropped to the image."""
+    import numpy as np
+    h, w = a.shape
+    kh, kw = k.shape
+    H, W = 1 << max(1, (h + kh - 2).bit_length()), 1 << max(1, (w + kw - 2).bit_length())
+    full = np.fft.irfft2(np.fft.rfft2(a, (H, W)) * np.fft.rfft2(k, (H, W)), (H, W))
+    if not compat:
+        return full[:h + kh - 1, :w + kw - 1]
+    yo, xo = (kh + 1) // 2, (kw + 1) // 2
+    return full[yo:yo + h, xo:xo + w] / k.sum()
+
+
+def bench_conv2d(estl, torch):
+    """2D FFT convolution (Convolution2D_FFT, Convolution.h:95-148): a batch of
+    real images with one filter; the filter spectrum is set once, outside the
+    timed region; three launches per batch.  rel-L2 of the first image against
+    a numpy FP64 FFT convolution."""
+    import numpy as np
+    out = {"workload": "real FP32 images * one real filter, N(0,1) images, uniform(0.1,1) filters, seed 8",
+           "method": "CUDA events over 5 batches after 2 warm-up batches"}
+    st = torch.cuda.Stream()
+    for h, w, kh, kw, count, flags in ((2048, 2048, 31, 31, 8, 0), (1000, 1000, 15, 15, 64, estl.CONV_REFERENCE_COMPAT),
+                                       (512, 512, 64, 64, 64, 0)):
+        g = torch.Generator(device="cuda").manual_seed(8)
+        imgs = torch.randn((count, h, w), device="cuda", generator=g)
+        filt = torch.rand((kh, kw), device="cuda", generator=g) * 0.9 + 0.1
+        p = estl.Conv2DPlan(w, h, kw, kh, count, flags)
+        p.set_filter(filt, stream=st)
+        res = p.execute(imgs, stream=st)
+        for _ in range(2):
+            p.execute(imgs, out=res, stream=st)
+        st.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(5):
+            p.execute(imgs, out=res, stream=st)
+        e1.record(st)
+        st.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        ref = fp64_conv2d(imgs[0].cpu().numpy().astype(np.float64), filt.cpu().numpy().astype(np.float64),
+                          bool(flags & estl.CONV_REFERENCE_COMPAT))
+        err = float(np.sqrt(np.sum((res[0].cpu().numpy().astype(np.float64) - ref) ** 2) / np.sum(ref ** 2)))
+        pw = 1 << max(1, (w + kw - 2).bit_length())
+        ph = 1 << max(1, (h + kh - 2).bit_length())
+        # HBM bytes of the three launches: real rows in (4 B) + complex rows out (8 B) for the
+        # image rows, column pass read + write (8 + 8 B) of those rows, output rows read (8 B)
+        # and written (4 B per output pixel)
+        oh, ow = res.shape[1], res.shape[2]
+        moved = count * (4 * h * w + 8 * h * pw + 8 * h * pw + 8 * oh * pw + 8 * oh * pw + 4 * oh * ow)
+        out[f"{w}x{h}*{kw}x{kh}" + ("_compat" if flags else "")] = {
+            "count": count, "padded": f"{pw}x{ph}", "ms": round(ms, 3),
+            "images_per_s": round(count / (ms * 1e-3), 1),
+            "mpixel_per_s": round(count * h * w / (ms * 1e-3) / 1e6, 1),
+            "hbm_gbs_moved": round(moved / (ms * 1e-3) / 1e9, 1), "rel_l2": float(f"{err:.3e}"), "launches": 3}
+        p.close()
+        del imgs, res
     return out
 
 
@@ -694,8 +818,11 @@ def main():
     configs = {}
     if rank == 0 and not args.no_configs:
         for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
-                        ("split_precision", bench_split_precision), ("fft2d", bench_fft2d), ("bluestein", bench_bluestein),
+                        ("split_precision", bench_split_precision), ("fft2d", bench_fft2d), ("conv2d", bench_conv2d),
+                        ("conv_pairs", bench_conv_pairs), ("bluestein", bench_bluestein),
                         ("served_conv", bench_served_conv)):
+            if args.configs and key not in args.configs.split(","):
+                continue
             try:
                 configs[key] = fn(estl, torch)
             except Exception as ex:  # reported, never silently dropped

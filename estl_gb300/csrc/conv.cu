@@ -37,7 +37,9 @@ std::vector<ConvKernelDesc>& conv_table() {
     std::vector<ConvKernelDesc> v;
 #define ESTL_XC_SINGLE(M, E, R, C)                                          \
   v.push_back(cdesc<SpecSingleKernel<M, E, R, C>>(CK_SPEC_SINGLE, M, E, R, C)); \
-  v.push_back(cdesc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C));
+  v.push_back(cdesc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C)); \
+  v.push_back(cdesc<SpecPairKernel<M, E, R, C>>(CK_SPEC_PAIR, M, E, R, C));     \
+  v.push_back(cdesc<ConvPairKernel<M, E, R, C>>(CK_CONV_PAIR, M, E, R, C));
 #define ESTL_XC_COL(M, E, R, C)                                           \
   v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C)); \
   v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));
@@ -53,6 +55,10 @@ std::vector<ConvKernelDesc>& conv_table() {
         CK_SPEC_SINGLE, M, E, R, C, 1));                                                                    \
     v.push_back(cdesc<ConvSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(      \
         CK_CONV_SINGLE, M, E, R, C, 1));                                                                    \
+    v.push_back(cdesc<SpecPairKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(        \
+        CK_SPEC_PAIR, M, E, R, C, 1));                                                                      \
+    v.push_back(cdesc<ConvPairKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(        \
+        CK_CONV_PAIR, M, E, R, C, 1));                                                                      \
   }
 #define ESTL_XC_COL(M, E, R, C)                                                \
   v.push_back(cdesc<ConvColKernel<M, E, R, C, true>>(CK_COL_FILTER, M, E, R, C, 1)); \
@@ -112,7 +118,7 @@ estl_status launch_conv(const ConvLayout& L, const ConvBuffers& b, int which, cu
     if (l.grid < 1 || l.grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "convolution grid of %lld CTAs", l.grid);
     const long long N = 1LL << l.logn;
     ConvArgs a;
-    const bool filt = l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW;
+    const bool filt = ck_is_filter(l.kind);
     a.rows = Ptr<const ConvRow>{(filt ? b.filt_rows : b.sig_rows) + l.row_begin, l.row_count};
     a.nrows = l.row_count;
     a.sig = filt ? Ptr<const float>{b.filt, b.filt_elems} : Ptr<const float>{b.sig, b.sig_elems};
@@ -124,6 +130,7 @@ estl_status launch_conv(const ConvLayout& L, const ConvBuffers& b, int which, cu
     a.bank = Ptr<const cf32>{E.bank, kBankSize};
     a.logn = l.logn;
     a.split = l.tc ? L.split : SPLIT_NONE;
+    a.shared = L.shared;
     void* args[] = {&a};
     s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)l.grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                    "cudaLaunchKernel(conv)");

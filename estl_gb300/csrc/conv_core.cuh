@@ -48,7 +48,8 @@ struct ConvArgs {
   Ptr<cf32> s2;        // four-step scratch: N per row
   Ptr<const cf32> bank;
   int logn;
-  int split;  // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
+  int split;   // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
+  int shared;  // paired kernels: every request uses one filter spectrum H (not an A / B pair)
 };
 
 ESTL_HD cf32 cconj(cf32 v) { return {v.x, -v.y}; }
@@ -142,6 +143,143 @@ struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) {
     B::template run_mode<1>(a, cta, tid, sm);
   }
+};
+
+// ---------------------------------------------------------------------------
+// N <= 2^14, two real requests per complex transform (the real-input
+// specialisation).  Rows 2i and 2i+1 of a launch share one N-point complex
+// FFT: z = x1 + i x2, Z = FFT(z), and with Zm_k = Z_{(N-k) mod N}
+//   X1_k = (Z_k + conj(Zm_k)) / 2,      X2_k = (Z_k - conj(Zm_k)) / (2i).
+// Both outputs are real, so one inverse transform carries both:
+//   IFFT(X1 H1 + i X2 H2) = y1 + i y2,  X1 H1 + i X2 H2 = Z A + conj(Zm) B
+// with A = (H1 + H2) / 2, B = (H1 - H2) / 2.  The spectrum kernel builds A and
+// B the same way from one transform of h1 + i h2 and stores them in the two
+// rows' spectrum slots (scaled by 1/N, each H conjugated for correlation).
+// With one filter for every request (ArgS::shared) the spectrum is H itself
+// and Y = Z H.  An unpaired last row runs with x2 = 0 (its spectrum slot holds
+// A = B = H1 / 2).  Zm comes from one extra shared-memory exchange.
+// ---------------------------------------------------------------------------
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
+struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
+  using B = ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC>;
+  using TL = typename B::TL;
+  using Sidx = typename B::Sidx;
+  static constexpr int C = B::C;
+  // the mirror exchange needs the buffer even for single-pass tiles
+  static constexpr int EXCH = C * B::CS;
+  static constexpr int TC_OFF = (EXCH + 1) & ~1;
+  static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(B::NT / 32) + 1) / 2) : EXCH;
+
+  // 1 / (N * DC of the request's spectrum) for the reference normalisation
+  ESTL_HD static float dc_of(const ConvArgs& a, const ConvRow& r, float dc) {
+    return r.dc_norm ? 1.f / ((float)(1 << a.logn) * dc) : 1.f;
+  }
+
+  // MODE 0: convolution of rows (2i, 2i+1); MODE 1: spectra of filter rows (2i, 2i+1)
+  template <int MODE>
+  ESTL_HD static void run_mode(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const long long ri = 2 * (cta * C + c);
+    const bool valid = ri < a.nrows;
+    const bool has2 = ri + 1 < a.nrows;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, EXCH};
+    const Sidx sidx{};
+    if constexpr (TC) tc_init_atab(Ptr<uint32_t>{reinterpret_cast<uint32_t*>(smraw + TC_OFF), kTcAtabWords}, a.split, tid, B::NT);
+    ConvRow r1{}, r2{};
+    if (valid) r1 = a.rows[ri];
+    if (has2) r2 = a.rows[ri + 1];
+    cf32 v[TL::E];
+    {
+      const Ptr<const float> s1 = valid ? a.sig.sub(r1.sig_off, r1.sig_len) : Ptr<const float>{a.sig.p, 0};
+      const Ptr<const float> s2 = has2 ? a.sig.sub(r2.sig_off, r2.sig_len) : Ptr<const float>{a.sig.p, 0};
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) {
+        const int pos = t + TL::T * j;
+        v[j] = cf32{valid && pos < r1.sig_len ? s1[pos] : 0.f, has2 && pos < r2.sig_len ? s2[pos] : 0.f};
+      }
+    }
+    any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
+    const bool mirror = MODE == 1 || !a.shared;  // uniform over the launch
+    cf32 zm[TL::E];
+    if (mirror) {
+      ESTL_SYNC();  // the last pass's exchange reads are done
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+      ESTL_SYNC();
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) zm[j] = sm[sidx(c, (TL::M - (t + TL::T * j)) & (TL::M - 1))];
+      ESTL_SYNC();  // before the next passes reuse the exchange buffer
+    }
+    if constexpr (MODE == 1) {
+      if (valid) {
+        const Ptr<cf32> oa = a.spec_out.sub(r1.spec_off, TL::M);
+        const Ptr<cf32> ob = has2 ? a.spec_out.sub(r2.spec_off, TL::M) : Ptr<cf32>{a.spec_out.p, 0};
+        const float sc = 0.5f * r1.scale;
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) {
+          const int pos = t + TL::T * j;
+          // H1 = (Z + conj Zm) / 2, H2 = (Z - conj Zm) / (2i); each conjugated for correlation
+          const cf32 h1{0.5f * (v[j].x + zm[j].x), 0.5f * (v[j].y - zm[j].y) * r1.conj};
+          const cf32 h2{0.5f * (v[j].y + zm[j].y), -0.5f * (v[j].x - zm[j].x) * r1.conj};
+          oa[pos] = cf32{sc * (h1.x + h2.x), sc * (h1.y + h2.y)};
+          if (has2) ob[pos] = cf32{sc * (h1.x - h2.x), sc * (h1.y - h2.y)};
+        }
+      }
+    } else {
+      float g1 = 1.f, g2 = 1.f;
+      if (valid) {
+        const Ptr<const cf32> ha = a.spec.sub(r1.spec_off, TL::M);
+        if (a.shared) {
+#pragma unroll
+          for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(ha, t + TL::T * j)));
+          const float dc = ldg(a.spec, r1.spec_off).x;
+          g1 = dc_of(a, r1, dc);
+          g2 = dc_of(a, r2, dc);
+        } else {
+          const Ptr<const cf32> hb = has2 ? a.spec.sub(r2.spec_off, TL::M) : ha;
+#pragma unroll
+          for (int j = 0; j < TL::E; ++j) {
+            const int pos = t + TL::T * j;
+            const cf32 y = cadd(cmul(v[j], ldg(ha, pos)), cmul(cconj(zm[j]), ldg(hb, pos)));
+            v[j] = cconj(y);
+          }
+          const float a0 = ldg(a.spec, r1.spec_off).x, b0 = has2 ? ldg(a.spec, r2.spec_off).x : a0;
+          g1 = dc_of(a, r1, a0 + b0);
+          g2 = dc_of(a, r2, a0 - b0);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
+      }
+      any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
+      // FFT(conj(Y)) = N conj(y1 + i y2): y1 = re, y2 = -im
+      if (valid) {
+        const Ptr<float> o1 = a.out.sub(r1.out_off, r1.out_len);
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) {
+          const int m = t + TL::T * j - r1.out_shift;
+          if (m >= 0 && m < r1.out_len) o1[m] = v[j].x * g1;
+        }
+      }
+      if (has2) {
+        const Ptr<float> o2 = a.out.sub(r2.out_off, r2.out_len);
+#pragma unroll
+        for (int j = 0; j < TL::E; ++j) {
+          const int m = t + TL::T * j - r2.out_shift;
+          if (m >= 0 && m < r2.out_len) o2[m] = -v[j].y * g2;
+        }
+      }
+    }
+  }
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) { run_mode<0>(a, cta, tid, sm); }
+};
+
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
+struct SpecPairKernel : ConvPairKernel<LOGM, LOGE, LOGR, LOGC, TC> {
+  using P = ConvPairKernel<LOGM, LOGE, LOGR, LOGC, TC>;
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* sm) { P::template run_mode<1>(a, cta, tid, sm); }
 };
 
 // ---------------------------------------------------------------------------

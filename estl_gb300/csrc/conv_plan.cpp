@@ -114,8 +114,20 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       const int lc = single_logc(logn), le = std::min(4, logn);
       const long long grid = (cnt + (1LL << lc) - 1) >> lc;
       const long long fgrid = (fcnt + (1LL << lc) - 1) >> lc;
-      if (fcnt) L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, fgrid, logn, fb, fcnt, 0});
-      L.launches.push_back(ConvLaunch{CK_CONV_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
+      if (flags & CONV_NO_PAIRING) {
+        if (fcnt) L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, fgrid, logn, fb, fcnt, 0});
+        L.launches.push_back(ConvLaunch{CK_CONV_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
+      } else {
+        // two real requests per complex transform (rows 2i, 2i+1 of the bucket); one
+        // shared filter keeps its plain spectrum
+        const long long pgrid = ((cnt + 1) / 2 + (1LL << lc) - 1) >> lc;
+        const long long pfgrid = ((fcnt + 1) / 2 + (1LL << lc) - 1) >> lc;
+        if (fcnt && shared_filter)
+          L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, fgrid, logn, fb, fcnt, 0});
+        else if (fcnt)
+          L.launches.push_back(ConvLaunch{CK_SPEC_PAIR, logn, le, 4, lc, pfgrid, logn, fb, fcnt, 0});
+        L.launches.push_back(ConvLaunch{CK_CONV_PAIR, logn, le, 4, lc, pgrid, logn, rb, cnt, 0});
+      }
     } else {
       const int logn2 = logn / 2, logn1 = logn - logn2;
       const int cc = four_step_logc(logn2), cr = four_step_logc(logn1);
@@ -131,14 +143,15 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
     }
   }
   L.buckets = (int)buckets.size();
+  L.shared = shared_filter ? 1 : 0;
   L.split = conv_split(flags);
   // split precision: the tiles with radix-16 passes run their tensor-core variant
   for (ConvLaunch& l : L.launches) {
-    const bool single = l.kind == CK_SPEC_SINGLE || l.kind == CK_CONV_SINGLE;
+    const bool single = ck_is_single(l.kind);
     l.tc = (L.split != 0 && l.loge == 4 && l.logm >= 4 && (!single || l.logm <= kConvTcSingleMaxLog)) ? 1 : 0;
   }
   for (const ConvLaunch& l : L.launches)
-    L.is_spectrum_launch.push_back(l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW);
+    L.is_spectrum_launch.push_back(ck_is_filter(l.kind));
   L.spec_elems = spec;
   L.scratch_elems = scratch;
   size_t off = 0;

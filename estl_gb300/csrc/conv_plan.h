@@ -12,11 +12,11 @@
 
 namespace estl {
 
-enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2 };
+enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2, CONV_NO_PAIRING = 4 };
 // Bits 8-9 of the flags: the split precision of the FFT stages (SplitKind;
 // 0 = FP32), ESTL_CONV_PRECISION(p) in the C ABI.
 constexpr int kConvSplitShift = 8;
-constexpr int kConvFlagMask = CONV_CORRELATE | CONV_REFERENCE_COMPAT | (3 << kConvSplitShift);
+constexpr int kConvFlagMask = CONV_CORRELATE | CONV_REFERENCE_COMPAT | CONV_NO_PAIRING | (3 << kConvSplitShift);
 inline int conv_split(int flags) { return (flags >> kConvSplitShift) & 3; }
 
 // One convolution request: offsets (in floats) into the caller's packed
@@ -34,7 +34,18 @@ enum ConvLaunchKind {
   CK_COL_SIGNAL = 4,   // four-step column pass of the signals
   CK_MID = 5,          // row DFT, multiply, row DFT, twiddle
   CK_OUT = 6,          // column DFT -> real output
+  CK_SPEC_PAIR = 7,    // two filters per complex FFT -> the A / B spectra of a request pair, N <= 2^14
+  CK_CONV_PAIR = 8,    // two signals per complex FFT -> two outputs, N <= 2^14 (fused)
 };
+
+// launches that read the filter rows (and write spectra)
+inline bool ck_is_filter(int kind) {
+  return kind == CK_SPEC_SINGLE || kind == CK_COL_FILTER || kind == CK_SPEC_ROW || kind == CK_SPEC_PAIR;
+}
+// single-tile launches (N <= 2^14)
+inline bool ck_is_single(int kind) {
+  return kind == CK_SPEC_SINGLE || kind == CK_CONV_SINGLE || kind == CK_SPEC_PAIR || kind == CK_CONV_PAIR;
+}
 
 struct ConvLaunch {
   int kind;
@@ -59,6 +70,7 @@ struct ConvLayout {
   // a caller run the spectrum launches once and the convolution launches often
   std::vector<char> is_spectrum_launch;
   int split = 0;  // SplitKind of the tensor-core launches
+  int shared = 0;  // one filter for every request (ConvArgs::shared of the paired kernels)
 };
 
 constexpr int kConvMaxLogN = 22;

@@ -246,6 +246,12 @@ estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direction, const 
  * (:141-143), L samples kept (:146-148).  n may be at most 2^22. */
 #define ESTL_CONV_CORRELATE 1
 #define ESTL_CONV_REFERENCE_COMPAT 2
+/* Real-input specialisation (the default for padded lengths n <= 2^14): two
+ * requests of the same n share one complex transform (signals as real and
+ * imaginary parts; the two spectra separated with X_{n-k}), so a pair costs
+ * one forward and one inverse FFT.  This flag runs every request as its own
+ * complex transform instead. */
+#define ESTL_CONV_NO_PAIRING 4
 /* Split precision of the convolution's FFT stages (ESTL_PREC_SPLIT_*), or'd
  * into the flags; 0 = FP32. */
 #define ESTL_CONV_PRECISION(p) ((p) << 8)

@@ -241,7 +241,9 @@ const std::vector<EmuConvKernel>& emu_conv_kernels() {
     std::vector<EmuConvKernel> k;
 #define ESTL_XC_SINGLE(M, E, R, C)                                      \
   k.push_back(mkc<SpecSingleKernel<M, E, R, C>>(CK_SPEC_SINGLE, M, E, R, C)); \
-  k.push_back(mkc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C));
+  k.push_back(mkc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C)); \
+  k.push_back(mkc<SpecPairKernel<M, E, R, C>>(CK_SPEC_PAIR, M, E, R, C));     \
+  k.push_back(mkc<ConvPairKernel<M, E, R, C>>(CK_CONV_PAIR, M, E, R, C));
 #define ESTL_XC_COL(M, E, R, C)                                       \
   k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C)); \
   k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));
@@ -256,6 +258,10 @@ const std::vector<EmuConvKernel>& emu_conv_kernels() {
         CK_SPEC_SINGLE, M, E, R, C, 1));                                                                   \
     k.push_back(mkc<ConvSingleKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(         \
         CK_CONV_SINGLE, M, E, R, C, 1));                                                                   \
+    k.push_back(mkc<SpecPairKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(           \
+        CK_SPEC_PAIR, M, E, R, C, 1));                                                                     \
+    k.push_back(mkc<ConvPairKernel<M, E, R, C, (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog)>>(           \
+        CK_CONV_PAIR, M, E, R, C, 1));                                                                     \
   }
 #define ESTL_XC_COL(M, E, R, C)                                                 \
   k.push_back(mkc<ConvColKernel<M, E, R, C, true>>(CK_COL_FILTER, M, E, R, C, 1)); \
@@ -600,8 +606,9 @@ int emu_conv_run(const long long* reqs, int count, int flags, int shared, const 
       return 3;
     }
     const long long N = 1LL << l.logn;
-    const bool f = l.kind == CK_SPEC_SINGLE || l.kind == CK_COL_FILTER || l.kind == CK_SPEC_ROW;
-    if (l.s_off + l.row_count * N > (long long)s1.size() && (l.kind >= CK_COL_FILTER)) {
+    const bool f = ck_is_filter(l.kind);
+    const bool four = !ck_is_single(l.kind);
+    if (l.s_off + l.row_count * N > (long long)s1.size() && four) {
       set_err(err, errlen, "launch scratch range outside the scratch buffer");
       return 1;
     }
@@ -613,11 +620,12 @@ int emu_conv_run(const long long* reqs, int count, int flags, int shared, const 
     a.spec = Ptr<const cf32>{spec.data(), L.spec_elems};
     a.spec_out = Ptr<cf32>{spec.data(), L.spec_elems};
     a.out = Ptr<float>{out, L.out_elems};
-    a.s1 = Ptr<cf32>{s1.data() + (l.kind >= CK_COL_FILTER ? l.s_off : 0), l.kind >= CK_COL_FILTER ? l.row_count * N : 0};
-    a.s2 = Ptr<cf32>{s2.data() + (l.kind >= CK_COL_FILTER ? l.s_off : 0), l.kind >= CK_COL_FILTER ? l.row_count * N : 0};
+    a.s1 = Ptr<cf32>{s1.data() + (four ? l.s_off : 0), four ? l.row_count * N : 0};
+    a.s2 = Ptr<cf32>{s2.data() + (four ? l.s_off : 0), four ? l.row_count * N : 0};
     a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
     a.logn = l.logn;
     a.split = l.tc ? L.split : SPLIT_NONE;
+    a.shared = L.shared;
     if (!run_generic(k->nt, k->smem, k->fn, a, l.grid)) {
       std::lock_guard<std::mutex> g(g_msg_mu);
       set_err(err, errlen, g_msg);

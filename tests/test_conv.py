@@ -105,6 +105,58 @@ def test_emulated_shared_filter(emu):
         assert rel(out[i * (L + K - 1):(i + 1) * (L + K - 1)], ref) < TOL
 
 
+NO_PAIRING = 4
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_emulated_pairs_odd_buckets(emu, flags):
+    """Two real requests per complex transform (the default for n <= 2^14):
+    buckets of one, two, three and five requests of different lengths (odd
+    buckets leave an unpaired last request), every flag combination, paired
+    and unpaired (ESTL_CONV_NO_PAIRING), against the oracle."""
+    shapes = [(700, 90), (1000, 20), (600, 300), (900, 60), (1020, 5),  # n = 1024: five requests
+              (3000, 1000), (2500, 1597),                                # n = 4096: two
+              (9000, 700), (12000, 300), (8500, 2),                      # n = 16384: three
+              (40, 9)]                                                   # n = 64: one
+    reqs, sig, filt, _ = make_requests(shapes, 21)
+    compat = bool(flags & 2)
+    if compat:
+        filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L if compat else L + K - 1
+    outs = [emu_conv(emu, creqs, sig, filt, oo, flags=flags | extra) for extra in (0, NO_PAIRING)]
+    for L, K, so, fo, o in creqs:
+        s, f = sig[so:so + L], filt[fo:fo + K]
+        if compat:
+            ref = compat_reference(s, f)
+            if flags & 1:
+                full = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=True)
+                sh = (K + 1) // 2
+                ref = full[sh: sh + L] / np.sum(f.astype(np.float64))
+        else:
+            ref = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1))
+        n_out = L if compat else L + K - 1
+        for out in outs:
+            assert rel(out[o:o + n_out], ref) < TOL, (flags, L, K)
+
+
+def test_emulated_pairs_shared_filter(emu):
+    """One filter for every request (the convolution plan): pairs multiply by
+    the plain spectrum H; odd and even counts."""
+    for n in (6, 7):
+        L, K = 5000, 77
+        rng = np.random.default_rng(n)
+        sig = rng.standard_normal(L * n).astype(np.float32)
+        filt = rng.standard_normal(K).astype(np.float32)
+        reqs = [(L, K, i * L, 0, i * (L + K - 1)) for i in range(n)]
+        out = emu_conv(emu, reqs, sig, filt, n * (L + K - 1), shared=True)
+        for i in range(n):
+            ref = oracle.conv_fft(sig[i * L:(i + 1) * L].astype(np.float64), filt.astype(np.float64))
+            assert rel(out[i * (L + K - 1):(i + 1) * (L + K - 1)], ref) < TOL
+
+
 SPLIT_TOL = {1: TOL, 2: 2e-5, 3: TOL}
 
 
@@ -210,3 +262,18 @@ def test_gpu_split_precision(engine, split):
     for L, K, so, fo, oo in reqs:
         ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
         assert rel(out[oo:oo + L + K - 1], ref) < SPLIT_TOL[split], (split, L, K)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flags", [0, NO_PAIRING, 1 << 8, (1 << 8) | NO_PAIRING, 3 << 8])
+def test_gpu_pairs(engine, flags):
+    """Paired (default) and unpaired single-tile convolutions, FP32 and split
+    precision, odd buckets, against the oracle."""
+    shapes = [(700, 90), (1000, 20), (600, 300), (900, 60), (1020, 5), (3000, 1000), (2500, 1597),
+              (9000, 700), (12000, 300), (8500, 2), (40, 9)] * 3
+    reqs, sig, filt, olen = make_requests(shapes, 22)
+    out = gpu_conv_batch(engine, reqs, sig, filt, olen, flags=flags)
+    tol = SPLIT_TOL.get(flags >> 8, TOL)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < tol, (flags, L, K)
