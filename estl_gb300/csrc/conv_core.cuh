@@ -20,6 +20,10 @@
 #pragma once
 #include "fft_core.cuh"
 
+#if !defined(__CUDA_ARCH__)
+#include <cmath>
+#endif
+
 namespace estl {
 
 // One request (or one filter) inside a launch.  Offsets are element offsets
@@ -148,17 +152,92 @@ struct SpecSingleKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
 // ---------------------------------------------------------------------------
 // N <= 2^14, two real requests per complex transform (the real-input
 // specialisation).  Rows 2i and 2i+1 of a launch share one N-point complex
-// FFT: z = x1 + i x2, Z = FFT(z), and with Zm_k = Z_{(N-k) mod N}
-//   X1_k = (Z_k + conj(Zm_k)) / 2,      X2_k = (Z_k - conj(Zm_k)) / (2i).
+// FFT: z = x1 + i s x2, Z = FFT(z), and with Zm_k = Z_{(N-k) mod N}
+//   X1_k = (Z_k + conj(Zm_k)) / 2,      s X2_k = (Z_k - conj(Zm_k)) / (2i).
 // Both outputs are real, so one inverse transform carries both:
-//   IFFT(X1 H1 + i X2 H2) = y1 + i y2,  X1 H1 + i X2 H2 = Z A + conj(Zm) B
-// with A = (H1 + H2) / 2, B = (H1 - H2) / 2.  The spectrum kernel builds A and
-// B the same way from one transform of h1 + i h2 and stores them in the two
-// rows' spectrum slots (scaled by 1/N, each H conjugated for correlation).
-// With one filter for every request (ArgS::shared) the spectrum is H itself
-// and Y = Z H.  An unpaired last row runs with x2 = 0 (its spectrum slot holds
-// A = B = H1 / 2).  Zm comes from one extra shared-memory exchange.
+//   IFFT(X1 H1 + i s X2 H2) = y1 + i s y2.
+// FP32 rounding in both transforms is relative to the larger of the two
+// halves, so the halves are balanced with exact powers of two: s = 2^k from
+// the two signals' energies (k = half the difference of their binary
+// exponents), and each filter spectrum is stored normalised, H / 2^e with
+// 2^(2e) ~ sum h^2; e is kept in Im H_0, which is zero for a real filter.
+// The spectrum kernel makes both normalised spectra from one transform of
+// h1 2^-e1 + i h2 2^-e2 (scaled by 1/N, conjugated for correlation) and stores
+// them in the two rows' spectrum slots.  With one filter for every request
+// (ConvArgs::shared) the spectrum is the plain H of SpecSingleKernel and
+// Y = Z H.  An unpaired last row runs with x2 = 0.  Zm comes from one extra
+// shared-memory exchange; the energies from a row reduction.
 // ---------------------------------------------------------------------------
+
+// Sums of (x, y) over the T consecutive threads of each row of the CTA; every
+// thread gets its row's sums.  buf: shared scratch of 2 * NT floats (free).
+template <int T, int NT>
+ESTL_HD void row_sum2(float& x, float& y, int tid, float* buf) {
+#if defined(__CUDA_ARCH__)
+  constexpr int W = T < 32 ? T : 32;
+#pragma unroll
+  for (int o = 1; o < W; o <<= 1) {
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+    y += __shfl_xor_sync(0xffffffffu, y, o);
+  }
+  if constexpr (T > 32) {
+    const int warp = tid >> 5;
+    if ((tid & 31) == 0) {
+      buf[2 * warp] = x;
+      buf[2 * warp + 1] = y;
+    }
+    __syncthreads();
+    const int w0 = (tid / T) * (T / 32);
+    x = 0.f;
+    y = 0.f;
+    for (int w = 0; w < T / 32; ++w) {
+      x += buf[2 * (w0 + w)];
+      y += buf[2 * (w0 + w) + 1];
+    }
+    __syncthreads();
+  }
+#else
+  buf[2 * tid] = x;
+  buf[2 * tid + 1] = y;
+  ESTL_SYNC();
+  const int r0 = (tid / T) * T;
+  x = 0.f;
+  y = 0.f;
+  for (int i = 0; i < T; ++i) {
+    x += buf[2 * (r0 + i)];
+    y += buf[2 * (r0 + i) + 1];
+  }
+  ESTL_SYNC();
+#endif
+}
+
+ESTL_HD int ilogb_f(float v) {
+#if defined(__CUDA_ARCH__)
+  return ilogbf(v);
+#else
+  return std::ilogb(v);
+#endif
+}
+ESTL_HD float pow2_f(int k) {
+#if defined(__CUDA_ARCH__)
+  return ldexpf(1.f, k);
+#else
+  return std::ldexp(1.f, k);
+#endif
+}
+// k with 2^k ~ sqrt(e1 / e2) (0 when either energy is zero), |k| <= 60
+ESTL_HD int balance_exp(float e1, float e2) {
+  if (!(e1 > 0.f) || !(e2 > 0.f)) return 0;
+  int k = (ilogb_f(e1) - ilogb_f(e2)) / 2;
+  return k > 60 ? 60 : (k < -60 ? -60 : k);
+}
+// e with 2^(2e) ~ energy (0 for a zero filter), |e| <= 60
+ESTL_HD int norm_exp(float energy) {
+  if (!(energy > 0.f)) return 0;
+  int e = ilogb_f(energy) / 2;
+  return e > 60 ? 60 : (e < -60 ? -60 : e);
+}
+
 template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
 struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
   using B = ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC>;
@@ -169,11 +248,9 @@ struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
   static constexpr int EXCH = C * B::CS;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(B::NT / 32) + 1) / 2) : EXCH;
-
-  // 1 / (N * DC of the request's spectrum) for the reference normalisation
-  ESTL_HD static float dc_of(const ConvArgs& a, const ConvRow& r, float dc) {
-    return r.dc_norm ? 1.f / ((float)(1 << a.logn) * dc) : 1.f;
-  }
+  static_assert(EXCH >= B::NT, "row reduction scratch");
+  // the mirror values double the live registers: allow 128 per thread
+  static constexpr int MINB = B::NT <= 128 ? 4 : (B::NT <= 256 ? 2 : 1);
 
   // MODE 0: convolution of rows (2i, 2i+1); MODE 1: spectra of filter rows (2i, 2i+1)
   template <int MODE>
@@ -191,6 +268,7 @@ struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
     if (valid) r1 = a.rows[ri];
     if (has2) r2 = a.rows[ri + 1];
     cf32 v[TL::E];
+    float e1 = 0.f, e2 = 0.f;
     {
       const Ptr<const float> s1 = valid ? a.sig.sub(r1.sig_off, r1.sig_len) : Ptr<const float>{a.sig.p, 0};
       const Ptr<const float> s2 = has2 ? a.sig.sub(r2.sig_off, r2.sig_len) : Ptr<const float>{a.sig.p, 0};
@@ -198,7 +276,18 @@ struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
       for (int j = 0; j < TL::E; ++j) {
         const int pos = t + TL::T * j;
         v[j] = cf32{valid && pos < r1.sig_len ? s1[pos] : 0.f, has2 && pos < r2.sig_len ? s2[pos] : 0.f};
+        e1 += v[j].x * v[j].x;
+        e2 += v[j].y * v[j].y;
       }
+    }
+    row_sum2<TL::T, B::NT>(e1, e2, tid, reinterpret_cast<float*>(smraw));
+    // MODE 0: x2 scaled by 2^k to the energy of x1; MODE 1: each filter normalised
+    const int k = MODE == 0 ? balance_exp(e1, e2) : 0;
+    const int f1 = MODE == 1 ? norm_exp(e1) : 0, f2 = MODE == 1 ? norm_exp(e2) : 0;
+    {
+      const float g1 = MODE == 1 ? pow2_f(-f1) : 1.f, g2 = MODE == 1 ? pow2_f(-f2) : pow2_f(k);
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) v[j] = cf32{v[j].x * g1, v[j].y * g2};
     }
     any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
     const bool mirror = MODE == 1 || !a.shared;  // uniform over the launch
@@ -220,41 +309,51 @@ struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) {
           const int pos = t + TL::T * j;
-          // H1 = (Z + conj Zm) / 2, H2 = (Z - conj Zm) / (2i); each conjugated for correlation
-          const cf32 h1{0.5f * (v[j].x + zm[j].x), 0.5f * (v[j].y - zm[j].y) * r1.conj};
-          const cf32 h2{0.5f * (v[j].y + zm[j].y), -0.5f * (v[j].x - zm[j].x) * r1.conj};
-          oa[pos] = cf32{sc * (h1.x + h2.x), sc * (h1.y + h2.y)};
-          if (has2) ob[pos] = cf32{sc * (h1.x - h2.x), sc * (h1.y - h2.y)};
+          // H1 = (Z + conj Zm) / 2, H2 = (Z - conj Zm) / (2i), each conjugated for correlation;
+          // Im H_0 carries the normalisation exponent
+          oa[pos] = cf32{sc * (v[j].x + zm[j].x), pos ? sc * (v[j].y - zm[j].y) * r1.conj : (float)f1};
+          if (has2) ob[pos] = cf32{sc * (v[j].y + zm[j].y), pos ? -sc * (v[j].x - zm[j].x) * r1.conj : (float)f2};
         }
       }
     } else {
       float g1 = 1.f, g2 = 1.f;
       if (valid) {
-        const Ptr<const cf32> ha = a.spec.sub(r1.spec_off, TL::M);
+        const Ptr<const cf32> h1 = a.spec.sub(r1.spec_off, TL::M);
+        const float N = (float)(1 << a.logn);
         if (a.shared) {
+          // one plain spectrum: Y = Z H, y2 carries 2^k
 #pragma unroll
-          for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(ha, t + TL::T * j)));
-          const float dc = ldg(a.spec, r1.spec_off).x;
-          g1 = dc_of(a, r1, dc);
-          g2 = dc_of(a, r2, dc);
+          for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h1, t + TL::T * j)));
+          const float dc = ldg(h1, 0).x;
+          g1 = r1.dc_norm ? 1.f / (N * dc) : 1.f;
+          g2 = (r2.dc_norm ? 1.f / (N * dc) : 1.f) * pow2_f(-k);
         } else {
-          const Ptr<const cf32> hb = has2 ? a.spec.sub(r2.spec_off, TL::M) : ha;
+          const Ptr<const cf32> h2 = has2 ? a.spec.sub(r2.spec_off, TL::M) : h1;
+          const cf32 d1 = ldg(h1, 0), d2 = ldg(h2, 0);  // (DC / 2^e, e)
 #pragma unroll
           for (int j = 0; j < TL::E; ++j) {
             const int pos = t + TL::T * j;
-            const cf32 y = cadd(cmul(v[j], ldg(ha, pos)), cmul(cconj(zm[j]), ldg(hb, pos)));
+            cf32 a1 = ldg(h1, pos), a2 = ldg(h2, pos);
+            if (pos == 0) {
+              a1.y = 0.f;
+              a2.y = 0.f;
+            }
+            const cf32 x1{0.5f * (v[j].x + zm[j].x), 0.5f * (v[j].y - zm[j].y)};
+            const cf32 x2{0.5f * (v[j].y + zm[j].y), -0.5f * (v[j].x - zm[j].x)};  // s X2
+            const cf32 q = cmul(x2, a2);
+            const cf32 y = cadd(cmul(x1, a1), cf32{-q.y, q.x});  // X1 H1 + i s X2 H2
             v[j] = cconj(y);
           }
-          const float a0 = ldg(a.spec, r1.spec_off).x, b0 = has2 ? ldg(a.spec, r2.spec_off).x : a0;
-          g1 = dc_of(a, r1, a0 + b0);
-          g2 = dc_of(a, r2, a0 - b0);
+          // the reference DC normalisation cancels the stored 2^-e
+          g1 = r1.dc_norm ? 1.f / (N * d1.x) : pow2_f((int)d1.y);
+          g2 = (r2.dc_norm ? 1.f / (N * d2.x) : pow2_f((int)d2.y)) * pow2_f(-k);
         }
       } else {
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) v[j] = cf32{0.f, 0.f};
       }
       any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
-      // FFT(conj(Y)) = N conj(y1 + i y2): y1 = re, y2 = -im
+      // FFT(conj(Y)) = conj(y1 + i s y2): y1 = re, s y2 = -im
       if (valid) {
         const Ptr<float> o1 = a.out.sub(r1.out_off, r1.out_len);
 #pragma unroll
