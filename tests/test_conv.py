@@ -142,6 +142,24 @@ def test_emulated_pairs_odd_buckets(emu, flags):
             assert rel(out[o:o + n_out], ref) < TOL, (flags, L, K)
 
 
+def test_emulated_pairs_disparate_magnitudes(emu):
+    """Paired requests whose outputs differ by many orders of magnitude (a
+    2-tap filter beside a 700-tap one, signals scaled by 1e4 and 1e-3,
+    filters by 1e-3 and 1e2): the power-of-two balancing keeps every request
+    at the FP32 tolerance of its own magnitude."""
+    shapes = [(8500, 2), (9000, 700), (8000, 300), (3000, 5), (3000, 1000)]
+    reqs, sig, filt, olen = make_requests(shapes, 31)
+    scale_s = [1e4, 1.0, 1e-3, 1.0, 1e3]
+    scale_f = [1.0, 1e-3, 1.0, 1e2, 1.0]
+    for (L, K, so, fo, _), a, b in zip(reqs, scale_s, scale_f):
+        sig[so:so + L] *= np.float32(a)
+        filt[fo:fo + K] *= np.float32(b)
+    out = emu_conv(emu, reqs, sig, filt, olen)
+    for L, K, so, fo, oo in reqs:
+        ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
+        assert rel(out[oo:oo + L + K - 1], ref) < TOL, (L, K)
+
+
 def test_emulated_pairs_shared_filter(emu):
     """One filter for every request (the convolution plan): pairs multiply by
     the plain spectrum H; odd and even counts."""
@@ -272,6 +290,9 @@ def test_gpu_pairs(engine, flags):
     shapes = [(700, 90), (1000, 20), (600, 300), (900, 60), (1020, 5), (3000, 1000), (2500, 1597),
               (9000, 700), (12000, 300), (8500, 2), (40, 9)] * 3
     reqs, sig, filt, olen = make_requests(shapes, 22)
+    for i, (L, K, so, fo, _) in enumerate(reqs):  # magnitudes over eight decades
+        sig[so:so + L] *= np.float32(10.0 ** ((i % 5) - 2))
+        filt[fo:fo + K] *= np.float32(10.0 ** (2 - (i % 4)))
     out = gpu_conv_batch(engine, reqs, sig, filt, olen, flags=flags)
     tol = SPLIT_TOL.get(flags >> 8, TOL)
     for L, K, so, fo, oo in reqs:
