@@ -87,6 +87,7 @@ SIGNATURES = {
     "estl_conv2d_plan_execute": (_INT, [_P, _P, _P, _P]),
     "estl_conv2d_plan_launches": (_I64, [_P]),
     "estl_conv2d_plan_destroy": (_INT, [_P]),
+    "estl_conv2d_host": (_INT, [_I64, _I64, _I64, _I64, _INT, _P, _P, _P]),
     "estl_packed_plan_create": (_INT, [_P, _P, _I64, _INT, _INT, ctypes.POINTER(_P)]),
     "estl_packed_execute": (_INT, [_P, _P, _P, _P]),
     "estl_packed_check": (_INT, [_P]),

@@ -4,6 +4,7 @@
 #include <climits>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "conv2d_core.cuh"
@@ -190,6 +191,36 @@ estl_status estl_conv2d_plan_execute(estl_conv2d_plan p, const float* d_images, 
   a.mode = 1;
   s = conv2d_launch(p->row, a, st);
   if (s != ESTL_OK) return s;
+  return ok();
+}
+
+// One image, host buffers, blocking: the call Convolution2D_FFT::convolve
+// makes (Convolution.h:95-148), for the C++ plugin Convolution2D_FFT_CUDA.
+estl_status estl_conv2d_host(int64_t width, int64_t height, int64_t kwidth, int64_t kheight, int flags,
+                             const float* h_image, const float* h_kernel, float* h_out) {
+  if (!h_image || !h_kernel || !h_out) return fail(ESTL_INVALID_ARG, "estl_conv2d_host: null argument");
+  estl_conv2d_plan p = nullptr;
+  estl_status s = estl_conv2d_plan_create(width, height, kwidth, kheight, 1, flags, &p);
+  if (s != ESTL_OK) return s;
+  const size_t in_b = (size_t)(width * height) * sizeof(float), k_b = (size_t)(kwidth * kheight) * sizeof(float);
+  const size_t out_b = (size_t)p->g.out_w * (size_t)p->g.out_h * sizeof(float);
+  float *d_in = nullptr, *d_k = nullptr, *d_out = nullptr;
+  s = dev_alloc((void**)&d_in, in_b, "2D convolution image");
+  if (s == ESTL_OK) s = dev_alloc((void**)&d_k, k_b, "2D convolution filter");
+  if (s == ESTL_OK) s = dev_alloc((void**)&d_out, out_b, "2D convolution output");
+  if (s == ESTL_OK) s = check_cuda(cudaMemcpy(d_in, h_image, in_b, cudaMemcpyHostToDevice), "cudaMemcpy(image)");
+  if (s == ESTL_OK) s = check_cuda(cudaMemcpy(d_k, h_kernel, k_b, cudaMemcpyHostToDevice), "cudaMemcpy(filter)");
+  if (s == ESTL_OK) s = estl_conv2d_plan_set_filter(p, d_k, nullptr);
+  if (s == ESTL_OK) s = estl_conv2d_plan_execute(p, d_in, d_out, nullptr);
+  if (s == ESTL_OK) s = check_cuda(cudaMemcpy(h_out, d_out, out_b, cudaMemcpyDeviceToHost), "cudaMemcpy(output)");
+  const estl_status keep = s;
+  const std::string msg = keep == ESTL_OK ? std::string() : std::string(estl_last_error());
+  cudaDeviceSynchronize();
+  if (d_in) dev_free(d_in, in_b);
+  if (d_k) dev_free(d_k, k_b);
+  if (d_out) dev_free(d_out, out_b);
+  estl_conv2d_plan_destroy(p);
+  if (keep != ESTL_OK) return fail(keep, "%s", msg.c_str());
   return ok();
 }
 

@@ -312,6 +312,12 @@ estl_status estl_conv2d_plan_create(int64_t width, int64_t height, int64_t kwidt
 estl_status estl_conv2d_plan_set_filter(estl_conv2d_plan plan, const float* d_filter, void* stream);
 estl_status estl_conv2d_plan_execute(estl_conv2d_plan plan, const float* d_images, float* d_out, void* stream);
 int64_t estl_conv2d_plan_launches(estl_conv2d_plan plan);
+/* One image, host buffers, blocking (the call Convolution2D_FFT::convolve
+ * makes): h_image height x width floats, h_kernel kheight x kwidth floats,
+ * h_out estl_conv2d_output_size floats.  Device buffers are allocated and
+ * freed inside the call. */
+estl_status estl_conv2d_host(int64_t width, int64_t height, int64_t kwidth, int64_t kheight, int flags,
+                             const float* h_image, const float* h_kernel, float* h_out);
 estl_status estl_conv2d_plan_destroy(estl_conv2d_plan plan);
 
 /* ---- Uneven batches: packed transforms of mixed lengths ----
