@@ -54,13 +54,15 @@ def parse():
 
 def compact_choice(c):
     """Short text form of an autotuner plan choice."""
+    def r32(key):
+        return " radix-32" if c.get(key, -1) == 5 else ""
     if c["mode"] == 1:
-        return f"single {c['single_loge']}.{c['single_logc']}"
+        return f"single {c['single_loge']}.{c['single_logc']}{r32('single_logr')}"
     if c["mode"] == 4:
         return f"three-pass R 2^{c['logn2']} Q 2^{c.get('logn3', -1)} chunk {c['chunk']} pipe {c['pipe']}"
     kind = "stream" if c["mode"] == 3 else "four-step"
-    return (f"{kind} col {c['logn2']}.{c['col_loge']}.{c['col_logc']} row {c['row_loge']}.{c['row_logc']} "
-            f"chunk {c['chunk']} lag {c['lag']} pipe {c['pipe']}")
+    return (f"{kind} col {c['logn2']}.{c['col_loge']}.{c['col_logc']}{r32('col_logr')} "
+            f"row {c['row_loge']}.{c['row_logc']}{r32('row_logr')} chunk {c['chunk']} lag {c['lag']} pipe {c['pipe']}")
 
 
 def dist_env():

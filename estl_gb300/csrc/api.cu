@@ -603,6 +603,9 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
       choice.row_logc = opt->row_logc;
       choice.pipe = opt->pipelined < 0 ? 0 : opt->pipelined;
       choice.logn3 = opt->split2_log2;
+      choice.single_logr = opt->single_logr;
+      choice.col_logr = opt->col_logr;
+      choice.row_logr = opt->row_logr;
     }
   } else {
     if (precision == ESTL_PREC_FP32) tuner_lookup(n, batch, &choice);

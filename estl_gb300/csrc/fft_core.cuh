@@ -217,6 +217,48 @@ struct DFT<16> {
   }
 };
 
+// w32^k = exp(-2 pi i k / 32) = cos(pi k / 16) - i sin(pi k / 16), k = 1..7
+constexpr float kC32_1 = 0.98078528040323044913f;  // cos(pi/16)
+constexpr float kS32_1 = 0.19509032201612826785f;  // sin(pi/16)
+constexpr float kC32_3 = 0.83146961230254523708f;  // cos(3 pi/16)
+constexpr float kS32_3 = 0.55557023301960222474f;  // sin(3 pi/16)
+
+template <>
+struct DFT<32> {
+  // decimation in time: E = DFT16(x[2m]), O = DFT16(x[2m+1]),
+  // X[k] = E[k] + w32^k O[k], X[k+16] = E[k] - w32^k O[k].
+  ESTL_HD static void run(cf32* x) {
+    cf32 e[16], o[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      e[m] = x[2 * m];
+      o[m] = x[2 * m + 1];
+    }
+    DFT<16>::run(e);
+    DFT<16>::run(o);
+    o[1] = cmulc(o[1], kC32_1, -kS32_1);
+    o[2] = cmulc(o[2], kC16, -kS16);
+    o[3] = cmulc(o[3], kC32_3, -kS32_3);
+    o[4] = mul_w8_1(o[4]);
+    o[5] = cmulc(o[5], kS32_3, -kC32_3);
+    o[6] = cmulc(o[6], kS16, -kC16);
+    o[7] = cmulc(o[7], kS32_1, -kC32_1);
+    o[8] = mul_mi(o[8]);
+    o[9] = cmulc(o[9], -kS32_1, -kC32_1);
+    o[10] = cmulc(o[10], -kS16, -kC16);
+    o[11] = cmulc(o[11], -kS32_3, -kC32_3);
+    o[12] = mul_w8_3(o[12]);
+    o[13] = cmulc(o[13], -kC32_3, -kS32_3);
+    o[14] = cmulc(o[14], -kC16, -kS16);
+    o[15] = cmulc(o[15], -kC32_1, -kS32_1);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      x[k] = cadd(e[k], o[k]);
+      x[k + 16] = csub(e[k], o[k]);
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Twiddle bank: one device table holding w_{2^k}^j for every k <= kBankLog
 // at index 2^k + j, followed by 4096-entry "low" tables for 2^(kBankLog+1)..2^kMaxLog
@@ -283,6 +325,13 @@ ESTL_HD void twiddle_apply(cf32* x, const Ptr<const cf32>& tw, int u) {
     x[7] = cmul(x[7], cmul(w3, w4));
   } else if constexpr (R == 16) {
     apply_powers16(x, ldg(tw, u), ldg(tw, 2 * u), ldg(tw, 4 * u), ldg(tw, 8 * u));
+  } else if constexpr (R == 32) {
+    const cf32 w1 = ldg(tw, u), w2 = ldg(tw, 2 * u), w4 = ldg(tw, 4 * u), w8 = ldg(tw, 8 * u), w16 = ldg(tw, 16 * u);
+    // x_r *= w^r: r < 16 directly, r >= 16 as w^16 * w^(r - 16)
+#pragma unroll
+    for (int r = 16; r < 32; ++r) x[r] = cmul(x[r], w16);
+    apply_powers16(x, w1, w2, w4, w8);
+    apply_powers16(x + 16, w1, w2, w4, w8);
   }
 }
 

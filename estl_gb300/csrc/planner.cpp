@@ -110,6 +110,9 @@ static const TileCfg* find_tc(int kind, int logm, int logc) {
   return nullptr;
 }
 
+// Radix of a tile choice: -1 = radix 16.
+static int lr_of(int logr) { return logr < 0 ? 4 : logr; }
+
 // Whether a step of this configuration runs as its pipelined variant.
 static int use_pipe(const PlanChoice& ch, const TileCfg* c) {
   if (ch.pipe == 0) return 0;
@@ -231,12 +234,13 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     static const int col_c[10] = {0, 0, 0, 0, 0, 0, 0, 5, 4, 3}, row_c[10] = {0, 0, 0, 0, 0, 0, 0, 4, 3, 2};
     auto col_for = [&](int m) -> const TileCfg* {
       if (choice.col_loge >= 0)
-        if (const TileCfg* c = find_tile(STEP_COL, m, choice.col_loge, 4, choice.col_logc)) return c;
+        if (const TileCfg* c = find_tile(STEP_COL, m, choice.col_loge, lr_of(choice.col_logr), choice.col_logc)) return c;
       return find_tile(STEP_COL, m, 4, 4, col_c[m]);
     };
     const TileCfg* ca = col_for(lr);
     const TileCfg* cb = col_for(lq);
-    const TileCfg* r = choice.row_loge >= 0 ? find_tile(STEP_ROW, lp, choice.row_loge, 4, choice.row_logc) : nullptr;
+    const TileCfg* r =
+        choice.row_loge >= 0 ? find_tile(STEP_ROW, lp, choice.row_loge, lr_of(choice.row_logr), choice.row_logc) : nullptr;
     if (!r) r = find_tile(STEP_ROW, lp, 4, 4, row_c[lp]);
     if (!ca || !cb || !r || cb->logc > lp || ca->logc > lq + lp || r->logc > lr + lq) {
       set_err(err, "no three-pass tiles instantiated for log2 N = %lld with first column DFTs of 2^%lld", logn, lr);
@@ -279,7 +283,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     if (tc)
       c = find_tc(STEP_SINGLE, logn, choice.single_logc);
     else if (choice.single_loge >= 0)
-      c = find_tile(STEP_SINGLE, logn, choice.single_loge, 4, choice.single_logc);
+      c = find_tile(STEP_SINGLE, logn, choice.single_loge, lr_of(choice.single_logr), choice.single_logc);
     else
       c = default_single(logn);
     if (!c) {
@@ -321,11 +325,11 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     row = find_tile(STEP_ROW, logn1, td[4], 4, td[5]);
   } else {
     if (choice.col_loge >= 0)
-      col = find_tile(STEP_COL, logn2, choice.col_loge, 4, choice.col_logc);
+      col = find_tile(STEP_COL, logn2, choice.col_loge, lr_of(choice.col_logr), choice.col_logc);
     else
       col = default_pass(STEP_COL, logn2, logn1, logn1);
     if (choice.row_loge >= 0)
-      row = find_tile(STEP_ROW, logn1, choice.row_loge, 4, choice.row_logc);
+      row = find_tile(STEP_ROW, logn1, choice.row_loge, lr_of(choice.row_logr), choice.row_logc);
     else
       row = default_pass(STEP_ROW, (int)logn1, std::min((int)logn2, logn1 <= 9 ? 3 : 2), (int)logn2);
   }
@@ -448,6 +452,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       PlanChoice ch;
       ch.mode = 1;
       ch.single_loge = c.loge;
+      ch.single_logr = c.logr;
       ch.single_logc = c.logc;
       ch.pipe = c.pipe;
       out.push_back(ch);
@@ -488,8 +493,10 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
             ch.mode = 2;
             ch.logn2 = logn2;
             ch.col_loge = c.loge;
+            ch.col_logr = c.logr;
             ch.col_logc = c.logc;
             ch.row_loge = r.loge;
+            ch.row_logr = r.logr;
             ch.row_logc = r.logc;
             ch.chunk = chunk == 0 ? 0 : std::max(1LL, chunk / n);
             ch.pipe = pipe;

@@ -78,6 +78,9 @@ struct PlanChoice {
   int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
   int pipe = 0;         // tile kernels: 0 plain, 1 pipelined variant (where one exists), -1 pipelined if any
   int split = 0;        // 0 FP32; else the SplitKind of tensor-core radix-16 passes (tc_core.cuh)
+  // log2 of the largest radix of the single / column / row tiles (-1 = 4:
+  // radix 16; 5: radix-32 passes, 32 elements per thread)
+  int single_logr = -1, col_logr = -1, row_logr = -1;
 };
 
 struct Plan1D {

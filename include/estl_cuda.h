@@ -102,7 +102,8 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
  * cp.async double-buffered variant where one exists, 2 for the persistent
  * bulk-load variants (row tiles by bulk copies, column tiles by 2D tensor
  * copies).  Mode 4 reads split_log2 as log2 R and split2_log2 as log2 Q
- * (0 or -1 = default).  A zero-initialised struct with mode = 0 is the
+ * (0 or -1 = default).  *_logr: log2 of the largest radix of the tile
+ * (-1 or 4: radix 16; 5: radix-32 passes with 32 elements per thread).  A zero-initialised struct with mode = 0 is the
  * automatic plan. */
 typedef struct estl_plan_options {
   int mode;
@@ -115,6 +116,7 @@ typedef struct estl_plan_options {
   int row_loge, row_logc;
   int pipelined;
   int split2_log2;
+  int single_logr, col_logr, row_logr;
 } estl_plan_options;
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,

@@ -321,6 +321,9 @@ PlanChoice choice_from(const int* f) {
   c.pipe = f[10];
   c.split = f[11];
   c.logn3 = f[12];
+  c.single_logr = f[13];
+  c.col_logr = f[14];
+  c.row_logr = f[15];
   return c;
 }
 
@@ -362,7 +365,7 @@ const EmuC2Kernel* emu_c2_pick(int col, int logm, int logw) {
 extern "C" {
 
 // Runs the plan for (n, batch) on interleaved complex64 host data.
-// choice: 13 ints (PlanChoice fields) or NULL for the planner default.
+// choice: 16 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
 static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen);
@@ -549,13 +552,13 @@ int emu_plan_describe(long long n, long long batch, const int* choice, char* buf
 }
 
 // Candidate choices of the autotuner for (n, batch): writes up to max rows
-// of 13 ints, returns the number of candidates.
+// of 16 ints, returns the number of candidates.
 int emu_plan_candidates(long long n, long long batch, int* out, int max) {
   std::vector<PlanChoice> c = plan_candidates(n, batch);
   int k = 0;
   for (const PlanChoice& ch : c) {
     if (k >= max) break;
-    int* f = out + 13 * k++;
+    int* f = out + 16 * k++;
     f[0] = ch.mode;
     f[1] = ch.single_loge;
     f[2] = ch.single_logc;
@@ -569,6 +572,9 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[10] = ch.pipe;
     f[11] = ch.split;
     f[12] = ch.logn3;
+    f[13] = ch.single_logr;
+    f[14] = ch.col_logr;
+    f[15] = ch.row_logr;
   }
   return (int)c.size();
 }

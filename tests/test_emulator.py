@@ -26,10 +26,13 @@ def pad_choice(choice):
     """PlanChoice fields: mode, single_loge, single_logc, logn2, col_loge,
     col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available),
     split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes),
-    logn3 (three-pass: log2 of the second column DFT length, 0 = default)."""
+    logn3 (three-pass: log2 of the second column DFT length, 0 = default),
+    single_logr, col_logr, row_logr (log2 largest radix, -1 = 16)."""
     c = list(choice)
     if len(c) < 13:
         c += [0] * (13 - len(c))
+    if len(c) < 16:
+        c += [-1] * (16 - len(c))
     return c
 
 
@@ -38,20 +41,20 @@ def emu_run(emu, n, batch, x, sign=-1, choice=None):
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 13)(*pad_choice(choice))
+        ch = (ctypes.c_int * 16)(*pad_choice(choice))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (13 * 4096))()
+    buf = (ctypes.c_int * (16 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[13 * i: 13 * i + 13]) for i in range(min(k, 4096))]
+    return [list(buf[16 * i: 16 * i + 16]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 13)(*pad_choice(choice)) if choice is not None else None
+    ch = (ctypes.c_int * 16)(*pad_choice(choice)) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())

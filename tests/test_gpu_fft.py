@@ -242,3 +242,37 @@ def test_three_pass(engine, logn, lr, lq, pipe):
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("logn", range(9, 15))
+def test_radix32_single_tiles(engine, logn):
+    """Single-tile kernels with radix-32 passes (32 elements per thread)
+    against the oracle, both directions."""
+    import torch
+    n = 1 << logn
+    logc = {9: 4, 10: 3, 11: 2, 12: 1, 13: 0, 14: 0}[logn]
+    x = uniform_c64((max(3, (1 << 20) // n), n), 1100 + logn)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, x.shape[0], direction, mode="single",
+                        tiles={"single_loge": 5, "single_logc": logc, "single_logr": 5})
+        y = p.execute(xd).cpu().numpy()
+        assert oracle.rel_l2(y, oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("logn,split,col,row,pipe", [(18, 9, (5, 3), (5, 3), 0), (19, 9, (5, 4), (5, 2), 2),
+                                                     (19, 10, (5, 3), (5, 3), 2), (20, 10, (5, 2), (5, 2), 2),
+                                                     (20, 10, (5, 3), (5, 2), 0), (21, 10, (5, 3), (4, 2), 2)])
+def test_radix32_four_step_tiles(engine, logn, split, col, row, pipe):
+    """Four-step column / row tiles with radix-32 passes, plain and bulk-load."""
+    import torch
+    n = 1 << logn
+    x = uniform_c64((2, n), 1200 + logn)
+    xd = torch.from_numpy(x).cuda()
+    tiles = {"split_log2": split, "col_loge": col[0], "col_logc": col[1], "col_logr": 5,
+             "row_loge": row[0], "row_logc": row[1], "row_logr": 5 if row[0] == 5 else -1, "pipelined": pipe}
+    for direction in (-1, +1):
+        p = engine.Plan(n, 2, direction, mode="four_step", tiles=tiles)
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
