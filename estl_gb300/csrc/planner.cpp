@@ -303,12 +303,13 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
 
   // four-step.  Defaults: the autotuner's winners on a GB300 for 1 GiB
   // batches, log2 N -> (log2 N2, column log2 E / log2 C, row log2 E / log2 C,
-  // pipelined: 2 = the bulk-load variants where they exist); other lengths
-  // split N2 = 2^floor(log2 N / 2).
-  static const int tuned4[][7] = {{15, 7, 4, 5, 4, 3, 0},  {16, 7, 4, 5, 4, 2, 2},  {17, 8, 4, 4, 4, 2, 2},
-                                  {18, 9, 4, 3, 4, 2, 2},  {19, 10, 4, 3, 4, 2, 2}, {20, 10, 4, 2, 4, 2, 2},
-                                  {21, 10, 4, 3, 4, 2, 2}, {22, 11, 4, 2, 4, 2, 2}, {23, 11, 4, 2, 4, 2, 2},
-                                  {24, 12, 5, 2, 5, 2, 0}};
+  // pipelined: 2 = the bulk-load variants where they exist, column / row log2
+  // radix); other lengths split N2 = 2^floor(log2 N / 2).
+  static const int tuned4[][9] = {
+      {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 2, 2, 4, 4},  {17, 8, 4, 4, 4, 2, 2, 4, 4},
+      {18, 9, 5, 4, 5, 3, 2, 5, 5},  {19, 9, 5, 3, 4, 2, 2, 5, 4},  {20, 10, 5, 3, 5, 3, 2, 5, 5},
+      {21, 10, 5, 3, 4, 2, 2, 5, 4}, {22, 11, 4, 2, 4, 2, 2, 4, 4}, {23, 11, 4, 2, 4, 2, 2, 4, 4},
+      {24, 12, 5, 2, 5, 2, 0, 4, 4}};
   const int* td = nullptr;
   if (!tc && choice.logn2 < 0 && choice.col_loge < 0 && choice.row_loge < 0)
     for (const auto& t : tuned4)
@@ -321,8 +322,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     col = find_tc(STEP_COL, logn2, choice.col_logc);
     row = find_tc(STEP_ROW, logn1, choice.row_logc);
   } else if (td) {
-    col = find_tile(STEP_COL, logn2, td[2], 4, td[3]);
-    row = find_tile(STEP_ROW, logn1, td[4], 4, td[5]);
+    col = find_tile(STEP_COL, logn2, td[2], td[7], td[3]);
+    row = find_tile(STEP_ROW, logn1, td[4], td[8], td[5]);
   } else {
     if (choice.col_loge >= 0)
       col = find_tile(STEP_COL, logn2, choice.col_loge, lr_of(choice.col_logr), choice.col_logc);
