@@ -45,11 +45,12 @@ std::vector<TileCfg> build_configs() {
 // DFTs; column tiles as wide as 512 threads allow; row tiles of 8 rows
 // (N1 <= 2^9) or 4 rows (larger); chunks of 2^27 elements (1 GiB scratch).
 const TileCfg* default_single(int logm) {
-  // autotuner winners on a GB300 (1 GiB batches): log2 M -> (log2 E, log2 C)
-  static const int tuned[][3] = {{10, 4, 1}, {11, 4, 0}, {12, 5, 0}, {13, 5, 0}, {14, 5, 0}};
+  // autotuner winners on a GB300 (1 GiB batches): log2 M -> (log2 E, log2 C,
+  // log2 radix); 2^13 and 2^14 run radix-32 passes (three instead of four)
+  static const int tuned[][4] = {{10, 4, 1, 4}, {11, 4, 0, 4}, {12, 5, 0, 4}, {13, 5, 0, 5}, {14, 5, 0, 5}};
   for (const auto& t : tuned)
     if (t[0] == logm)
-      if (const TileCfg* c = find_tile(STEP_SINGLE, logm, t[1], 4, t[2])) return c;
+      if (const TileCfg* c = find_tile(STEP_SINGLE, logm, t[1], t[3], t[2])) return c;
   const TileCfg* best = nullptr;
   const int want_e = logm >= 13 ? 5 : std::min(4, logm);
   for (const TileCfg& c : tile_configs()) {
@@ -306,7 +307,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   // pipelined: 2 = the bulk-load variants where they exist, column / row log2
   // radix); other lengths split N2 = 2^floor(log2 N / 2).
   static const int tuned4[][9] = {
-      {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 2, 2, 4, 4},  {17, 8, 4, 4, 4, 2, 2, 4, 4},
+      {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 2, 2, 4, 4},  {17, 8, 4, 4, 4, 3, 2, 4, 4},
       {18, 9, 5, 4, 5, 3, 2, 5, 5},  {19, 9, 5, 3, 4, 2, 2, 5, 4},  {20, 10, 5, 3, 5, 3, 2, 5, 5},
       {21, 10, 5, 3, 4, 2, 2, 5, 4}, {22, 11, 4, 2, 4, 2, 2, 4, 4}, {23, 11, 4, 2, 4, 2, 2, 4, 4},
       {24, 12, 5, 2, 5, 2, 0, 4, 4}};
