@@ -165,6 +165,21 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
               st.logm, st.loge, st.logc);
 }
 
+estl_status launch_pdl(const void* fn, long long grid, int threads, void** args, int smem, cudaStream_t stream,
+                       const char* what) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return check_cuda(cudaLaunchKernelExC(&cfg, fn, args), what);
+}
+
 // cuTensorMapEncodeTiled from the driver, through the runtime (no -lcuda).
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -249,8 +264,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
       if (s != ESTL_OK) return s;
     }
     void* args[] = {&a, &map};
-    s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
-                   "cudaLaunchKernel");
+    s = launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx");
     if (s != ESTL_OK) return s;
   }
   return ESTL_OK;

@@ -13,6 +13,7 @@ namespace estl {
 template <class K>
 __global__ void __launch_bounds__(K::NT, K::MINB) conv_kernel(ConvArgs a) {
   extern __shared__ float2 estl_conv_smem[];
+  pdl_enter();
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_conv_smem));
 }
 
@@ -132,8 +133,7 @@ estl_status launch_conv(const ConvLayout& L, const ConvBuffers& b, int which, cu
     a.split = l.tc ? L.split : SPLIT_NONE;
     a.shared = L.shared;
     void* args[] = {&a};
-    s = check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)l.grid), dim3(d->nthreads), args, d->smem_bytes, stream),
-                   "cudaLaunchKernel(conv)");
+    s = launch_pdl(d->fn, l.grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx(conv)");
     if (s != ESTL_OK) return s;
   }
   return ESTL_OK;

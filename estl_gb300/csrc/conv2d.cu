@@ -15,6 +15,7 @@ namespace estl {
 template <class K>
 __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) conv2d_kernel(Conv2dArgs a) {
   extern __shared__ float2 estl_conv2d_smem[];
+  pdl_enter();
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_conv2d_smem));
 }
 
@@ -81,8 +82,7 @@ estl_status conv2d_launch(const Conv2dKernelDesc* d, const Conv2dArgs& a, cudaSt
   if (grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "2D convolution grid of %lld CTAs", grid);
   Conv2dArgs b = a;
   void* args[] = {&b};
-  return check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
-                    "cudaLaunchKernel(conv2d)");
+  return launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx(conv2d)");
 }
 
 }  // namespace

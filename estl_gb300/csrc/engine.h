@@ -40,6 +40,12 @@ estl_status ok();
 estl_status check_cuda(cudaError_t e, const char* what);
 estl_status require_init();
 
+// Kernel launch with programmatic stream serialisation: the kernel (which
+// starts with pdl_enter) may be scheduled while the previous kernel of the
+// stream finishes its last wave.
+estl_status launch_pdl(const void* fn, long long grid, int threads, void** args, int smem, cudaStream_t stream,
+                       const char* what);
+
 // Budgeted device allocation (counted against Engine::budget).
 estl_status dev_alloc(void** p, size_t bytes, const char* what);
 void dev_free(void* p, size_t bytes);

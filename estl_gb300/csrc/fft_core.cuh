@@ -442,6 +442,19 @@ ESTL_CX int min_blocks(int nt, int e) {
   return nt * e >= 16384 ? 1 : (16384 / (nt * e) < 2048 / nt ? 16384 / (nt * e) : 2048 / nt);
 }
 
+// Programmatic dependent launch (kernels launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization): wait until the
+// previous kernel of the stream has completed and its writes are visible,
+// then let the next kernel's CTAs be scheduled as soon as every CTA of this
+// grid has started, so that its launch and prologue overlap this grid's last
+// wave.  Without the launch attribute both instructions do nothing.
+ESTL_HD void pdl_enter() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+#endif
+}
+
 // Keeps the compiler from hoisting every iteration's table loads to the top
 // of an unrolled epilogue (which costs 2 registers per load in flight).
 ESTL_HD void schedule_fence() {
