@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <unordered_map>
@@ -167,6 +168,14 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
 
 estl_status launch_pdl(const void* fn, long long grid, int threads, void** args, int smem, cudaStream_t stream,
                        const char* what) {
+  // ESTL_NO_PDL=1 launches with plain stream serialisation
+  static const bool pdl = [] {
+    const char* e = std::getenv("ESTL_NO_PDL");
+    return !(e && *e && *e != '0');
+  }();
+  if (!pdl)
+    return check_cuda(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)threads), args, (size_t)smem, stream),
+                      what);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)threads);
