@@ -149,6 +149,7 @@ struct BulkRowKernel {
   static constexpr int MIN_BLOCKS =
       SMEM_BLOCKS < 1 ? 1 : (SMEM_BLOCKS < min_blocks(NT, TL::E) ? SMEM_BLOCKS : min_blocks(NT, TL::E));
   static_assert(TL::M % 2 == 0, "rows of an even number of elements (16-byte copies)");
+  static constexpr bool PERSISTENT = true;
 
   ESTL_HD static long long ntiles(const TileArgs& a) { return a.rows << (a.logn - LOGM - LOGC); }
 
@@ -183,6 +184,7 @@ struct BulkRowKernel {
     ESTL_SYNC();
     long long k = 0;
     for (long long tile = cta; tile < nt; tile += grid, ++k) {
+      if (tile + grid >= nt) pdl_trigger();  // last tile: let the next kernel's CTAs in as this one drains
       const int s = (int)(k & 1);
       const Ptr<cf32> stage{smraw + s * STAGE, STAGE};
       if (cta_any(!mbar_wait(&bar[s], (uint32_t)((k >> 1) & 1)))) {
@@ -251,6 +253,7 @@ struct BulkColKernel {
   static constexpr int MIN_BLOCKS =
       SMEM_BLOCKS < 1 ? 1 : (SMEM_BLOCKS < min_blocks(NT, TL::E) ? SMEM_BLOCKS : min_blocks(NT, TL::E));
   static_assert((BH * C * 8) % 128 == 0, "boxes keep the 128-byte alignment of the stage");
+  static constexpr bool PERSISTENT = true;
 
   ESTL_HD static long long ntiles(const TileArgs& a) { return a.rows << (a.logn - LOGM - LOGC); }
 
@@ -306,6 +309,7 @@ struct BulkColKernel {
     ESTL_SYNC();
     long long k = 0;
     for (long long tile = cta; tile < nt; tile += grid, ++k) {
+      if (tile + grid >= nt) pdl_trigger();  // last tile: let the next kernel's CTAs in as this one drains
       const int s = (int)(k & 1);
       const Ptr<cf32> stage{base + s * STAGE, STAGE};
       if (cta_any(!mbar_wait(&bar[s], (uint32_t)((k >> 1) & 1)))) {

@@ -448,12 +448,31 @@ ESTL_CX int min_blocks(int nt, int e) {
 // then let the next kernel's CTAs be scheduled as soon as every CTA of this
 // grid has started, so that its launch and prologue overlap this grid's last
 // wave.  Without the launch attribute both instructions do nothing.
-ESTL_HD void pdl_enter() {
+ESTL_HD void pdl_wait() {
 #if defined(__CUDA_ARCH__)
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
+#endif
+}
+ESTL_HD void pdl_trigger() {
+#if defined(__CUDA_ARCH__)
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 #endif
 }
+ESTL_HD void pdl_enter() {
+  pdl_wait();
+  pdl_trigger();
+}
+
+// Kernels whose CTAs are all resident from the start (persistent tile loops)
+// trigger their dependents when a CTA has issued its last tile instead.
+template <class K, class = void>
+struct is_persistent {
+  static constexpr bool value = false;
+};
+template <class K>
+struct is_persistent<K, decltype((void)K::PERSISTENT)> {
+  static constexpr bool value = K::PERSISTENT;
+};
 
 // Keeps the compiler from hoisting every iteration's table loads to the top
 // of an unrolled epilogue (which costs 2 registers per load in flight).

@@ -27,7 +27,8 @@ struct KernelDesc {
 template <class K>
 __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tile_kernel(TileArgs a) {
   extern __shared__ float2 estl_smem[];
-  pdl_enter();
+  pdl_wait();
+  if constexpr (!is_persistent<K>::value) pdl_trigger();
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
 }
 
@@ -36,7 +37,8 @@ __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tile_kernel(TileArgs a) 
 template <class K>
 __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tma_tile_kernel(TileArgs a, const __grid_constant__ CUtensorMap map) {
   extern __shared__ float2 estl_smem[];
-  pdl_enter();
+  pdl_wait();
+  if constexpr (!is_persistent<K>::value) pdl_trigger();
   a.tmap = &map;
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_smem));
 }
