@@ -401,10 +401,12 @@ struct Tile {
     return ((b - k) << LR) + k + (r << LNS);
   }
 
-  // Shared-memory row padding: one spare slot per 16 elements keeps the
-  // scattered pass stores free of bank conflicts.
-  ESTL_CX static int pad(int m) { return m + (m >> 4); }
-  static constexpr int MP = M + (M >> 4);
+  // Shared-memory row padding: one spare slot per R elements keeps the
+  // scattered radix-R pass stores (a half-warp writing slots R apart) free of
+  // bank conflicts: 16 for radix-16 tiles, 32 for radix-32 tiles.
+  static constexpr int PADSH = (LOGR >= 5 && LOGM >= 5) ? 5 : 4;
+  ESTL_CX static int pad(int m) { return m + (m >> PADSH); }
+  static constexpr int MP = M + (M >> PADSH);
 };
 
 // Stride (in complex elements) between the shared-memory rows of a tile of
