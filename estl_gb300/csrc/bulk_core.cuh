@@ -139,8 +139,10 @@ struct BulkRowKernel {
   using Base = RowKernel<LOGM, LOGE, LOGR, LOGC>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static_assert(C >= 2 && C <= 8, "landing rows 16-byte aligned and conflict-free for 2 <= C <= 8");
-  static constexpr int RS = TL::M + 16 / C;  // landing row stride (elements, even)
+  static_assert(C >= 1 && C <= 8, "landing rows 16-byte aligned and conflict-free for 1 <= C <= 8");
+  // landing row stride (elements, even); one row per tile (a whole transform,
+  // N2 = 1: the single-tile case) needs no padding
+  static constexpr int RS = C == 1 ? TL::M : TL::M + 16 / C;
   static constexpr int EXCH = TL::MP * C;    // exchange layout of RowKernel (pad(m) * C + c)
   static constexpr int STAGE = ((EXCH > C * RS ? EXCH : C * RS) + 1) & ~1;
   static constexpr int SMEM_ELEMS = 2 * STAGE + 2;  // two stages, then two 8-byte mbarriers
@@ -192,8 +194,11 @@ struct BulkRowKernel {
         return;
       }
       cf32 v[TL::E];
+      // a four-step row pass reads the column pass's (already conjugated)
+      // scratch; a whole transform per tile (N2 = 1) reads the plan's input
+      const float lsgn = logn2 == 0 ? a.sgn : 1.f;
 #pragma unroll
-      for (int j = 0; j < TL::E; ++j) v[j] = stage[c * RS + t + TL::T * j];
+      for (int j = 0; j < TL::E; ++j) v[j] = conj_if(stage[c * RS + t + TL::T * j], lsgn);
       ESTL_SYNC();  // the stage becomes the exchange buffer
       run_passes<TL, 0>(v, t, c, stage, tw, typename Base::Sidx{});
       ESTL_SYNC();  // every exchange read of this stage is done

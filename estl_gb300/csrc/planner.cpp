@@ -291,6 +291,16 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
       set_err(err, "no single-kernel tile instantiated for log2 n = %lld", logn);
       return false;
     }
+    // pipelined = 2 with one transform per tile: the persistent bulk-load row
+    // tile with N2 = 1 (one row = one whole transform)
+    if (!tc && choice.pipe == 2 && c->logc == 0 && find_tile(STEP_ROW, logn, c->loge, c->logr, 0, 2)) {
+      Step s{STEP_ROW, logn, c->loge, c->logr, 0, batch, BUF_IN, BUF_OUT, 0, total, 0, total, batch, logn};
+      s.pipe = 2;
+      p.steps.push_back(s);
+      p.hbm_passes = 1;
+      *out = p;
+      return true;
+    }
     const long long per = 1LL << c->logc;
     Step s{STEP_SINGLE, c->logm, c->loge, c->logr, c->logc, (batch + per - 1) / per, BUF_IN, BUF_OUT,
            0, total, 0, total, batch, logn};
@@ -458,6 +468,10 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
       ch.single_logc = c.logc;
       ch.pipe = c.pipe;
       out.push_back(ch);
+      if (!c.pipe && c.logc == 0 && find_tile(STEP_ROW, logn, c.loge, c.logr, 0, 2)) {
+        ch.pipe = 2;  // the same tile with bulk loads (persistent row tile, N2 = 1)
+        out.push_back(ch);
+      }
     }
   }
   if (find_stream_cfg(logn)) {

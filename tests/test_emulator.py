@@ -209,3 +209,19 @@ def test_three_pass(emu, logn, lr, lq, pipe):
         rc, msg, y = emu_run(emu, n, 1, x, sign, choice)
         assert rc == 0, msg
         assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < 2 * logn * 2.0 ** -24
+
+
+@pytest.mark.parametrize("logn,loge,logr", [(12, 5, 4), (13, 5, 4), (13, 5, 5)])
+def test_bulk_single_tiles(emu, logn, loge, logr):
+    """Single-tile sizes on the persistent bulk-load row tile with one whole
+    transform per tile (pipelined = 2, N2 = 1), two CTAs looping over five
+    transforms through both stages."""
+    n = 1 << logn
+    choice = [1, loge, 0, -1, -1, -1, -1, -1, 0, 0, 2, 0, 0, logr, -1, -1]
+    d = describe(emu, n, 5, choice)
+    assert d["kernels"][0]["kind"] == "row" and d["kernels"][0]["pipe"] == 2 and d["hbm_passes"] == 1
+    x = rand_c64((5, n), 70 + logn)
+    for sign in (-1, +1):
+        rc, msg, y = emu_run(emu, n, 5, x, sign, choice)
+        assert rc == 0, msg
+        assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL

@@ -276,3 +276,21 @@ def test_radix32_four_step_tiles(engine, logn, split, col, row, pipe):
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("logn,logr", [(12, 4), (13, 4), (13, 5)])
+def test_bulk_single_tiles(engine, logn, logr):
+    """Single-tile sizes on the persistent bulk-load row tile (one whole
+    transform per tile), both directions, against the oracle."""
+    import torch
+    n = 1 << logn
+    x = uniform_c64(((1 << 22) // n, n), 1300 + logn)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, x.shape[0], direction, mode="single",
+                        tiles={"single_loge": 5, "single_logc": 0, "single_logr": logr, "pipelined": 2})
+        d = p.describe()
+        assert d["kernels"][0]["kind"] == "row" and d["kernels"][0]["pipe"] == 2
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
