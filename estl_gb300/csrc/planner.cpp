@@ -317,8 +317,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   // pipelined: 2 = the bulk-load variants where they exist, column / row log2
   // radix); other lengths split N2 = 2^floor(log2 N / 2).
   static const int tuned4[][9] = {
-      {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 2, 2, 4, 4},  {17, 8, 4, 4, 4, 3, 2, 4, 4},
-      {18, 9, 5, 4, 5, 3, 2, 5, 5},  {19, 9, 5, 3, 4, 2, 2, 5, 4},  {20, 10, 5, 3, 5, 3, 2, 5, 5},
+      {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 3, 2, 4, 4},  {17, 7, 4, 5, 5, 3, 2, 4, 5},
+      {18, 9, 4, 3, 4, 3, 2, 4, 4},  {19, 9, 5, 4, 5, 3, 2, 5, 5},  {20, 10, 5, 3, 5, 3, 2, 5, 5},
       {21, 10, 5, 3, 4, 2, 2, 5, 4}, {22, 11, 4, 2, 4, 2, 2, 4, 4}, {23, 11, 4, 2, 4, 2, 2, 4, 4},
       {24, 12, 5, 2, 5, 2, 0, 4, 4}};
   const int* td = nullptr;
