@@ -310,6 +310,15 @@ struct estl_plan_s {
   void* host_aux[2] = {nullptr, nullptr};  // streamed plans: work lists of the chunk plans
   size_t host_aux_bytes[2] = {0, 0};
   StreamAux host_saux[2] = {};
+  // the smaller chunks that open and close a host pipeline (estl_execute_host):
+  // chunk transforms -> plan (and its streamed work list)
+  struct RampChunk {
+    Plan1D lay;
+    void* aux = nullptr;
+    size_t aux_bytes = 0;
+    StreamAux saux{};
+  };
+  std::unordered_map<long long, RampChunk> ramp;
   // other host layouts (estl_execute_layout / estl_execute_host_layout):
   // interleaved staging of the device path, raw-layout staging of the host path
   cf32* lay_in = nullptr;
@@ -345,6 +354,7 @@ static void plan_release(estl_plan p) {
   dev_free(p->scratch, p->scratch_bytes);
   dev_free(p->aux, p->aux_bytes);
   for (int s = 0; s < 2; ++s) dev_free(p->host_aux[s], p->host_aux_bytes[s]);
+  for (auto& kv : p->ramp) dev_free(kv.second.aux, kv.second.aux_bytes);
   dev_free(p->blue_chirp, p->blue_chirp_bytes);
   dev_free(p->blue_spec, p->blue_spec_bytes);
   dev_free(p->blue_a, p->blue_work_bytes);
@@ -729,7 +739,8 @@ estl_status estl_plan_check(estl_plan plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
   estl_status s = check_cuda(cudaDeviceSynchronize(), "plan execute");
   if (s != ESTL_OK) return s;
-  const StreamAux* auxes[3] = {&plan->saux, &plan->host_saux[0], &plan->host_saux[1]};
+  std::vector<const StreamAux*> auxes = {&plan->saux, &plan->host_saux[0], &plan->host_saux[1]};
+  for (const auto& kv : plan->ramp) auxes.push_back(&kv.second.saux);
   for (const StreamAux* a : auxes) {
     if (!a->error) continue;
     int e = 0;
@@ -954,6 +965,50 @@ static estl_status host_pipeline_setup(estl_plan p) {
   return ESTL_OK;
 }
 
+// The plan of a ramp chunk of `cnt` transforms (made on first use).
+static estl_status ramp_chunk(estl_plan p, long long cnt, const Plan1D** lay, const StreamAux** aux) {
+  auto it = p->ramp.find(cnt);
+  if (it == p->ramp.end()) {
+    estl_plan_s::RampChunk rc;
+    std::string err;
+    if (!make_plan_like(p->layout, cnt, &rc.lay, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+    rc.aux_bytes = stream_aux_bytes(rc.lay);
+    if (rc.aux_bytes) {
+      estl_status s = dev_alloc(&rc.aux, rc.aux_bytes, "stream work list");
+      if (s == ESTL_OK) s = stream_prepare(rc.lay, rc.aux, rc.aux_bytes, &rc.saux);
+      if (s != ESTL_OK) {
+        dev_free(rc.aux, rc.aux_bytes);
+        return s;
+      }
+    }
+    it = p->ramp.emplace(cnt, rc).first;
+  }
+  *lay = &it->second.lay;
+  *aux = &it->second.saux;
+  return ESTL_OK;
+}
+
+// Chunk sizes (transforms) of one host pipeline run: full chunks, opened by
+// chunks of 1/8, 1/4 and 1/2 and closed the same way in reverse, so that the
+// first copy-in and the last copy-out (which overlap nothing) are short.
+static std::vector<long long> host_schedule(long long batch, long long chunk) {
+  std::vector<long long> ramp;
+  for (long long d : {8LL, 4LL, 2LL})
+    if (chunk / d >= 1 && (ramp.empty() || chunk / d != ramp.back())) ramp.push_back(chunk / d);
+  std::vector<long long> out;
+  long long sum_ramp = 0;
+  for (long long r : ramp) sum_ramp += r;
+  if (batch < 4 * chunk || ramp.empty()) {  // too short for a steady state: equal chunks
+    for (long long b0 = 0; b0 < batch; b0 += chunk) out.push_back(std::min(chunk, batch - b0));
+    return out;
+  }
+  for (long long r : ramp) out.push_back(r);
+  long long mid = batch - 2 * sum_ramp;
+  for (; mid > 0; mid -= chunk) out.push_back(std::min(chunk, mid));
+  for (auto it = ramp.rbegin(); it != ramp.rend(); ++it) out.push_back(*it);
+  return out;
+}
+
 estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
   if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
   estl_status s = require_init();
@@ -963,14 +1018,25 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
   s = host_pipeline_setup(plan);
   if (s != ESTL_OK) return s;
   const long long n = plan->layout.n, batch = plan->layout.batch, chunk = plan->host_chunk;
-  const long long nchunks = (batch + chunk - 1) / chunk;
+  const std::vector<long long> sched = host_schedule(batch, chunk);
+  const long long nchunks = (long long)sched.size();
   cudaStream_t sh = plan->st[0], sc = plan->st[1], sd = plan->st[2];
-  for (long long i = 0; i < nchunks; ++i) {
+  long long b0 = 0;
+  for (long long i = 0; i < nchunks; b0 += sched[(size_t)i], ++i) {
     const int k = (int)(i & 1);
-    const long long b0 = i * chunk, cnt = std::min(chunk, batch - b0);
+    const long long cnt = sched[(size_t)i];
     const size_t bytes = (size_t)(cnt * n) * sizeof(cf32);
-    const Plan1D& lay = cnt == chunk ? plan->host_plan_full : plan->host_plan_tail;
-    const StreamAux* aux = cnt == chunk ? &plan->host_saux[0] : &plan->host_saux[1];
+    const Plan1D* layp = &plan->host_plan_full;
+    const StreamAux* aux = &plan->host_saux[0];
+    if (cnt != chunk) {
+      if (cnt == batch % chunk) {
+        layp = &plan->host_plan_tail;
+        aux = &plan->host_saux[1];
+      } else if ((s = ramp_chunk(plan, cnt, &layp, &aux)) != ESTL_OK) {
+        return s;
+      }
+    }
+    const Plan1D& lay = *layp;
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sh, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaMemcpyAsync(plan->din[k], h_in + 2 * b0 * n, bytes, cudaMemcpyHostToDevice, sh),
                         "cudaMemcpyAsync(H2D)")) != ESTL_OK)

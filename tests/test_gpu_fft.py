@@ -294,3 +294,22 @@ def test_bulk_single_tiles(engine, logn, logr):
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+@pytest.mark.parametrize("n,batch", [(4096, 4 * 2048 + 5), (1 << 18, 4 * 32 + 7), (1 << 13, 4 * 1024)])
+def test_execute_host_ramped_chunks(engine, n, batch):
+    """Host pipelines long enough for the opening and closing ramp of smaller
+    chunks (1/8, 1/4, 1/2 of the 64 MiB chunk): bit-identical to the device
+    execute, forward and backward."""
+    import torch
+    rng = np.random.default_rng(n + batch)
+    x = rng.standard_normal((batch, n, 2), dtype=np.float32).view(np.complex64)[..., 0]
+    xh = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    xd = xh.cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, batch, direction)
+        yd = p.execute(xd).cpu()
+        p.execute_host(xh.numpy(), yh.numpy())
+        assert torch.equal(yh, yd)
+        p.close()
