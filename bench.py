@@ -199,13 +199,19 @@ def rel_l2_rows(y, ref):
     return np.sqrt(np.sum(np.abs(y - ref) ** 2, axis=-1) / np.sum(np.abs(ref) ** 2, axis=-1))
 
 
-def bench_config1(estl, torch):
+def bench_config1(estl, torch, autotune=True):
     """N = 4096, batch = 256 (8 MiB, L2-sized): a CUDA graph of 64 executes over
     32 rotating buffer pairs (512 MiB, larger than L2), forward, plus the
-    rel-L2 error of one batch against an FP64 DFT."""
+    rel-L2 error of one batch against an FP64 DFT.  With autotune, the engine's
+    autotuner picks the plan of (4096, 256) first (a latency-bound size: its
+    best tile differs from the 1 GiB sweep's)."""
     import numpy as np
 
     n, batch, rot, reps = 4096, 256, 32, 64
+    tuned = None
+    if autotune:
+        r = estl.autotune(n, batch, iters=20)
+        tuned = [[round(f["ms"], 4), compact_choice(f["choice"])] for f in r["fastest"][:3]]
     rng = np.random.default_rng(1)
     x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
     xs = [torch.from_numpy(x).cuda() for _ in range(rot)]
@@ -230,8 +236,12 @@ def bench_config1(estl, torch):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / (10 * reps)
+    d = plan.describe()["kernels"]
+    del g  # the graph holds the plan's ordering event
+    plan.close()
     return {"workload": "C2C FP32 forward, N=4096, batch=256, uniform[-1,1) seed 1",
             "method": "CUDA graph of 64 executes over 32 rotating buffer pairs (512 MiB > L2)",
+            "plan": d, "autotune_fastest": tuned,
             "us_per_transform_batch": round(1e3 * ms, 3), "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1),
             "gflops": round(5 * n * 12 * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": err}
 
@@ -819,7 +829,8 @@ def main():
 
     configs = {}
     if rank == 0 and not args.no_configs:
-        for key, fn in (("plain_4096x256", bench_config1), ("uneven_8192", bench_uneven),
+        config1 = lambda e, t: bench_config1(e, t, autotune=not args.no_autotune)  # noqa: E731
+        for key, fn in (("plain_4096x256", config1), ("uneven_8192", bench_uneven),
                         ("split_precision", bench_split_precision), ("fft2d", bench_fft2d), ("conv2d", bench_conv2d),
                         ("conv_pairs", bench_conv_pairs), ("bluestein", bench_bluestein),
                         ("served_conv", bench_served_conv)):
