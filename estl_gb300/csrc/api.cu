@@ -887,7 +887,12 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const Strea
                                cudaStream_t stream, const LayoutIO* io = nullptr) {
   std::lock_guard<std::mutex> g(plan->mu);
   estl_status s;
-  if (plan->done_recorded) {
+  // executes that touch device state of the plan (scratch, work lists,
+  // staging, Bluestein buffers, profiling events) are ordered behind the
+  // previous one; a plan without such state (one tile launch in to out) is not
+  const bool stateful = layout.scratch_elems > 0 || layout.blue_m > 0 || io || plan->profiling ||
+                        (aux && aux->nitems > 0);
+  if (stateful && plan->done_recorded) {
     s = check_cuda(cudaStreamWaitEvent(stream, plan->done, 0), "cudaStreamWaitEvent");
     if (s != ESTL_OK) return s;
   }
@@ -906,6 +911,7 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const Strea
     s = launch_layout_out(io->layout, out, io->dst, io->total, stream);
     if (s != ESTL_OK) return s;
   }
+  if (!stateful) return ESTL_OK;
   s = check_cuda(cudaEventRecord(plan->done, stream), "cudaEventRecord");
   if (s != ESTL_OK) return s;
   plan->done_recorded = true;

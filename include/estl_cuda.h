@@ -154,8 +154,10 @@ int64_t estl_plan_launches(estl_plan plan);
  * (FFT_OpenCL_Contiguous.h:107-124) without its host copies; backward
  * transforms are computed for every transform of the batch (the reference
  * conjugates only batch 0, FFT_OpenCL_Contiguous.h:100-102,134-136).
- * Successive executes of one plan are serialised on the device (they share
- * the plan's scratch); use separate plans for concurrent streams. */
+ * Successive executes of a plan that holds device scratch (four-step and
+ * three-pass plans, Bluestein, layout staging) are serialised on the device;
+ * a one-launch plan (n <= 2^14) has no state and its executes on different
+ * streams may overlap.  Use separate plans for concurrent multi-pass work. */
 estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* stream);
 
 /* Host-to-host execute with the semantics of FFT<D>::execute (FFT.h:35,
