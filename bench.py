@@ -72,6 +72,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_value(local_ms, world, bytes_per_step, steps, device="cuda"):
+    """Whole-job throughput of `world` replicas (one process per GPU, each
+    running the same fixed per-GPU workload: weak scaling): every rank's timed
+    milliseconds are reduced with MAX over the default process group, and the
+    value is world * bytes_per_step * steps over that time, in GB/s.  Returns
+    (value, max_ms)."""
+    import torch
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return world * bytes_per_step * steps / (ms / 1e3) / 1e9, ms
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -751,13 +766,8 @@ def main():
                 s[2] += byts
             p.set_profiling(False)
     launches = sum(st[0] for st in stats.values())
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
     bytes_per_step = sum(2 * 16.0 * TOTAL for _ in logns)
-    value = world * bytes_per_step * args.steps / (total_ms / 1e3) / 1e9
+    value, total_ms = replica_value(total_ms, world, bytes_per_step, args.steps)
     peak, peak_src = measured_peak()
 
     # dominant kernel: largest share of the profiled device time
@@ -817,13 +827,8 @@ def main():
             e2e_step()
         t1 = time.perf_counter()
         barrier()
-        e2e_s = t1 - t0
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_s = float(tt.item())
-        e2e = {"value": round(world * bytes_per_step * e2e_steps / e2e_s / 1e9, 2), "unit": "GB/s",
+        e2e_value, _ = replica_value(1e3 * (t1 - t0), world, bytes_per_step, e2e_steps)
+        e2e = {"value": round(e2e_value, 2), "unit": "GB/s",
                "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
                "path": "estl_execute_host (C ABI), pinned host buffers, chunked H2D/compute/D2H pipeline"}
 
