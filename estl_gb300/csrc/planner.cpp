@@ -319,7 +319,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   static const int tuned4[][9] = {
       {15, 7, 4, 5, 4, 3, 0, 4, 4},  {16, 7, 4, 5, 4, 3, 2, 4, 4},  {17, 7, 4, 5, 5, 3, 2, 4, 5},
       {18, 9, 4, 3, 4, 3, 2, 4, 4},  {19, 9, 5, 4, 5, 3, 2, 5, 5},  {20, 10, 5, 3, 5, 3, 2, 5, 5},
-      {21, 10, 5, 3, 4, 2, 2, 5, 4}, {22, 11, 4, 2, 4, 2, 2, 4, 4}, {23, 11, 4, 2, 4, 2, 2, 4, 4},
+      {21, 11, 5, 2, 5, 3, 2, 5, 5}, {22, 11, 5, 2, 4, 2, 2, 5, 4}, {23, 11, 4, 2, 4, 2, 2, 4, 4},
       {24, 12, 5, 2, 5, 2, 0, 4, 4}};
   const int* td = nullptr;
   if (!tc && choice.logn2 < 0 && choice.col_loge < 0 && choice.row_loge < 0)
