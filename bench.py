@@ -702,7 +702,7 @@ def main():
     if args.mode == "auto" and not args.no_autotune:
         # the engine's autotuner picks each size's plan (cached per GPU, n, log2 batch)
         for logn in logns:
-            r = estl.autotune(1 << logn, TOTAL >> logn, iters=3)
+            r = estl.autotune(1 << logn, TOTAL >> logn, iters=5)
             tuned[f"2^{logn}"] = {"candidates": r["candidates"],
                                   "fastest": [[round(f["ms"], 4), compact_choice(f["choice"])] for f in r["fastest"][:3]]}
     plans = {}
