@@ -8,7 +8,8 @@
 // copies (cp.async.bulk, global -> shared, completion counted in bytes on an
 // mbarrier) while the CTA computes the current tile.  A stage is first the
 // landing zone of its tile's rows (row c at c * RS, RS = M + 16/C so that the
-// column-fastest reads are conflict-free), then, once every thread holds its
+// column-fastest reads are conflict-free; RS = M for one row per tile, which
+// also runs whole transforms: N2 = 1), then, once every thread holds its
 // elements in registers, the Stockham exchange buffer of that tile.  The
 // next load into the stage is issued after the tile's last exchange.
 //
@@ -17,6 +18,9 @@
 //
 // BulkColKernel runs the column pass the same way; its tiles are strided
 // column runs, fetched as 2D tensor copies (TMA boxes) through a tensor map.
+//
+// Both are launched with plain stream order; when a programmatically launched
+// kernel precedes them they trigger their dependents at their last tile.
 //
 // Waits are bounded: after kBulkSpinLimit polls the kernel records the tile in
 // an error word, waits (bounded again) for its copies in flight and returns.
