@@ -300,6 +300,7 @@ struct estl_plan_s {
   size_t aux_bytes = 0;
   StreamAux saux{};
   std::mutex mu;
+  std::mutex host_mu;  // one host pipeline run at a time (staging buffers, chunk plans)
   cudaEvent_t done = nullptr;  // last execute of this plan (scratch reuse order)
   bool done_recorded = false;
   // host pipeline (lazily created by estl_execute_host)
@@ -1025,6 +1026,7 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
   if (s != ESTL_OK) return s;
   s = check_buffers(h_in, h_out);
   if (s != ESTL_OK) return s;
+  std::lock_guard<std::mutex> hg(plan->host_mu);
   s = host_pipeline_setup(plan);
   if (s != ESTL_OK) return s;
   const long long n = plan->layout.n, batch = plan->layout.batch, chunk = plan->host_chunk;
@@ -1101,6 +1103,7 @@ estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_
   estl_status s = require_init();
   if (s != ESTL_OK) return s;
   if (!h_in || !h_out || h_in == h_out) return fail(ESTL_INVALID_ARG, "need distinct host buffers");
+  std::lock_guard<std::mutex> hg(plan->host_mu);
   s = host_pipeline_setup(plan);
   if (s != ESTL_OK) return s;
   const long long n = plan->layout.n, batch = plan->layout.batch, chunk = plan->host_chunk, total = n * batch;
