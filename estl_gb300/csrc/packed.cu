@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "engine.h"
@@ -231,6 +232,22 @@ estl_status estl_packed_plan_destroy(estl_packed_plan p) {
   if (!p) return ESTL_OK;
   cudaDeviceSynchronize();
   packed_release(p);
+  return ESTL_OK;
+}
+
+// One call: plan (persistent mode), execute on `stream`, wait for it, check
+// the dependency waits, release the plan.
+estl_status estl_execute_packed(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                const void* d_in, void* d_out, void* stream) {
+  estl_packed_plan p = nullptr;
+  estl_status s = estl_packed_plan_create(offsets, sizes, count, direction, ESTL_PACKED_PERSISTENT, &p);
+  if (s != ESTL_OK) return s;
+  s = estl_packed_execute(p, d_in, d_out, stream);
+  if (s == ESTL_OK) s = check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+  if (s == ESTL_OK) s = estl_packed_check(p);
+  const std::string msg = s == ESTL_OK ? std::string() : std::string(estl_last_error());
+  estl_packed_plan_destroy(p);
+  if (s != ESTL_OK) return fail(s, "%s", msg.c_str());
   return ESTL_OK;
 }
 

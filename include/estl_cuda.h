@@ -347,6 +347,10 @@ estl_status estl_packed_execute(estl_packed_plan plan, const void* d_in, void* d
 estl_status estl_packed_check(estl_packed_plan plan);
 estl_status estl_packed_plan_describe(estl_packed_plan plan, char* buf, size_t len);
 estl_status estl_packed_plan_destroy(estl_packed_plan plan);
+/* One blocking call for a batch used once: plan (persistent mode), execute on
+ * `stream`, wait, check, release. */
+estl_status estl_execute_packed(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                const void* d_in, void* d_out, void* stream);
 
 /* ---- Serving: a request loop with continuous batching ----
  * Requests (1D FFTs and FFT convolutions of mixed lengths, host buffers) are

@@ -130,3 +130,25 @@ def test_gpu_packed_backward_and_gaps(engine):
     for o, n in zip(offsets, sizes):
         mask[o:o + n] = False
     assert np.all(np.isnan(y[mask].real))
+
+
+@pytest.mark.gpu
+def test_gpu_execute_packed_one_call(engine):
+    """estl_execute_packed (plan, execute, wait, check, release in one call)
+    gives the persistent plan's result bit for bit."""
+    import torch
+
+    from estl_gb300._lib import check, lib
+    offsets, sizes, x = make_batch(500, 3, 15, 11, gap=3)
+    xd = torch.from_numpy(x).cuda()
+    ref, _ = gpu_packed(offsets, sizes, xd, 0, -1)
+    y = torch.full_like(xd, float("nan"))
+    check(lib().estl_execute_packed(offsets.ctypes.data, sizes.ctypes.data, len(sizes), -1,
+                                    ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    y = y.cpu().numpy()
+    mask = np.zeros(len(x), bool)
+    for o, n in zip(offsets, sizes):
+        mask[o:o + n] = True
+    assert np.array_equal(y[mask], ref[mask])
+    check_against_oracle(offsets, sizes, x, y, -1, every=10)
