@@ -10,7 +10,9 @@ Metric: compulsory HBM GB/s = 16 bytes per complex element and direction
 
 --impl reference times the reference's own algorithm for the path on the
 host cores instead (the FP32 restatement of FFT_OpenCL_Contiguous in
-oracle/ref_contiguous.c; neither the OpenCL original nor FFTW3 can run here).
+oracle/ref_contiguous.c; the OpenCL original cannot run here).  Beside it,
+cpu_baseline.libraries times FFTW3 single precision where the host has
+libfftw3f (dlopen probe), scipy.fft on all threads, and the FP64 oracle.
 """
 import argparse
 import json
@@ -189,6 +191,100 @@ def cpu_baseline_sample(logns, threads, budget_s=20.0):
     desc = (f"FP32 restatement of FFT_OpenCL_Contiguous (radix-16 Stockham, runtime twiddles), {threads} threads; "
             f"N=2^{done[0]}..2^{done[-1]}, max(2^22, N) complex per size, forward+backward")
     return tot_bytes / tot_s / 1e9, desc
+
+
+def _fftwf_time(x, sign, threads):
+    """Seconds for one fftwf_plan_many_dft(FFTW_ESTIMATE) execute of the rows
+    of x (the FFT_FFTW3.h:26-28 call: rank 1, howmany = rows, stride 1,
+    distance n, out of place), or None where the host has no libfftw3f."""
+    import ctypes
+    import ctypes.util
+
+    import numpy as np
+    names = [ctypes.util.find_library("fftw3f"), "libfftw3f.so.3"]
+    lib = None
+    for name in names:
+        if name:
+            try:
+                lib = ctypes.CDLL(name)
+                break
+            except OSError:
+                pass
+    if lib is None:
+        return None
+    try:
+        thr = ctypes.CDLL(ctypes.util.find_library("fftw3f_threads") or "libfftw3f_threads.so.3")
+        if thr.fftwf_init_threads():
+            thr.fftwf_plan_with_nthreads(ctypes.c_int(threads))
+    except OSError:
+        pass
+    lib.fftwf_plan_many_dft.restype = ctypes.c_void_p
+    lib.fftwf_plan_many_dft.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint]
+    lib.fftwf_execute.argtypes = [ctypes.c_void_p]
+    lib.fftwf_destroy_plan.argtypes = [ctypes.c_void_p]
+    rows, n = x.shape
+    y = np.empty_like(x)
+    dims = (ctypes.c_int * 1)(n)
+    plan = lib.fftwf_plan_many_dft(1, dims, rows, x.ctypes.data, None, 1, n, y.ctypes.data, None, 1, n, sign, 1 << 6)
+    if not plan:
+        return None
+    t0 = time.perf_counter()
+    lib.fftwf_execute(ctypes.c_void_p(plan))
+    dt = time.perf_counter() - t0
+    lib.fftwf_destroy_plan(ctypes.c_void_p(plan))
+    return dt
+
+
+def cpu_library_sample(logns, threads, budget_s=4.0):
+    """Optimised CPU FFTs beside the port, on the same kind of sample (2^22
+    complex64 per size, uniform[-1,1), forward + backward), each for about
+    budget_s: FFTW3 single precision with FFTW_ESTIMATE where the host has it,
+    scipy.fft (pocketfft, complex64, all threads) as a labelled stand-in, and
+    the FP64 oracle.  Returns {name: GB/s or "unavailable ..."}."""
+    import numpy as np
+
+    import oracle
+    try:
+        import scipy.fft as sfft
+    except ImportError:
+        sfft = None
+
+    def run(fn):
+        rng = np.random.default_rng(2)
+        tot_b, tot_s = 0.0, 0.0
+        for logn in logns:
+            n = 1 << logn
+            batch = max(1, (1 << 22) // n)
+            x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(np.complex64)
+            for sign in (-1, +1):
+                dt = fn(x, sign)
+                if dt is None:
+                    return None
+                tot_s += dt
+                tot_b += 16.0 * n * batch
+            if tot_s > budget_s:
+                break
+        return round(tot_b / tot_s / 1e9, 3)
+
+    def timed(f):
+        def g(x, sign):
+            t0 = time.perf_counter()
+            f(x, sign)
+            return time.perf_counter() - t0
+        return g
+
+    out = {}
+    v = run(lambda x, s: _fftwf_time(x, s, threads))
+    out["fftw3f_estimate"] = v if v is not None else "unavailable on this box (no libfftw3f)"
+    if sfft is not None:
+        out["scipy_fft_c64"] = run(timed(lambda x, s: (sfft.fft if s < 0 else sfft.ifft)(x, axis=-1, workers=threads)))
+    else:
+        out["scipy_fft_c64"] = "unavailable (scipy not importable)"
+    out["oracle_fp64"] = run(timed(lambda x, s: oracle.fft(x, s, nthreads=threads)))
+    out["unit"] = "GB/s"
+    return out
 
 
 def fp64_fft(x, sign=-1):
@@ -665,9 +761,11 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "C2C FP32 FFT sweep N=2^10..2^24, forward+backward (bounded host sample)",
                    "sample": desc, "parallelism": "host threads"},
-        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc,
+                         "libraries": cpu_library_sample(logns, threads)},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "notes": "FFTW3 (the reference's CPU backend) is not installed on this box; MKL backend does not compile",
+        "notes": "FFTW3 (the reference's CPU backend) is probed with dlopen and timed where present "
+                 "(cpu_baseline.libraries); MKL backend does not compile",
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -850,7 +948,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, desc = cpu_baseline_sample(logns, threads, budget_s=20.0)
-        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc}
+        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": desc,
+               "libraries": cpu_library_sample(logns, threads)}
 
     if rank == 0:
         line = {
