@@ -196,6 +196,8 @@ estl_status estl_conv_execute(const estl_conv_request* reqs, int64_t count, int 
   if (workspace_bytes < L.workspace_bytes)
     return fail(ESTL_INVALID_ARG, "workspace of %zu bytes, %zu needed", workspace_bytes, L.workspace_bytes);
   if ((uintptr_t)d_workspace & 255) return fail(ESTL_INVALID_ARG, "workspace must be 256-byte aligned");
+  if (((uintptr_t)d_signals | (uintptr_t)d_filters | (uintptr_t)d_out) & 3)
+    return fail(ESTL_INVALID_ARG, "signal, filter and output buffers must be 4-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   char* w = static_cast<char*>(d_workspace);
   // descriptors: from pageable host memory, copied before the call returns

@@ -164,6 +164,7 @@ estl_status estl_conv2d_plan_create(int64_t width, int64_t height, int64_t kwidt
 // by 1 / (Pw Ph) and conjugated for correlation.
 estl_status estl_conv2d_plan_set_filter(estl_conv2d_plan p, const float* d_filter, void* stream) {
   if (!p || !d_filter) return fail(ESTL_INVALID_ARG, "estl_conv2d_plan_set_filter: null argument");
+  if ((uintptr_t)d_filter & 3) return fail(ESTL_INVALID_ARG, "estl_conv2d_plan_set_filter: filter must be 4-byte aligned");
   Engine& E = engine();
   const cudaStream_t st = (cudaStream_t)stream;
   Conv2dArgs a = conv2d_filter_args(p->g, p->kw, p->kh, (p->flags & ESTL_CONV_REFERENCE_COMPAT) != 0,
@@ -180,6 +181,8 @@ estl_status estl_conv2d_plan_set_filter(estl_conv2d_plan p, const float* d_filte
 estl_status estl_conv2d_plan_execute(estl_conv2d_plan p, const float* d_images, float* d_out, void* stream) {
   if (!p || !d_images || !d_out) return fail(ESTL_INVALID_ARG, "estl_conv2d_plan_execute: null argument");
   if (!p->filter_set) return fail(ESTL_INVALID_ARG, "estl_conv2d_plan_execute: set the filter first");
+  if (((uintptr_t)d_images | (uintptr_t)d_out) & 3)
+    return fail(ESTL_INVALID_ARG, "estl_conv2d_plan_execute: buffers must be 4-byte aligned");
   Engine& E = engine();
   const cudaStream_t st = (cudaStream_t)stream;
   Conv2dArgs a = conv2d_exec_args(p->g, p->w, p->h, p->count, (p->flags & ESTL_CONV_REFERENCE_COMPAT) != 0, d_images,

@@ -184,4 +184,12 @@ def test_gpu_conv2d_errors(engine):
         p.execute(torch.zeros(64, device="cuda"))
     with pytest.raises(EstlError):  # wrong filter size
         p.set_filter(torch.zeros(8, device="cuda"))
+    from estl_gb300._lib import lib
+    k = torch.zeros(16, device="cuda")
+    # a float pointer off its 4-byte boundary is refused before any launch
+    assert lib().estl_conv2d_plan_set_filter(p._h, ctypes.c_void_p(k.data_ptr() + 2), None) != 0
+    p.set_filter(k[:9])
+    x = torch.zeros(200, device="cuda")
+    assert lib().estl_conv2d_plan_execute(p._h, ctypes.c_void_p(x.data_ptr() + 1),
+                                          ctypes.c_void_p(x.data_ptr() + 128), None) != 0
     p.close()
