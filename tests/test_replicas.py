@@ -55,3 +55,17 @@ def test_reference_arm_other_ranks_exit_without_work():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2"],
                        capture_output=True, text=True, timeout=120, env=env)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_cpu_library_baselines_are_labelled():
+    """cpu_baseline.libraries: FFTW3 single precision is either timed or
+    reported unavailable, scipy.fft and the FP64 oracle carry GB/s."""
+    sys.path.insert(0, ROOT)
+    import bench
+    libs = bench.cpu_library_sample([10, 12], 2, budget_s=0.05)
+    assert libs["unit"] == "GB/s"
+    f = libs["fftw3f_estimate"]
+    assert (isinstance(f, float) and f > 0) or f.startswith("unavailable")
+    assert libs["oracle_fp64"] > 0
+    s = libs["scipy_fft_c64"]
+    assert (isinstance(s, float) and s > 0) or s.startswith("unavailable")
