@@ -122,7 +122,11 @@ const std::vector<cf32>& host_bank() {
 // The threads of one emulated CTA are fibers (ucontext coroutines) on the
 // calling host thread: a barrier is a yield to a round-robin scheduler that
 // resumes every fiber once per round, so all fibers reach each barrier before
-// any passes it.  No OS threads, no futexes.
+// any passes it.  No OS threads, no futexes.  A round runs the fibers in
+// thread order, or in reverse thread order (every odd CTA of a grid): a
+// shared-memory slot read in the same barrier interval in which another
+// thread writes it then holds the old value (or the NaN poison) in one of
+// the two orders, and the race fails the parity check.
 struct FiberSched {
   std::vector<ucontext_t> ctx;
   std::vector<std::vector<char>> stacks;
@@ -142,7 +146,7 @@ void fiber_entry() {
   // returning resumes uc_link (the scheduler)
 }
 
-void run_fibers(int nt, const std::function<void(int)>& body) {
+void run_fibers(int nt, const std::function<void(int)>& body, bool reverse) {
   static thread_local FiberSched sched;
   FiberSched& s = sched;
   if ((int)s.stacks.size() < nt) {
@@ -163,7 +167,8 @@ void run_fibers(int nt, const std::function<void(int)>& body) {
   }
   for (;;) {
     bool any = false;
-    for (int t = 0; t < nt; ++t) {
+    for (int i = 0; i < nt; ++i) {
+      const int t = reverse ? nt - 1 - i : i;
       if (s.done[t]) continue;
       any = true;
       s.current = t;
@@ -175,7 +180,10 @@ void run_fibers(int nt, const std::function<void(int)>& body) {
 }
 
 template <class Fn, class Args>
-bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
+// reversible: the kernel's threads may run in either order between barriers
+// (false for kernels whose copies are issued by one thread and complete at
+// issue in the emulator, with the other threads' mbarrier waits returning at once)
+bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid, bool reversible = true) {
   // the device limit on dynamic shared memory per CTA (227 KB on sm_103a)
   if (smem_elems * (long long)sizeof(cf32) > 227LL * 1024) {
     std::lock_guard<std::mutex> g(g_msg_mu);
@@ -205,12 +213,14 @@ bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long g
         failed = true;
       }
     };
-    run_fibers(nt, body);
+    run_fibers(nt, body, reversible && (cta & 1));
   }
   return !failed;
 }
 
-bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) { return run_generic(k.nt, k.smem, k.fn, a, grid); }
+bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
+  return run_generic(k.nt, k.smem, k.fn, a, grid, k.pipe != 2);
+}
 
 }  // namespace
 
