@@ -284,7 +284,9 @@ estl_status estl_conv_execute(const estl_conv_request* reqs, int64_t count, int 
 /* A convolution plan: `count` signals of signal_len samples, packed
  * back-to-back, all with one filter whose spectrum is computed once
  * (estl_conv_plan_set_filter) and cached on the device; outputs are packed
- * back-to-back with estl_conv_output_length samples each.  Stream ordered. */
+ * back-to-back with estl_conv_output_length samples each.  Stream ordered.
+ * The executes of one plan share its device scratch: executes on unordered
+ * streams race on it, so order them or make one plan per stream. */
 typedef struct estl_conv_plan_s* estl_conv_plan;
 estl_status estl_conv_plan_create(int64_t signal_len, int64_t filter_len, int64_t count, int flags,
                                   estl_conv_plan* plan);
@@ -307,7 +309,9 @@ estl_status estl_conv_plan_destroy(estl_conv_plan plan);
  * Ph <= 2^12, Pw Ph <= 2^26.  Three launches per execute (row FFTs of the
  * padded rows, column FFT x spectrum x inverse column FFT, inverse row FFTs
  * with the real crop); the filter spectrum is computed once per
- * estl_conv2d_plan_set_filter.  Stream ordered. */
+ * estl_conv2d_plan_set_filter.  Stream ordered; the executes of one plan
+ * share its device scratch, so executes on unordered streams race on it:
+ * order them or make one plan per stream. */
 estl_status estl_conv2d_output_size(int64_t width, int64_t height, int64_t kwidth, int64_t kheight, int flags,
                                     int64_t* out_width, int64_t* out_height);
 typedef struct estl_conv2d_plan_s* estl_conv2d_plan;
