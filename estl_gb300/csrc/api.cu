@@ -480,8 +480,17 @@ const char* estl_status_string(estl_status s) {
 
 int64_t estl_max_batch(int64_t n) {
   Engine& E = engine();
-  if (!E.inited || ilog2_exact(n) < 0 || ilog2_exact(n) > kMaxLogN) return 0;
-  size_t used = E.used.load();
+  if (!E.inited || n < 1) return 0;
+  size_t fixed = 0;
+  if (ilog2_exact(n) < 0) {
+    // Bluestein: chirp (n), kernel spectrum (M), two work buffers and the
+    // inner plan's scratch of at most 2^26 elements each, held once per plan
+    if (n < 3 || n > (1LL << (kBluesteinMaxLogM - 1))) return 0;
+    fixed = sizeof(cf32) * ((size_t)n + (size_t)bluestein_m(n) + 3 * ((size_t)1 << 26));
+  } else if (ilog2_exact(n) > kMaxLogN) {
+    return 0;
+  }
+  const size_t used = E.used.load() + fixed;
   if (used >= E.budget) return 0;
   long long b = (long long)((E.budget - used) / (3 * sizeof(cf32) * (size_t)n));
   return b > INT32_MAX ? INT32_MAX : b;

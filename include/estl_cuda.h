@@ -73,7 +73,10 @@ const char* estl_status_string(estl_status status);
  * its own input, output and scratch buffers; clamped to INT32_MAX.
  * Replaces FFT_OpenCL_Contiguous::getMaxBatchSize (FFT_OpenCL_Contiguous.h:43-44),
  * computed in 64 bits instead of the int that overflows above 2 GiB
- * (uOpenCL.h:323-332).  Returns 0 before estl_init or for unsupported n. */
+ * (uOpenCL.h:323-332).  Lengths that are not powers of two (Bluestein plans)
+ * first set aside the plan's fixed buffers (chirp, kernel spectrum, work and
+ * scratch: at most 8 (n + M) + 1.5 GiB).  Returns 0 before estl_init or for
+ * unsupported n. */
 int64_t estl_max_batch(int64_t n);
 
 /* Plan `batch` transforms of length n (power of two, 1 <= n <= 2^24).

@@ -165,6 +165,9 @@ def test_errors(engine):
     with pytest.raises(EstlError):
         p.execute_ptr(x.data_ptr() + 4, x.data_ptr() + 256)  # misaligned
     assert engine.max_batch(4096) > 1000
+    # Bluestein lengths: the budget less the plan's fixed buffers; out-of-range lengths: 0
+    assert engine.max_batch(1000) > 1000 and engine.max_batch(1 << 23) > 0
+    assert engine.max_batch(1 << 25) == 0 and engine.max_batch((1 << 23) + 1) == 0 and engine.max_batch(0) == 0
 
 
 def test_autotune_keeps_results(engine, tmp_path, monkeypatch):
