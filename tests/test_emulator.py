@@ -225,3 +225,16 @@ def test_bulk_single_tiles(emu, logn, loge, logr):
         rc, msg, y = emu_run(emu, n, 5, x, sign, choice)
         assert rc == 0, msg
         assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL
+
+
+@pytest.mark.parametrize("logn", range(1, 9))
+def test_exhaustive_small_sizes_and_batches(emu, logn):
+    """Small sizes exhaustively: N = 2..2^8, every batch 1..17 (ragged last
+    CTAs of every tile), both directions, default plans, against the oracle."""
+    n = 1 << logn
+    for batch in range(1, 18):
+        x = rand_c64((batch, n), 100 * logn + batch)
+        for sign in (-1, +1):
+            rc, msg, y = emu_run(emu, n, batch, x, sign)
+            assert rc == 0, (n, batch, msg)
+            assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL, (n, batch, sign)

@@ -134,6 +134,45 @@ def test_execute_host_matches_device(engine):
         assert np.array_equal(yp, yd)
 
 
+def sentinel_c64(count, device="cuda"):
+    """count complex64 elements, every one 1234.5 - 6789.25i."""
+    import torch
+    g = torch.empty((count, 2), dtype=torch.float32, device=device)
+    g[:, 0] = 1234.5
+    g[:, 1] = -6789.25
+    return torch.view_as_complex(g)
+
+
+@pytest.mark.parametrize("logn", range(1, 9))
+def test_small_sizes_every_batch_with_guards(engine, logn):
+    """N = 2..2^8, every batch 1..17, both directions: results against the
+    oracle, the input unchanged, and guard regions of sentinel values on both
+    sides of the input and of the output untouched (nothing written outside
+    the output)."""
+    import torch
+    n = 1 << logn
+    G = 1024  # guard elements on each side (8 KiB: keeps both buffers 16-byte aligned)
+    s = complex(1234.5, -6789.25)
+    st = torch.cuda.current_stream().cuda_stream
+    for batch in range(1, 18):
+        m = batch * n
+        x = uniform_c64((batch, n), 5000 + 100 * logn + batch)
+        xin = sentinel_c64(m + 2 * G)
+        xin[G:G + m] = torch.from_numpy(x.reshape(-1)).cuda()
+        for direction in (-1, +1):
+            out = sentinel_c64(m + 2 * G)
+            p = engine.Plan(n, batch, direction)
+            p.execute_ptr(xin.data_ptr() + 8 * G, out.data_ptr() + 8 * G, st)
+            torch.cuda.synchronize()
+            o = out.cpu().numpy()
+            xi = xin.cpu().numpy()
+            assert np.all(o[:G] == s) and np.all(o[G + m:] == s), (n, batch, direction)
+            assert np.all(xi[:G] == s) and np.all(xi[G + m:] == s) and np.array_equal(xi[G:G + m], x.reshape(-1))
+            e = oracle.rel_l2(o[G:G + m].reshape(batch, n), oracle.fft(x, direction))
+            assert e.max() < tol(n), (n, batch, direction, e.max())
+            p.close()
+
+
 def test_non_default_stream(engine):
     import torch
     x = uniform_c64((16, 1 << 15), 3)
