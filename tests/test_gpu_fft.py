@@ -209,6 +209,30 @@ def test_errors(engine):
     assert engine.max_batch(1 << 25) == 0 and engine.max_batch((1 << 23) + 1) == 0 and engine.max_batch(0) == 0
 
 
+def test_hbm_budget_refusal_leaves_nothing_behind(engine):
+    """Allocator failure made on the host: with the budget 1 MiB above the
+    bytes in use, plans that need device scratch (four-step 2^20, Bluestein
+    10^6) are refused with ESTL_OUT_OF_MEMORY and the bytes in use do not
+    change; a single-pass plan, which needs none, still runs; the budget is
+    restored afterwards."""
+    from estl_gb300 import EstlError
+    used, budget = engine.memory_usage()
+    try:
+        engine.init(0, used + (1 << 20))
+        for n, batch in ((1 << 20, 16), (1000000, 4)):
+            with pytest.raises(EstlError) as e:
+                engine.Plan(n, batch, -1)
+            assert e.value.name == "ESTL_OUT_OF_MEMORY", (n, str(e.value))
+            assert engine.memory_usage()[0] == used
+        x = uniform_c64((4, 4096), 9)
+        y, p = run(engine, x, -1)
+        assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < 2e-6
+        p.close()
+    finally:
+        engine.init(0, budget)
+    assert engine.memory_usage()[1] == budget
+
+
 def test_autotune_keeps_results(engine, tmp_path, monkeypatch):
     import torch
     monkeypatch.setenv("ESTL_TUNE_CACHE", str(tmp_path / "tune.jsonl"))
