@@ -704,8 +704,20 @@ int emu_conv2d_run(long long w, long long h, long long kw, long long kh, long lo
 // elements).  persistent: the work-queue kernel run as one CTA (items in
 // queue order); else one CTA per item, launch by launch.  Returns 0 ok,
 // 1 out-of-bounds access, 2 layout error, 4 a dependency wait gave up.
+int emu_packed_run_launches(const long long* offsets, const long long* sizes, long long count, int persistent,
+                            int sign, const float* in, float* out, int skip_columns, char* err, int errlen);
+
 int emu_packed_run(const long long* offsets, const long long* sizes, long long count, int persistent, int sign,
                    const float* in, float* out, char* err, int errlen) {
+  return emu_packed_run_launches(offsets, sizes, count, persistent, sign, in, out, 0, err, errlen);
+}
+
+// As emu_packed_run, with skip_columns = 1 leaving out every launch that holds
+// column items (non-persistent mode): the row items' dependency waits then
+// wait for counts that nothing raises, give up after their iteration limit,
+// set the error word and skip their work (return 4, output untouched).
+int emu_packed_run_launches(const long long* offsets, const long long* sizes, long long count, int persistent,
+                            int sign, const float* in, float* out, int skip_columns, char* err, int errlen) {
   PackedLayout L;
   std::string e;
   if (!build_packed_layout(offsets, sizes, count, persistent != 0, &L, &e)) {
@@ -739,6 +751,7 @@ int emu_packed_run(const long long* offsets, const long long* sizes, long long c
     a.sgn = sign < 0 ? 1.f : -1.f;
     a.persistent = persistent ? 1 : 0;
     counters[0] = 0;
+    if (skip_columns && !persistent && a.nitems > 0 && L.items[(size_t)a.item_base].kind == PK_COL) continue;
     int slot[2] = {0, 0};
     auto fn = [&slot](const PackedArgs& args, long long cta, int tid, cf32* sm) { packed_run(args, cta, tid, sm, slot); };
     const long long grid = persistent ? 1 : a.nitems;

@@ -80,6 +80,23 @@ def test_layout_validation(emu):
         assert rc == 2 and msg
 
 
+def test_emulated_dependency_wait_gives_up(emu):
+    """A row item whose column items never run (their launch left out): the
+    bounded dependency wait runs out, sets the error word (status 4) and the
+    item is skipped, so the output stays untouched; with the column launch
+    the same transform completes and agrees with the oracle."""
+    offsets, sizes, x = make_batch(1, 13, 13, 21)
+    y = np.full_like(x, np.nan + 1j * np.nan)
+    err = ctypes.create_string_buffer(512)
+    rc = emu.emu_packed_run_launches(offsets.ctypes.data, sizes.ctypes.data, 1, 0, -1, x.ctypes.data, y.ctypes.data,
+                                     1, err, len(err))
+    assert rc == 4 and "gave up" in err.value.decode()
+    assert np.all(np.isnan(y.real))
+    rc, msg, y = emu_packed(emu, offsets, sizes, x, False, -1)
+    assert rc == 0, msg
+    check_against_oracle(offsets, sizes, x, y, -1)
+
+
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
@@ -152,3 +169,4 @@ def test_gpu_execute_packed_one_call(engine):
         mask[o:o + n] = True
     assert np.array_equal(y[mask], ref[mask])
     check_against_oracle(offsets, sizes, x, y, -1, every=10)
+
