@@ -19,8 +19,9 @@ from ._lib import (BACKWARD, FORWARD, LAYOUT_BLOCK_PLANAR, LAYOUT_INTERLEAVED, L
                    PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, PREC_SPLIT_FP16, EstlError,
                    PlanOptions, check, lib)
 
-__all__ = ["init", "shutdown", "Plan", "Plan2D", "Conv2DPlan", "fft", "autotune", "max_batch", "memory_usage",
-           "EstlError", "FORWARD", "BACKWARD", "CONV_CORRELATE", "CONV_REFERENCE_COMPAT"]
+__all__ = ["init", "shutdown", "Plan", "Plan2D", "Conv2DPlan", "PackedPlan", "fft", "fft_packed", "autotune",
+           "max_batch", "memory_usage", "EstlError", "FORWARD", "BACKWARD", "CONV_CORRELATE",
+           "CONV_REFERENCE_COMPAT"]
 
 _initialised = False
 
@@ -248,6 +249,90 @@ class Conv2DPlan:
             self.close()
         except Exception:
             pass
+
+
+class PackedPlan:
+    """An uneven batch: transform i of length sizes[i] (a power of two in
+    [2, 2^18]) at complex-element offset offsets[i] of both the input and the
+    output buffer, transforms not overlapping.  mode "persistent": one launch
+    whose CTAs take work items from a device queue; "per_size": one launch per
+    size class.  The reference has one FFT object per size (tests/Test.cpp:45-60)."""
+
+    MODES = {"persistent": 0, "per_size": 1}
+
+    def __init__(self, offsets, sizes, direction=FORWARD, mode="persistent"):
+        import numpy as np
+        self._offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        if self._offsets.ndim != 1 or self._offsets.shape != self._sizes.shape or self._sizes.size == 0:
+            raise EstlError(1, "offsets and sizes must be 1-D arrays of one non-zero length")
+        if mode not in self.MODES:
+            raise EstlError(1, f"mode must be one of {sorted(self.MODES)}")
+        _ensure_init()
+        self.direction = int(direction)
+        self.extent = int((self._offsets + self._sizes).max())
+        h = ctypes.c_void_p()
+        check(lib().estl_packed_plan_create(self._offsets.ctypes.data, self._sizes.ctypes.data, self._sizes.size,
+                                            self.direction, self.MODES[mode], ctypes.byref(h)))
+        self._h = h
+
+    def execute(self, x, out=None, stream=None):
+        """x: contiguous complex64 CUDA tensor of at least `extent` elements;
+        out (same size as x) receives the transforms, the gaps between them
+        are not written."""
+        import torch
+        if x.dtype != torch.complex64 or not x.is_cuda or not x.is_contiguous() or x.numel() < self.extent:
+            raise EstlError(1, f"input must be a contiguous complex64 CUDA tensor of >= {self.extent} elements")
+        if out is None:
+            out = torch.empty_like(x)
+        if out.dtype != torch.complex64 or not out.is_cuda or not out.is_contiguous() or out.numel() < self.extent:
+            raise EstlError(1, f"output must be a contiguous complex64 CUDA tensor of >= {self.extent} elements")
+        check(lib().estl_packed_execute(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                        ctypes.c_void_p(_stream_handle(stream))))
+        return out
+
+    def check(self):
+        """Synchronise; raise if a row item's dependency wait gave up."""
+        check(lib().estl_packed_check(self._h))
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(1024)
+        check(lib().estl_packed_plan_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().estl_packed_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fft_packed(x, offsets, sizes, inverse=False, out=None, stream=None):
+    """One blocking call for an uneven batch used once (estl_execute_packed):
+    plan, execute, wait, check and release.  Arguments as PackedPlan."""
+    import numpy as np
+    import torch
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+    if offsets.ndim != 1 or offsets.shape != sizes.shape or sizes.size == 0:
+        raise EstlError(1, "offsets and sizes must be 1-D arrays of one non-zero length")
+    extent = int((offsets + sizes).max())
+    if x.dtype != torch.complex64 or not x.is_cuda or not x.is_contiguous() or x.numel() < extent:
+        raise EstlError(1, f"input must be a contiguous complex64 CUDA tensor of >= {extent} elements")
+    _ensure_init()
+    if out is None:
+        out = torch.empty_like(x)
+    if out.dtype != torch.complex64 or not out.is_cuda or not out.is_contiguous() or out.numel() < extent:
+        raise EstlError(1, f"output must be a contiguous complex64 CUDA tensor of >= {extent} elements")
+    check(lib().estl_execute_packed(offsets.ctypes.data, sizes.ctypes.data, sizes.size,
+                                    BACKWARD if inverse else FORWARD, ctypes.c_void_p(x.data_ptr()),
+                                    ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(_stream_handle(stream))))
+    return out
 
 
 _plan_cache = {}

@@ -170,3 +170,39 @@ def test_gpu_execute_packed_one_call(engine):
     assert np.array_equal(y[mask], ref[mask])
     check_against_oracle(offsets, sizes, x, y, -1, every=10)
 
+
+
+@pytest.mark.gpu
+def test_gpu_python_packed_api(engine):
+    """PackedPlan and fft_packed (the package's wrappers of the packed entry
+    points) give the raw C-ABI result bit for bit."""
+    import torch
+    offsets, sizes, x = make_batch(200, 2, 14, 13, gap=2)
+    xd = torch.from_numpy(x).cuda()
+    ref, _ = gpu_packed(offsets, sizes, xd, 0, +1)
+    p = engine.PackedPlan(offsets, sizes, engine.BACKWARD)
+    y = p.execute(xd, out=torch.full_like(xd, float("nan")))
+    p.check()
+    assert p.describe()["persistent"]
+    p.close()
+    z = engine.fft_packed(xd, offsets, sizes, inverse=True, out=torch.full_like(xd, float("nan")))
+    mask = np.zeros(len(x), bool)
+    for o, n in zip(offsets, sizes):
+        mask[o:o + n] = True
+    assert np.array_equal(y.cpu().numpy()[mask], ref[mask])
+    assert np.array_equal(z.cpu().numpy()[mask], ref[mask])
+
+
+def test_python_packed_api_validates_before_the_engine():
+    """Argument errors are raised on the host, before any engine call."""
+    import torch
+
+    import estl_gb300 as estl
+    with pytest.raises(estl.EstlError):
+        estl.PackedPlan([0, 16], [16])
+    with pytest.raises(estl.EstlError):
+        estl.PackedPlan([], [])
+    with pytest.raises(estl.EstlError):
+        estl.PackedPlan([0], [16], mode="bucketed")
+    with pytest.raises(estl.EstlError):  # a host tensor
+        estl.fft_packed(torch.zeros(16, dtype=torch.complex64), [0], [16])
