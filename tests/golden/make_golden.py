@@ -3,7 +3,8 @@ with mpmath at 40 significant digits (independent of the C oracle).
 
 Inputs follow the distributions of the benchmark configurations: re/im
 i.i.d. uniform[-1, 1) (the Apple harness distribution, OpenCL_FFT/main.cpp:439-440)
-and the known-answer cosine of tests/Test.cpp:60-63.  Output convention is
+and the known-answer cosine of tests/Test.cpp:60-63; powers of two 1..256 and
+the lengths 3, 5, 12, 100, 1000 (the Bluestein path).  Output convention is
 FFTW's (FFT_FFTW3.h:26-28): forward exp(-2 pi i jk/n), unnormalised.
 
 Run:  python tests/golden/make_golden.py
@@ -45,6 +46,14 @@ def main():
     x = np.cos(2 * np.pi * (eff * q) / m).astype(np.float32).astype(np.complex64)
     arrays["kat_x"] = x
     arrays["kat_y"] = dft_mp(x.astype(np.complex128), -1)
+    # lengths that are not powers of two (the Bluestein path), own generator so
+    # that the arrays above stay as they were
+    rng2 = np.random.default_rng(20112)
+    for n in (3, 5, 12, 100, 1000):
+        for sign in (-1, +1):
+            x = (rng2.uniform(-1, 1, n) + 1j * rng2.uniform(-1, 1, n)).astype(np.complex64)
+            arrays[f"x_{n}_{sign}"] = x
+            arrays[f"y_{n}_{sign}"] = dft_mp(x.astype(np.complex128), sign)
     np.savez_compressed(os.path.join(HERE, "dft_golden.npz"), **arrays)
     print("wrote", len(arrays), "arrays")
 

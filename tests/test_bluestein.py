@@ -43,6 +43,18 @@ def emu_blue(emu, x, sign):
     return rc, err.value.decode(), y
 
 
+@pytest.mark.parametrize("n", [3, 5, 12, 100, 1000])
+def test_emulated_bluestein_golden(emu, n):
+    """The Bluestein kernels (emulated) against the mpmath golden vectors."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "dft_golden.npz"))
+    for sign in (-1, +1):
+        x, ref = g[f"x_{n}_{sign}"], g[f"y_{n}_{sign}"]
+        rc, msg, y = emu_blue(emu, np.ascontiguousarray(x[None, :]), sign)
+        assert rc == 0, msg
+        assert rel(y, ref[None, :]).max() < TOL, (n, sign)
+
+
 @pytest.mark.parametrize("n", [3, 5, 6, 7, 12, 15, 100, 243, 1000, 3000])
 def test_emulated_bluestein(emu, n):
     x = rand_c64((3, n), n)

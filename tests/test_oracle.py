@@ -57,6 +57,16 @@ def test_golden_vectors():
     assert np.abs(out - g["kat_y"]).max() < 1e-12
 
 
+@pytest.mark.parametrize("n", [3, 5, 12, 100, 1000])
+def test_golden_vectors_other_lengths(n):
+    """The long-double direct DFT, the target of the lengths that are not
+    powers of two, against the mpmath golden vectors of those lengths."""
+    g = np.load(GOLDEN)
+    for sign in (-1, +1):
+        x, y = g[f"x_{n}_{sign}"], g[f"y_{n}_{sign}"]
+        assert oracle.rel_l2(oracle.dft_ld(x.astype(np.complex128), sign), y) < 1e-15, (n, sign)
+
+
 @pytest.mark.parametrize("logn", [1, 2, 3, 5, 8, 10])
 def test_against_long_double_dft(logn):
     n = 1 << logn
