@@ -1,5 +1,6 @@
 // packed_plan.cpp — see packed_plan.h.
 #include "packed_plan.h"
+#include "planner.h"
 
 #include <algorithm>
 #include <cmath>
@@ -42,8 +43,8 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
                       " is not a power of two in [2, 2^" + std::to_string(kPackedMaxLog) + "]";
       return false;
     }
-    if (offsets[i] < 0) {
-      if (err) *err = "transform " + std::to_string(i) + ": negative offset";
+    if (offsets[i] < 0 || offsets[i] > (1LL << kMaxTotalLog)) {
+      if (err) *err = "transform " + std::to_string(i) + ": offset outside [0, 2^" + std::to_string(kMaxTotalLog) + "]";
       return false;
     }
     L.lognv[i] = l;

@@ -149,6 +149,10 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     set_err(err, "batch must be >= 1 (got %lld)", batch);
     return false;
   }
+  if (batch > ((1LL << kMaxTotalLog) >> logn)) {
+    set_err(err, "n * batch must be at most 2^40 elements (got n = %lld, batch = %lld)", n, batch);
+    return false;
+  }
   Plan1D p;
   p.n = n;
   p.batch = batch;
@@ -395,6 +399,11 @@ bool make_plan2d(long long xdim, long long ydim, long long batch, const PlanChoi
     set_err(err, "batch must be >= 1 (got %lld)", batch);
     return false;
   }
+  if (batch > ((1LL << kMaxTotalLog) >> (logx + logy))) {
+    set_err(err, "xdim * ydim * batch must be at most 2^%lld elements (got batch %lld)", (long long)kMaxTotalLog,
+            batch);
+    return false;
+  }
   Plan1D p;
   if (!make_plan(xdim, ydim * batch, choice, &p, err)) return false;  // the row FFTs
   if (logy > 0) {
@@ -428,6 +437,10 @@ bool make_plan_bluestein(long long n, long long batch, Plan1D* out, std::string*
   }
   if (batch < 1) {
     set_err(err, "batch must be >= 1 (got %lld)", batch);
+    return false;
+  }
+  if (batch > (1LL << kMaxTotalLog) / n) {
+    set_err(err, "n * batch must be at most 2^40 elements (got n = %lld, batch = %lld)", n, batch);
     return false;
   }
   const long long m = bluestein_m(n);

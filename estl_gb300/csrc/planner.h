@@ -102,6 +102,10 @@ constexpr int kTcSingleMaxLog = 13;  // split precision: larger n run four-step
 constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;
 constexpr int kThreePassDefaultLog = 23;  // default plans of N >= 2^23 (FP32) run three passes
+// At most 2^40 complex elements per plan (8 TiB, beyond any device memory;
+// the planner's messages quote the number):
+// keeps every 64-bit product of a length and a batch far from overflow.
+constexpr int kMaxTotalLog = 40;
 
 // Returns false (with *err set) when n is not a power of two in [1, 2^24] or
 // the choice names no instantiated kernel.

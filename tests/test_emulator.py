@@ -162,6 +162,20 @@ def test_rejects_bad_sizes(emu):
     assert rc == 2
 
 
+def test_rejects_totals_beyond_2e40(emu):
+    """n * batch above 2^40 elements is refused by the planner (no 64-bit
+    product of sizes can overflow); exactly 2^40 is planned."""
+    buf = ctypes.create_string_buffer(2048)
+    assert emu.emu_plan_describe(1 << 24, 1 << 17, None, buf, len(buf)) == 2 and b"2^40" in buf.value
+    assert emu.emu_plan_describe(1 << 24, 1 << 16, None, buf, len(buf)) == 0
+    assert emu.emu_plan_describe(16, (1 << 62) + 1, None, buf, len(buf)) == 2
+    z = np.zeros(4, np.complex64)
+    err = ctypes.create_string_buffer(512)
+    assert emu.emu_plan2d_run(1 << 10, 1 << 10, 1 << 21, -1, z.ctypes.data, z.ctypes.data, err, len(err)) == 2
+    assert emu.emu_bluestein_run(1000, 1 << 31, -1, z.ctypes.data, z.ctypes.data, err, len(err)) == 2
+    assert b"2^40" in err.value
+
+
 def test_twiddle_bank_accuracy(emu):
     """The bank holds w_{2^k}^j rounded once from higher precision."""
     size = emu.emu_bank(None)

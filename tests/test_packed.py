@@ -74,6 +74,7 @@ def test_layout_validation(emu):
         (np.array([0], np.int64), np.array([12], np.int64)),          # not a power of two
         (np.array([0], np.int64), np.array([1 << 19], np.int64)),     # too long
         (np.array([-4], np.int64), np.array([4], np.int64)),          # negative offset
+        (np.array([(1 << 62)], np.int64), np.array([4], np.int64)),   # offset beyond 2^40
     ]
     for off, sz in bad:
         rc, msg, _ = emu_packed(emu, off, sz, x, 1, -1)
