@@ -65,6 +65,11 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       if (err) *err = "request " + std::to_string(i) + ": lengths must be >= 1 and offsets >= 0";
       return false;
     }
+    const long long lim = 1LL << kMaxTotalLog;  // no sum of a length and an offset can overflow
+    if (q.signal_len > lim || q.filter_len > lim || q.sig_off > lim || q.filt_off > lim || q.out_off > lim) {
+      if (err) *err = "request " + std::to_string(i) + ": lengths and offsets must be at most 2^40";
+      return false;
+    }
     int logn = conv_logn(q.signal_len, q.filter_len);
     if (logn > kConvMaxLogN) {
       if (err) *err = "request " + std::to_string(i) + ": padded length exceeds 2^" + std::to_string(kConvMaxLogN);

@@ -298,3 +298,17 @@ def test_gpu_pairs(engine, flags):
     for L, K, so, fo, oo in reqs:
         ref = oracle.conv_fft(sig[so:so + L].astype(np.float64), filt[fo:fo + K].astype(np.float64))
         assert rel(out[oo:oo + L + K - 1], ref) < tol, (flags, L, K)
+
+
+def test_emulated_request_validation(emu):
+    """Requests are checked before any work: lengths >= 1, offsets >= 0,
+    lengths and offsets at most 2^40 (no 64-bit sum overflows), padded length
+    at most the supported maximum."""
+    z = np.zeros(8, np.float32)
+    err = ctypes.create_string_buffer(512)
+    bad = [(0, 4, 0, 0, 0), (8, 4, -1, 0, 0), ((1 << 62), 4, 0, 0, 0), (8, (1 << 62), 0, 0, 0),
+           (8, 4, 0, 0, (1 << 62)), ((1 << 30), 4, 0, 0, 0)]
+    for r in bad:
+        arr = np.array([r], dtype=np.int64).ravel()
+        rc = emu.emu_conv_run(arr.ctypes.data, 1, 0, 0, z.ctypes.data, z.ctypes.data, z.ctypes.data, err, len(err))
+        assert rc == 2 and err.value, r
