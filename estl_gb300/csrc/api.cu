@@ -719,7 +719,8 @@ estl_status estl_plan2d_create(int64_t xdim, int64_t ydim, int64_t batch, int di
     return fail(ESTL_INVALID_ARG, "direction must be ESTL_FORWARD (-1) or ESTL_BACKWARD (+1), got %d", direction);
   if (precision != ESTL_PREC_FP32) return fail(ESTL_INVALID_ARG, "2D transforms run in FP32 (precision %d)", precision);
   PlanChoice choice;
-  if (xdim > 0 && batch > 0 && ydim > 0) tuner_lookup(xdim, ydim * batch, &choice);  // the row FFTs' tuned plan
+  if (xdim > 0 && batch > 0 && ydim > 0 && batch <= (1LL << kMaxTotalLog) / ydim)
+    tuner_lookup(xdim, ydim * batch, &choice);  // the row FFTs' tuned plan
   std::unique_ptr<estl_plan_s> p(new estl_plan_s);
   std::string err;
   if (!make_plan2d(xdim, ydim, batch, choice, &p->layout, &err) &&
