@@ -126,7 +126,10 @@ const std::vector<cf32>& host_bank() {
 // thread order, or in reverse thread order (every odd CTA of a grid): a
 // shared-memory slot read in the same barrier interval in which another
 // thread writes it then holds the old value (or the NaN poison) in one of
-// the two orders, and the race fails the parity check.
+// the two orders, and the race fails the parity check.  In the bulk-load
+// kernels thread 0's copies complete at issue and the mbarrier waits return
+// at once: thread order then catches a copy that overwrites a stage other
+// threads still read, reverse order a read of a stage before its copy.
 struct FiberSched {
   std::vector<ucontext_t> ctx;
   std::vector<std::vector<char>> stacks;
@@ -180,10 +183,7 @@ void run_fibers(int nt, const std::function<void(int)>& body, bool reverse) {
 }
 
 template <class Fn, class Args>
-// reversible: the kernel's threads may run in either order between barriers
-// (false for kernels whose copies are issued by one thread and complete at
-// issue in the emulator, with the other threads' mbarrier waits returning at once)
-bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid, bool reversible = true) {
+bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
   // the device limit on dynamic shared memory per CTA (227 KB on sm_103a)
   if (smem_elems * (long long)sizeof(cf32) > 227LL * 1024) {
     std::lock_guard<std::mutex> g(g_msg_mu);
@@ -213,14 +213,12 @@ bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long g
         failed = true;
       }
     };
-    run_fibers(nt, body, reversible && (cta & 1));
+    run_fibers(nt, body, (cta & 1) != 0);
   }
   return !failed;
 }
 
-bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
-  return run_generic(k.nt, k.smem, k.fn, a, grid, k.pipe != 2);
-}
+bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) { return run_generic(k.nt, k.smem, k.fn, a, grid); }
 
 }  // namespace
 
