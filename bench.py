@@ -58,8 +58,11 @@ def compact_choice(c):
     """Short text form of an autotuner plan choice."""
     def r32(key):
         return " radix-32" if c.get(key, -1) == 5 else ""
+    if c["mode"] == 1 and c.get("single_cluster", -1) > 0:
+        return f"cluster of {1 << c['single_cluster']} CTAs, N2 2^{c['logn2']}, E 2^{c['single_loge']}"
     if c["mode"] == 1:
-        return f"single {c['single_loge']}.{c['single_logc']}{r32('single_logr')}"
+        pipe = {3: " resident", 4: " resident half-exchange"}.get(c.get("pipe", 0), "")
+        return f"single {c['single_loge']}.{c['single_logc']}{r32('single_logr')}{pipe}"
     if c["mode"] == 4:
         return f"three-pass R 2^{c['logn2']} Q 2^{c.get('logn3', -1)} chunk {c['chunk']} pipe {c['pipe']}"
     kind = "stream" if c["mode"] == 3 else "four-step"

@@ -72,7 +72,7 @@ class Plan:
     MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3, "three_pass": 4}
 
     TILE_FIELDS = ("split_log2", "single_loge", "single_logc", "col_loge", "col_logc", "row_loge", "row_logc",
-                   "pipelined", "split2_log2", "single_logr", "col_logr", "row_logr")
+                   "pipelined", "split2_log2", "single_logr", "col_logr", "row_logr", "single_cluster_log2")
 
     def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0, tiles=None):
         """tiles: optional dict of estl_plan_options tile fields (split_log2, col_loge, ...; modes

@@ -137,7 +137,7 @@ class PlanOptions(ctypes.Structure):
                 ("col_loge", ctypes.c_int), ("col_logc", ctypes.c_int),
                 ("row_loge", ctypes.c_int), ("row_logc", ctypes.c_int), ("pipelined", ctypes.c_int),
                 ("split2_log2", ctypes.c_int), ("single_logr", ctypes.c_int), ("col_logr", ctypes.c_int),
-                ("row_logr", ctypes.c_int)]
+                ("row_logr", ctypes.c_int), ("single_cluster_log2", ctypes.c_int)]
 
 
 class ConvRequest(ctypes.Structure):

@@ -141,7 +141,7 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
   for (size_t i = 0; i < kt.descs.size(); ++i) {
     const KernelDesc& d = kt.descs[i];
     if (d.kind == st.kind && d.logm == st.logm && d.loge == st.loge && d.logr == st.logr && d.logc == st.logc &&
-        d.pipe == pipe && d.tc == st.tc) {
+        d.pipe == pipe && d.tc == st.tc && d.cluster == st.cluster && d.csplit == st.csplit) {
       if (!kt.attr_set[i]) {
         std::lock_guard<std::mutex> g(g_attr_mu);
         if (!kt.attr_set[i]) {
@@ -149,6 +149,11 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
               cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem_bytes),
               "cudaFuncSetAttribute(max dynamic shared memory)");
           if (s != ESTL_OK) return s;
+          if (d.cluster > 3) {  // clusters of more than 8 CTAs are non-portable
+            s = check_cuda(cudaFuncSetAttribute(d.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                           "cudaFuncSetAttribute(non-portable cluster size)");
+            if (s != ESTL_OK) return s;
+          }
           int per_sm = 0;
           s = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, d.fn, d.nthreads, d.smem_bytes),
                          "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -167,13 +172,13 @@ static estl_status lookup_kernel(const Step& st, int pipe, const KernelDesc** ou
 }
 
 estl_status launch_pdl(const void* fn, long long grid, int threads, void** args, int smem, cudaStream_t stream,
-                       const char* what) {
+                       const char* what, int cluster) {
   // ESTL_NO_PDL=1 launches with plain stream serialisation
   static const bool pdl = [] {
     const char* e = std::getenv("ESTL_NO_PDL");
     return !(e && *e && *e != '0');
   }();
-  if (!pdl)
+  if (!pdl && !cluster)
     return check_cuda(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)threads), args, (size_t)smem, stream),
                       what);
   cudaLaunchConfig_t cfg = {};
@@ -181,11 +186,22 @@ estl_status launch_pdl(const void* fn, long long grid, int threads, void** args,
   cfg.blockDim = dim3((unsigned)threads);
   cfg.dynamicSmemBytes = (size_t)smem;
   cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
+  int na = 0;
+  if (pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  if (cluster) {  // cluster tiles: 2^cluster consecutive CTAs per cluster
+    attr[na].id = cudaLaunchAttributeClusterDimension;
+    attr[na].val.clusterDim.x = 1u << cluster;
+    attr[na].val.clusterDim.y = 1;
+    attr[na].val.clusterDim.z = 1;
+    ++na;
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = na;
   return check_cuda(cudaLaunchKernelExC(&cfg, fn, args), what);
 }
 
@@ -277,7 +293,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     // programmatic launch their three-pass chains ran 1-4% slower)
     s = pipe ? check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
                           "cudaLaunchKernel")
-             : launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx");
+             : launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx", d->cluster);
     if (s != ESTL_OK) return s;
   }
   return ESTL_OK;
@@ -653,6 +669,7 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
       choice.single_logr = opt->single_logr;
       choice.col_logr = opt->col_logr;
       choice.row_logr = opt->row_logr;
+      choice.single_cluster = opt->single_cluster_log2;
     }
   } else {
     if (precision == ESTL_PREC_FP32) tuner_lookup(n, batch, &choice);

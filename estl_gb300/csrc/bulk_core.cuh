@@ -37,6 +37,12 @@ namespace estl {
 
 constexpr long long kBulkSpinLimit = 1LL << 22;
 
+// Bit of the bulk-load kernels' error word (TileArgs::err) above the tile
+// number: a CTA gave up on a wait and its bounded drain of the copies it had
+// in flight also ran out, so those copies may still land in shared memory
+// that a later launch owns.  estl_plan_check then marks the plan unusable.
+constexpr long long kErrCopiesInFlight = 1LL << 62;
+
 #if defined(__CUDA_ARCH__)
 ESTL_HD uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 #endif
@@ -130,9 +136,10 @@ ESTL_HD bool cta_any(bool x) {
 ESTL_HD void bulk_give_up(const TileArgs& a, long long tile, int tid, uint64_t* bar, int s, long long k,
                           bool other_pending) {
   if (tid != 0) return;
-  if (a.err) atomic_max_ll(a.err, tile + 1);
-  mbar_wait(&bar[s], (uint32_t)((k >> 1) & 1));
-  if (other_pending) mbar_wait(&bar[s ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+  long long e = tile + 1;
+  if (!mbar_wait(&bar[s], (uint32_t)((k >> 1) & 1))) e |= kErrCopiesInFlight;
+  if (other_pending && !mbar_wait(&bar[s ^ 1], (uint32_t)(((k + 1) >> 1) & 1))) e |= kErrCopiesInFlight;
+  if (a.err) atomic_max_ll(a.err, e);
 }
 
 // Row pass of the four-step (as RowKernel: C rows k2_0.. of one transform's

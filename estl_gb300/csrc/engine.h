@@ -43,8 +43,9 @@ estl_status require_init();
 // Kernel launch with programmatic stream serialisation: the kernel (which
 // starts with pdl_enter) may be scheduled while the previous kernel of the
 // stream finishes its last wave.
+// cluster > 0: launched in clusters of 2^cluster consecutive CTAs.
 estl_status launch_pdl(const void* fn, long long grid, int threads, void** args, int smem, cudaStream_t stream,
-                       const char* what);
+                       const char* what, int cluster = 0);
 
 // Budgeted device allocation (counted against Engine::budget).
 estl_status dev_alloc(void** p, size_t bytes, const char* what);

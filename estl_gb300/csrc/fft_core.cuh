@@ -344,6 +344,7 @@ ESTL_HD void twiddle_apply(cf32* x, const Ptr<const cf32>& tw, int u) {
 template <int LOGM, int LOGE, int LOGR>
 struct Tile {
   static_assert(LOGE >= LOGR || LOGE >= LOGM, "elements per thread must cover a radix");
+  static constexpr int LM = LOGM, LE = LOGE;
   static constexpr int M = 1 << LOGM;
   static constexpr int LR_FULL = (LOGR < LOGM) ? LOGR : LOGM;
   static constexpr int E = 1 << LOGE;
@@ -476,6 +477,17 @@ struct is_persistent<K, decltype((void)K::PERSISTENT)> {
   static constexpr bool value = K::PERSISTENT;
 };
 
+// Cluster tiles (cluster_core.cuh): log2 of the CTAs per cluster and of the
+// column DFT length; 0 for every other kernel.
+template <class K, class = void>
+struct cluster_of {
+  static constexpr int log_cluster = 0, log_split = 0;
+};
+template <class K>
+struct cluster_of<K, decltype((void)K::LOG_CLUSTER)> {
+  static constexpr int log_cluster = K::LOG_CLUSTER, log_split = K::LOG_SPLIT;
+};
+
 // Keeps the compiler from hoisting every iteration's table loads to the top
 // of an unrolled epilogue (which costs 2 registers per load in flight).
 ESTL_HD void schedule_fence() {
@@ -578,6 +590,29 @@ struct SingleKernel {
   }
 };
 
+// Four-step twiddle of a column tile's outputs: y[k2] *= w_N^{n1 k2} for the
+// thread's outputs k2 = t + T*j (T = TL::T).  w_N^{n1 k2} = w_N^{n1 t} * W^j
+// with W = w_N^{n1 T} = w_{E N1}^{n1}: one two-level table lookup for the
+// base, four for W, W^2, W^4, W^8, and the other powers by products (instead
+// of a scattered two-level lookup per element).
+template <class TL>
+ESTL_HD void fourstep_twiddle(cf32 (&v)[TL::E], int n1, int t, int logn, const Ptr<const cf32>& bank) {
+  static_assert(TL::E == 16 || TL::E == 32, "column tiles hold 16 or 32 elements per thread");
+  const int logw = TL::LE + logn - TL::LM;  // W = w_{E N1}^{n1}, N1 = N / M
+  const cf32 base = twiddle_n(bank, logn, n1 * t);
+  const cf32 w1 = twiddle_n(bank, logw, n1), w2 = twiddle_n(bank, logw, 2 * n1);
+  const cf32 w4 = twiddle_n(bank, logw, 4 * n1), w8 = twiddle_n(bank, logw, 8 * n1);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = cmul(v[j], base);
+  apply_powers16(v, w1, w2, w4, w8);
+  if constexpr (TL::E == 32) {
+    const cf32 base16 = cmul(base, twiddle_n(bank, logw, 16 * n1));
+#pragma unroll
+    for (int j = 16; j < 32; ++j) v[j] = cmul(v[j], base16);
+    apply_powers16(v + 16, w1, w2, w4, w8);
+  }
+}
+
 // Four-step column pass: N = N1 * N2, x[n1 + N1 n2].  A CTA owns C adjacent
 // columns n1 of one transform and runs their N2-point DFTs (M = N2), then
 // multiplies by w_N^{n1 k2} and writes S[k2 * N1 + n1].  Thread mapping is
@@ -640,21 +675,8 @@ struct ColKernel {
   // scattered two-level lookup per element).
   ESTL_HD static void store_twiddled(cf32 (&v)[TL::E], const Ptr<cf32>& out, int n1, int t, int logn,
                                      const Ptr<const cf32>& bank, int ologr = 0) {
-    static_assert(TL::E == 16 || TL::E == 32, "column tiles hold 16 or 32 elements per thread");
     const int logn1 = logn - LOGM;
-    const int logq = LOGE + logn1;  // W = w_{2^logq}^{n1}
-    const cf32 base = twiddle_n(bank, logn, n1 * t);
-    const cf32 w1 = twiddle_n(bank, logq, n1), w2 = twiddle_n(bank, logq, 2 * n1);
-    const cf32 w4 = twiddle_n(bank, logq, 4 * n1), w8 = twiddle_n(bank, logq, 8 * n1);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) v[j] = cmul(v[j], base);
-    apply_powers16(v, w1, w2, w4, w8);
-    if constexpr (TL::E == 32) {
-      const cf32 base16 = cmul(base, twiddle_n(bank, logq, 16 * n1));
-#pragma unroll
-      for (int j = 16; j < 32; ++j) v[j] = cmul(v[j], base16);
-      apply_powers16(v + 16, w1, w2, w4, w8);
-    }
+    fourstep_twiddle<TL>(v, n1, t, logn, bank);
     const int oshift = logn1 + ologr;  // output row pitch: N1, or 2^ologr N1 (three-pass middle pass)
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) out[((t + TL::T * j) << oshift) + n1] = v[j];

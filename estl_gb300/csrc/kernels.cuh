@@ -7,6 +7,8 @@
 #include "fft_core.cuh"
 #include "bulk_core.cuh"
 #include "pipe_core.cuh"
+#include "resident_core.cuh"
+#include "cluster_core.cuh"
 
 namespace estl {
 
@@ -19,9 +21,12 @@ struct KernelDesc {
   int nthreads;
   int smem_bytes;
   const void* fn;
-  int pipe;  // 1: grid-stride cp.async double-buffered variant (pipe_core.cuh); 2: bulk-load ring (bulk_core.cuh)
+  int pipe;  // 1: grid-stride cp.async double-buffered variant (pipe_core.cuh); 2: bulk-load ring (bulk_core.cuh);
+             // 3 / 4: resident whole transforms with a whole / half exchange buffer (resident_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
   int tmap;  // launched with a 2D tensor map of its input as a second parameter (tma_tile_kernel)
+  int cluster = 0;  // cluster tiles (cluster_core.cuh): log2 CTAs per cluster
+  int csplit = 0;   // cluster tiles: log2 of the column DFT length N2
 };
 
 template <class K>
@@ -46,7 +51,8 @@ __global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) tma_tile_kernel(TileArgs
 template <class K>
 KernelDesc make_desc(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0) {
   return KernelDesc{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
-                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe, tc, 0};
+                    reinterpret_cast<const void*>(&tile_kernel<K>), pipe, tc, 0, cluster_of<K>::log_cluster,
+                    cluster_of<K>::log_split};
 }
 
 template <class K>
@@ -65,6 +71,8 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
 #define ESTL_BULK_ROW(M, E, R, C) make_desc<BulkRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 2)
 #define ESTL_BULK_COL(M, E, R, C) make_tma_desc<BulkColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
+#define ESTL_RES(M, E, R, H) make_desc<ResKernel<M, E, R, H>>(KIND_SINGLE, M, E, R, 0, 2 + H)
+#define ESTL_CLUSTER_TILE(N, LR, N2, E) make_desc<ClusterKernel<N, LR, N2, E>>(KIND_SINGLE, N, E, 4, 0)
 #define ESTL_COLUMN(M, E, C) make_desc<ColKernel<M, E, 4, C, false, false>>(KIND_COLUMN, M, E, 4, C)
 #define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
 #define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)

@@ -8,6 +8,8 @@
 #include "fft_core.cuh"
 #include "bulk_core.cuh"
 #include "pipe_core.cuh"
+#include "resident_core.cuh"
+#include "cluster_core.cuh"
 
 namespace estl {
 
@@ -15,7 +17,8 @@ namespace {
 
 template <class K>
 TileCfg cfg_of(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0) {
-  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32)), pipe, tc};
+  return TileCfg{kind, logm, loge, logr, logc, K::NT, (int)(K::SMEM_ELEMS * (int)sizeof(cf32)), pipe, tc,
+                 cluster_of<K>::log_cluster, cluster_of<K>::log_split};
 }
 
 std::vector<TileCfg> build_configs() {
@@ -28,6 +31,8 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) v.push_back(cfg_of<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_BULK_COL(M, E, R, C) v.push_back(cfg_of<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
+#define ESTL_X_RES(M, E, R, H) v.push_back(cfg_of<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));
+#define ESTL_X_CLUSTER(N, LR, N2, E) v.push_back(cfg_of<ClusterKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0));
 #define ESTL_X_COLUMN(M, E, C) v.push_back(cfg_of<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -54,7 +59,7 @@ const TileCfg* default_single(int logm) {
   const TileCfg* best = nullptr;
   const int want_e = logm >= 13 ? 5 : std::min(4, logm);
   for (const TileCfg& c : tile_configs()) {
-    if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe || c.tc) continue;
+    if (c.kind != STEP_SINGLE || c.logm != logm || c.pipe || c.tc || c.cluster) continue;
     if (c.loge != want_e) continue;
     if (!best || std::abs(c.nthreads - 256) < std::abs(best->nthreads - 256)) best = &c;
   }
@@ -95,11 +100,22 @@ const StreamCfg* find_stream_cfg(int logn) {
   return nullptr;
 }
 
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe, int tc) {
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe, int tc, int cluster,
+                         int csplit) {
   for (const TileCfg& c : tile_configs())
     if (c.kind == kind && c.logm == logm && c.loge == loge && c.logr == logr && c.logc == logc && c.pipe == pipe &&
-        c.tc == tc)
+        c.tc == tc && c.cluster == cluster && c.csplit == csplit)
       return &c;
+  return nullptr;
+}
+
+// Cluster tiles that single-kernel plans use by default (measured on a
+// GB300, 1 GiB batches): log2 N -> (log2 CTAs per cluster, log2 N2, log2 E).
+static const TileCfg* default_cluster(int logn) {
+  static const int tuned[][4] = {{0, 0, 0, 0}};
+  for (const auto& t : tuned)
+    if (t[0] == logn)
+      if (const TileCfg* c = find_tile(STEP_SINGLE, logn, t[3], 4, 0, 0, 0, t[1], t[2])) return c;
   return nullptr;
 }
 
@@ -117,7 +133,7 @@ static int lr_of(int logr) { return logr < 0 ? 4 : logr; }
 // Whether a step of this configuration runs as its pipelined variant.
 static int use_pipe(const PlanChoice& ch, const TileCfg* c) {
   if (ch.pipe == 0) return 0;
-  const int want = ch.pipe == 2 ? 2 : 1;
+  const int want = ch.pipe >= 2 ? ch.pipe : 1;
   return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, want) ? want : 0;
 }
 
@@ -188,7 +204,9 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     mode = 4;
     three_default = true;
   }
-  if (mode == 0) mode = (logn <= (tc ? kTcSingleMaxLog : kSingleMaxLog)) ? 1 : 2;
+  const bool cluster_default = mode == 0 && !tc && logn > kSingleMaxLog && choice.single_cluster < 0 &&
+                               default_cluster(logn) != nullptr;
+  if (mode == 0) mode = (logn <= (tc ? kTcSingleMaxLog : kSingleMaxLog) || cluster_default) ? 1 : 2;
 
   if (mode == 3) {
     const StreamCfg* sc = find_stream_cfg(logn);
@@ -275,6 +293,27 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
       p.steps.push_back(c);
     }
     p.hbm_passes = 3;
+    *out = p;
+    return true;
+  }
+
+  if (mode == 1 && !tc && (choice.single_cluster > 0 || cluster_default)) {
+    // one transform per thread-block cluster (cluster_core.cuh)
+    const TileCfg* c =
+        cluster_default
+            ? default_cluster(logn)
+            : find_tile(STEP_SINGLE, logn, choice.single_loge >= 0 ? choice.single_loge : 4, 4, 0, 0, 0,
+                        choice.single_cluster, choice.logn2);
+    if (!c) {
+      set_err(err, "no cluster tile instantiated for log2 n = %lld with 2^%lld CTAs per transform", logn,
+              choice.single_cluster);
+      return false;
+    }
+    Step s{STEP_SINGLE, logn, c->loge, c->logr, 0, batch << c->cluster, BUF_IN, BUF_OUT, 0, total, 0, total, batch, logn};
+    s.cluster = c->cluster;
+    s.csplit = c->csplit;
+    p.steps.push_back(s);
+    p.hbm_passes = 1;
     *out = p;
     return true;
   }
@@ -473,7 +512,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
   if (logn == 0) return out;
   if (logn <= kSingleMaxLog) {
     for (const TileCfg& c : tile_configs()) {
-      if (c.kind != STEP_SINGLE || c.logm != logn || c.tc) continue;
+      if (c.kind != STEP_SINGLE || c.logm != logn || c.tc || c.pipe >= 3 || c.cluster) continue;
       PlanChoice ch;
       ch.mode = 1;
       ch.single_loge = c.loge;
@@ -485,7 +524,22 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
         ch.pipe = 2;  // the same tile with bulk loads (persistent row tile, N2 = 1)
         out.push_back(ch);
       }
+      for (int rp : {3, 4})  // the same tile resident: next transform's copy under this one's passes
+        if (!c.pipe && c.logc == 0 && find_tile(STEP_SINGLE, logn, c.loge, c.logr, 0, rp)) {
+          ch.pipe = rp;
+          out.push_back(ch);
+        }
     }
+  }
+  for (const TileCfg& c : tile_configs()) {  // one transform per thread-block cluster
+    if (c.kind != STEP_SINGLE || c.logm != logn || !c.cluster) continue;
+    PlanChoice ch;
+    ch.mode = 1;
+    ch.single_loge = c.loge;
+    ch.single_logc = 0;
+    ch.single_cluster = c.cluster;
+    ch.logn2 = c.csplit;
+    out.push_back(ch);
   }
   if (find_stream_cfg(logn)) {
     for (int lag : {0, 1, 2, 4, 8}) {
@@ -561,8 +615,9 @@ std::string Plan1D::describe() const {
     const Step& st = steps[i];
     std::snprintf(buf, sizeof buf,
                   "%s{\"kind\": \"%s\", \"logm\": %d, \"loge\": %d, \"logc\": %d, \"tiles\": %lld, \"pipe\": %d, "
-                  "\"tc\": %d}",
-                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe, st.tc);
+                  "\"tc\": %d, \"cluster\": %d, \"csplit\": %d}",
+                  shown ? ", " : "", names[st.kind], st.logm, st.loge, st.logc, st.grid, st.pipe, st.tc, st.cluster,
+                  st.csplit);
     s += buf;
     ++shown;
   }

@@ -29,11 +29,14 @@ struct TileCfg {
   int smem_bytes;
   int pipe;  // pipelined (grid-stride, cp.async double-buffered) variant
   int tc;    // radix-16 passes on the tensor cores (split precision)
+  int cluster = 0;  // cluster tiles (cluster_core.cuh): log2 CTAs per cluster, 0 otherwise
+  int csplit = 0;   // cluster tiles: log2 of the column DFT length N2
 };
 
 // All instantiated tile kernels (kernel_list.inc).
 const std::vector<TileCfg>& tile_configs();
-const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0);
+const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe = 0, int tc = 0, int cluster = 0,
+                         int csplit = 0);
 
 struct Step {
   int kind;
@@ -57,6 +60,10 @@ struct Step {
   // transform f = b * 2^ologr + k3 stores column output k2 at
   // b * N + k3 * N1 + k2 * 2^ologr * N1 (N1 = 2^(logn - logm)).
   int ologr = 0;
+  // STEP_SINGLE on a cluster tile: log2 CTAs per transform (the grid is
+  // rows * 2^cluster CTAs, launched in clusters of 2^cluster) and log2 of its
+  // column DFT length
+  int cluster = 0, csplit = 0;
 };
 
 // Streamed four-step configuration of a length (stream_list.inc), or nullptr.
@@ -81,6 +88,10 @@ struct PlanChoice {
   // log2 of the largest radix of the single / column / row tiles (-1 = 4:
   // radix 16; 5: radix-32 passes, 32 elements per thread)
   int single_logr = -1, col_logr = -1, row_logr = -1;
+  // single-kernel plans: log2 CTAs per transform of a cluster tile
+  // (cluster_core.cuh; its column DFT length in logn2), 0 = one CTA per
+  // transform, -1 = planner default
+  int single_cluster = -1;
 };
 
 struct Plan1D {
@@ -98,6 +109,7 @@ struct Plan1D {
 };
 
 constexpr int kSingleMaxLog = 14;
+constexpr int kClusterMaxLog = 17;  // single-pass plans on cluster tiles: up to 2^17 points
 constexpr int kTcSingleMaxLog = 13;  // split precision: larger n run four-step
 constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;

@@ -70,13 +70,13 @@ std::string tuner_cache_path() {
 }
 
 std::string choice_to_json(const PlanChoice& c) {
-  char buf[400];
+  char buf[448];
   std::snprintf(buf, sizeof buf,
                 "{\"mode\": %d, \"single_loge\": %d, \"single_logc\": %d, \"logn2\": %d, \"col_loge\": %d, "
                 "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"lag\": %d, \"pipe\": %d, "
-                "\"logn3\": %d, \"single_logr\": %d, \"col_logr\": %d, \"row_logr\": %d}",
+                "\"logn3\": %d, \"single_logr\": %d, \"col_logr\": %d, \"row_logr\": %d, \"single_cluster\": %d}",
                 c.mode, c.single_loge, c.single_logc, c.logn2, c.col_loge, c.col_logc, c.row_loge, c.row_logc, c.chunk,
-                c.lag, c.pipe, c.logn3, c.single_logr, c.col_logr, c.row_logr);
+                c.lag, c.pipe, c.logn3, c.single_logr, c.col_logr, c.row_logr, c.single_cluster);
   return buf;
 }
 
@@ -107,6 +107,7 @@ void tuner_load_cache() {
     e.choice.single_logr = (int)json_int(line, "single_logr", -1);
     e.choice.col_logr = (int)json_int(line, "col_logr", -1);
     e.choice.row_logr = (int)json_int(line, "row_logr", -1);
+    e.choice.single_cluster = (int)json_int(line, "single_cluster", -1);
     g_cache[{gpu, n, bb}] = e;  // later lines win
   }
 }

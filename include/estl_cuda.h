@@ -120,6 +120,12 @@ typedef struct estl_plan_options {
   int pipelined;
   int split2_log2;
   int single_logr, col_logr, row_logr;
+  /* single-kernel plans (mode 1): > 0 runs one transform per thread-block
+   * cluster of 2^single_cluster_log2 CTAs whose four-step transpose goes
+   * through distributed shared memory, with column DFTs of 2^split_log2
+   * points (one HBM pass up to 2^17 points); 0 = one CTA per transform,
+   * -1 = planner's choice */
+  int single_cluster_log2;
 } estl_plan_options;
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
@@ -225,8 +231,10 @@ estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* result_json
  * device, and hosts that forbid device allocation in plugin calls.  This
  * entry point has no counterpart in the reference.
  *
- * Runs `batch` transforms of length n with the four-step column and row
- * kernels of estl_execute, but keeps their scratch in one fixed device array
+ * Runs `batch` transforms of length n with four-step column and row kernels
+ * (the plain tiles of estl_execute's tile shapes, which have no device-side
+ * waits; estl_execute runs bulk-load variants of them at 2^16..2^22 and is
+ * faster there), but keeps their scratch in one fixed device array
  * of 2^22 complex64 (32 MiB) and uses its own 4.4 MB twiddle table; every GPU
  * that loads this library holds both until the process exits.  Needs neither
  * estl_init nor a plan and allocates nothing (no cudaMalloc, cudaFree or
@@ -236,7 +244,8 @@ estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* result_json
  *    ESTL_UNSUPPORTED_SIZE (estl_execute handles them).
  *  - The first call on a device resolves the arrays' device addresses and
  *    fills the twiddle table, synchronising `stream`; make that first call
- *    before any stream capture.
+ *    before any stream capture.  The same set-up runs again on the first call
+ *    after the device's context changed (cudaDeviceReset).
  *  - All calls share the array and leave their last contents in it; nothing
  *    in it needs to start at zero.  Calls whose work overlaps on the GPU
  *    (unordered streams, or several threads) race on it: order them. */

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -28,6 +29,8 @@
 #include "conv2d_core.cuh"
 #include "estl_cuda.h"
 #include "pipe_core.cuh"
+#include "resident_core.cuh"
+#include "cluster_core.cuh"
 #include "stream_core.cuh"
 #include "planner.h"
 
@@ -63,11 +66,13 @@ struct EmuKernel {
   RunFn fn;
   int pipe;
   int tc;
+  int cluster, csplit;  // cluster tiles: log2 CTAs per cluster, log2 column DFT length
 };
 
 template <class K>
 EmuKernel mk(int kind, int m, int e, int r, int c, int pipe = 0, int tc = 0) {
-  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, pipe, tc};
+  return EmuKernel{kind, m, e, r, c, K::NT, K::SMEM_ELEMS, &K::run, pipe, tc, cluster_of<K>::log_cluster,
+                   cluster_of<K>::log_split};
 }
 
 const std::vector<EmuKernel>& emu_kernels() {
@@ -81,6 +86,8 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) k.push_back(mk<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_BULK_COL(M, E, R, C) k.push_back(mk<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
+#define ESTL_X_RES(M, E, R, H) k.push_back(mk<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));
+#define ESTL_X_CLUSTER(N, LR, N2, E) k.push_back(mk<ClusterKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0));
 #define ESTL_X_COLUMN(M, E, C) k.push_back(mk<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -119,113 +126,185 @@ const std::vector<cf32>& host_bank() {
   return b;
 }
 
-// The threads of one emulated CTA are fibers (ucontext coroutines) on the
-// calling host thread: a barrier is a yield to a round-robin scheduler that
-// resumes every fiber once per round, so all fibers reach each barrier before
-// any passes it.  No OS threads, no futexes.  A round runs the fibers in
-// thread order, or in reverse thread order (every odd CTA of a grid): a
-// shared-memory slot read in the same barrier interval in which another
-// thread writes it then holds the old value (or the NaN poison) in one of
-// the two orders, and the race fails the parity check.  In the bulk-load
-// kernels thread 0's copies complete at issue and the mbarrier waits return
-// at once: thread order then catches a copy that overwrites a stage other
-// threads still read, reverse order a read of a stage before its copy.
+// The threads of one emulated CTA (or of the CTAs of one cluster) are fibers
+// (ucontext coroutines) on the calling host thread: a barrier is a yield to a
+// scheduler that resumes every fiber that is not waiting, so all fibers reach
+// each barrier before any passes it.  No OS threads, no futexes.  A round
+// runs the fibers in thread order, or in reverse thread order (every odd CTA
+// or cluster of a grid): a shared-memory slot read in the same barrier
+// interval in which another thread writes it then holds the old value (or the
+// NaN poison) in one of the two orders, and the race fails the parity check.
+// In the bulk-load kernels thread 0's copies complete at issue and the
+// mbarrier waits return at once: thread order then catches a copy that
+// overwrites a stage other threads still read, reverse order a read of a
+// stage before its copy.
+//
+// Clusters: __syncthreads releases the fibers of one CTA, a cluster barrier
+// those of every CTA of the cluster.  Each CTA runs on its own as far as it
+// can (lowest rank first, or highest first in reverse order) before the next
+// CTA runs at all, so a read of another CTA's shared memory that is not
+// ordered by a cluster barrier sees the poison in one of the two orders.  A
+// CTA whose threads wait at different kinds of barrier is reported.
+enum FiberState : char { F_RUN = 0, F_AT_CTA = 1, F_AT_CLUSTER = 2, F_DONE = 3 };
 struct FiberSched {
   std::vector<ucontext_t> ctx;
-  std::vector<std::vector<char>> stacks;
-  std::vector<char> done;
+  // not value-initialised: pages a fiber never touches are never committed
+  std::vector<std::unique_ptr<char[]>> stacks;
+  std::vector<char> state;
   ucontext_t main;
   int current = 0;
   const std::function<void(int)>* body = nullptr;
 };
 thread_local FiberSched* tl_sched = nullptr;
 constexpr size_t kFiberStack = 256 * 1024;
+// shared memory of the CTAs of the emulated cluster (estl_emu_cluster_smem)
+thread_local std::vector<cf32*>* tl_cluster_smem = nullptr;
+thread_local long long tl_cluster_smem_elems = 0;
 
 void fiber_entry() {
   FiberSched* s = tl_sched;
-  const int tid = s->current;
-  (*s->body)(tid);
-  s->done[tid] = 1;
+  const int f = s->current;
+  (*s->body)(f);
+  s->state[f] = F_DONE;
   // returning resumes uc_link (the scheduler)
 }
 
-void run_fibers(int nt, const std::function<void(int)>& body, bool reverse) {
+// Runs ncta * nt fibers; fiber f is thread f % nt of CTA f / nt.  Returns
+// false if the fibers deadlocked on mismatched barriers.
+bool run_fibers(int nt, const std::function<void(int)>& body, bool reverse, int ncta = 1) {
   static thread_local FiberSched sched;
   FiberSched& s = sched;
-  if ((int)s.stacks.size() < nt) {
-    s.stacks.resize(nt);
+  const int total = nt * ncta;
+  if ((int)s.stacks.size() < total) {
+    s.stacks.resize(total);
     for (auto& st : s.stacks)
-      if (st.empty()) st.resize(kFiberStack);
+      if (!st) st.reset(new char[kFiberStack]);
   }
-  s.ctx.assign(nt, ucontext_t{});
-  s.done.assign(nt, 0);
+  s.ctx.assign(total, ucontext_t{});
+  s.state.assign(total, F_RUN);
   s.body = &body;
   tl_sched = &s;
-  for (int t = 0; t < nt; ++t) {
-    getcontext(&s.ctx[t]);
-    s.ctx[t].uc_stack.ss_sp = s.stacks[t].data();
-    s.ctx[t].uc_stack.ss_size = kFiberStack;
-    s.ctx[t].uc_link = &s.main;
-    makecontext(&s.ctx[t], fiber_entry, 0);
+  for (int f = 0; f < total; ++f) {
+    getcontext(&s.ctx[f]);
+    s.ctx[f].uc_stack.ss_sp = s.stacks[f].get();
+    s.ctx[f].uc_stack.ss_size = kFiberStack;
+    s.ctx[f].uc_link = &s.main;
+    makecontext(&s.ctx[f], fiber_entry, 0);
   }
+  bool ok = true;
   for (;;) {
-    bool any = false;
-    for (int i = 0; i < nt; ++i) {
-      const int t = reverse ? nt - 1 - i : i;
-      if (s.done[t]) continue;
-      any = true;
-      s.current = t;
-      swapcontext(&s.main, &s.ctx[t]);
+    for (int ci = 0; ci < ncta; ++ci) {
+      const int cta = reverse ? ncta - 1 - ci : ci;
+      for (;;) {  // this CTA until its fibers wait at a cluster barrier or finish
+        for (int i = 0; i < nt; ++i) {
+          const int f = cta * nt + (reverse ? nt - 1 - i : i);
+          if (s.state[f] != F_RUN) continue;
+          s.current = f;
+          swapcontext(&s.main, &s.ctx[f]);
+        }
+        int at_cta = 0, other = 0;
+        for (int t = 0; t < nt; ++t) {
+          const char st = s.state[cta * nt + t];
+          if (st == F_AT_CTA) at_cta++;
+          else if (st != F_DONE) other++;
+        }
+        if (at_cta && !other) {
+          for (int t = 0; t < nt; ++t)
+            if (s.state[cta * nt + t] == F_AT_CTA) s.state[cta * nt + t] = F_RUN;
+          continue;
+        }
+        break;
+      }
     }
-    if (!any) break;
+    int at_cluster = 0, at_cta = 0, done = 0;
+    for (int f = 0; f < total; ++f) {
+      if (s.state[f] == F_AT_CLUSTER) at_cluster++;
+      else if (s.state[f] == F_AT_CTA) at_cta++;
+      else if (s.state[f] == F_DONE) done++;
+    }
+    if (done == total) break;
+    if (at_cluster && !at_cta && at_cluster + done == total) {
+      for (int f = 0; f < total; ++f)
+        if (s.state[f] == F_AT_CLUSTER) s.state[f] = F_RUN;
+      continue;
+    }
+    ok = false;  // mismatched barriers: nothing can run
+    break;
   }
   tl_sched = nullptr;
+  return ok;
 }
 
 template <class Fn, class Args>
-bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid) {
+bool run_generic(int nt, long long smem_elems, Fn fn, const Args& a, long long grid, int ncta = 1) {
   // the device limit on dynamic shared memory per CTA (227 KB on sm_103a)
   if (smem_elems * (long long)sizeof(cf32) > 227LL * 1024) {
     std::lock_guard<std::mutex> g(g_msg_mu);
     if (g_msg.empty()) g_msg = "kernel needs " + std::to_string(smem_elems * sizeof(cf32)) + " bytes of shared memory";
     return false;
   }
-  // shared memory base 256-byte aligned, like the device's dynamic shared memory
-  std::vector<cf32> smem_store((size_t)std::max<long long>(smem_elems, 1) + 32);
-  cf32* smem_base = reinterpret_cast<cf32*>(((uintptr_t)smem_store.data() + 255) & ~(uintptr_t)255);
-  struct View {
-    cf32* p;
-    size_t n;
-    cf32* begin() { return p; }
-    cf32* end() { return p + n; }
-    cf32* data() { return p; }
-  } smem{smem_base, (size_t)std::max<long long>(smem_elems, 1)};
+  if (ncta < 1 || grid % ncta) {
+    std::lock_guard<std::mutex> g(g_msg_mu);
+    if (g_msg.empty()) g_msg = "grid is not a whole number of clusters";
+    return false;
+  }
+  // shared memory bases 256-byte aligned, like the device's dynamic shared memory
+  const size_t elems = (size_t)std::max<long long>(smem_elems, 1);
+  std::vector<std::vector<cf32>> stores(ncta, std::vector<cf32>(elems + 32));
+  std::vector<cf32*> bases(ncta);
+  for (int r = 0; r < ncta; ++r)
+    bases[r] = reinterpret_cast<cf32*>(((uintptr_t)stores[r].data() + 255) & ~(uintptr_t)255);
   const float nan = std::numeric_limits<float>::quiet_NaN();
   bool failed = false;
-  for (long long cta = 0; cta < grid && !failed; ++cta) {
+  tl_cluster_smem = &bases;
+  tl_cluster_smem_elems = (long long)elems;
+  for (long long cl = 0; cl < grid / ncta && !failed; ++cl) {
     // poison shared memory so that a read of a slot this CTA never wrote
     // shows up as NaN in the output
-    for (auto& e : smem) e = cf32{nan, nan};
-    std::function<void(int)> body = [&](int tid) {
+    for (cf32* b : bases)
+      for (size_t e = 0; e < elems; ++e) b[e] = cf32{nan, nan};
+    std::function<void(int)> body = [&](int f) {
+      const int r = f / nt, tid = f % nt;
       try {
-        fn(a, cta, tid, smem.data());
+        fn(a, cl * ncta + r, tid, bases[r]);
       } catch (const EmuFault&) {
         failed = true;
       }
     };
-    run_fibers(nt, body, (cta & 1) != 0);
+    if (!run_fibers(nt, body, (cl & 1) != 0, ncta)) {
+      std::lock_guard<std::mutex> g(g_msg_mu);
+      if (g_msg.empty()) g_msg = "threads wait at mismatched barriers (deadlock)";
+      failed = true;
+    }
   }
+  tl_cluster_smem = nullptr;
   return !failed;
 }
 
-bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) { return run_generic(k.nt, k.smem, k.fn, a, grid); }
+bool run_kernel(const EmuKernel& k, const TileArgs& a, long long grid) {
+  return run_generic(k.nt, k.smem, k.fn, a, grid, 1 << k.cluster);
+}
 
 }  // namespace
 
-// __syncthreads of an emulated thread: yield to the CTA's scheduler.
+// __syncthreads of an emulated thread: wait for the other threads of its CTA.
 void estl_emu_sync() {
   FiberSched* s = tl_sched;
+  s->state[s->current] = F_AT_CTA;
   swapcontext(&s->ctx[s->current], &s->main);
+}
+
+// Cluster barrier: wait for every thread of every CTA of the cluster.
+void estl_emu_cluster_sync() {
+  FiberSched* s = tl_sched;
+  s->state[s->current] = F_AT_CLUSTER;
+  swapcontext(&s->ctx[s->current], &s->main);
+}
+
+cf32* estl_emu_cluster_smem(int rank, long long* n) {
+  if (!tl_cluster_smem || rank < 0 || rank >= (int)tl_cluster_smem->size()) estl_emu_fail("cluster rank", rank, 0);
+  *n = tl_cluster_smem_elems;
+  return (*tl_cluster_smem)[rank];
 }
 
 namespace {
@@ -332,6 +411,7 @@ PlanChoice choice_from(const int* f) {
   c.single_logr = f[13];
   c.col_logr = f[14];
   c.row_logr = f[15];
+  c.single_cluster = f[16];
   return c;
 }
 
@@ -516,7 +596,7 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
     const EmuKernel* k = nullptr;
     for (const EmuKernel& c : emu_kernels())
       if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc &&
-          c.pipe == st.pipe && c.tc == st.tc)
+          c.pipe == st.pipe && c.tc == st.tc && c.cluster == st.cluster && c.csplit == st.csplit)
         k = &c;
     if (!k) {
       set_err(err, errlen, "no emulated kernel for a plan step");
@@ -547,6 +627,36 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
   return 0;
 }
 
+// Self-test of the cluster scheduling: each CTA of a cluster of `ncta` writes
+// its rank into its own shared memory, synchronises (a cluster barrier when
+// cluster_barrier != 0, else only __syncthreads, which does not order another
+// CTA's writes) and reads its neighbour's slot.  Returns the number of reads
+// that saw the neighbour's value in the worse of the two scheduling orders:
+// ncta * nt with the cluster barrier; fewer without it.
+int emu_cluster_barrier_selftest(int ncta, int nt, int cluster_barrier) {
+  // two clusters: the first runs in forward order, the second in reverse
+  std::vector<int> seen(2 * ncta * nt, 0);
+  auto body = [&](const int& cb, long long cta, int tid, cf32* sm) {
+    const int rank = (int)(cta % ncta);
+    sm[tid] = cf32{(float)rank, 0.f};
+    if (cb) estl_emu_cluster_sync();
+    else estl_emu_sync();
+    const int peer = (rank + 1) % ncta;
+    const cf32 v = peer_buf(sm, nt, rank, peer)[tid];
+    seen[cta * nt + tid] = v.x == (float)peer;
+    if (cb) estl_emu_cluster_sync();
+    else estl_emu_sync();
+  };
+  if (!run_generic(nt, nt, body, cluster_barrier, 2LL * ncta, ncta)) return -1;
+  int worst = ncta * nt;
+  for (int cl = 0; cl < 2; ++cl) {
+    int ok = 0;
+    for (int i = 0; i < ncta * nt; ++i) ok += seen[cl * ncta * nt + i];
+    worst = std::min(worst, ok);
+  }
+  return worst;
+}
+
 // Plan description (JSON) for (n, batch, choice); returns 0 or 2.
 int emu_plan_describe(long long n, long long batch, const int* choice, char* buf, int len) {
   Plan1D p;
@@ -566,7 +676,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
   int k = 0;
   for (const PlanChoice& ch : c) {
     if (k >= max) break;
-    int* f = out + 16 * k++;
+    int* f = out + 17 * k++;
     f[0] = ch.mode;
     f[1] = ch.single_loge;
     f[2] = ch.single_logc;
@@ -583,6 +693,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[13] = ch.single_logr;
     f[14] = ch.col_logr;
     f[15] = ch.row_logr;
+    f[16] = ch.single_cluster;
   }
   return (int)c.size();
 }

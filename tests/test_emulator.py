@@ -27,12 +27,13 @@ def pad_choice(choice):
     col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available),
     split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes),
     logn3 (three-pass: log2 of the second column DFT length, 0 = default),
-    single_logr, col_logr, row_logr (log2 largest radix, -1 = 16)."""
+    single_logr, col_logr, row_logr (log2 largest radix, -1 = 16),
+    single_cluster (log2 CTAs per transform of a cluster tile, -1 = default)."""
     c = list(choice)
     if len(c) < 13:
         c += [0] * (13 - len(c))
-    if len(c) < 16:
-        c += [-1] * (16 - len(c))
+    if len(c) < 17:
+        c += [-1] * (17 - len(c))
     return c
 
 
@@ -41,20 +42,20 @@ def emu_run(emu, n, batch, x, sign=-1, choice=None):
     err = ctypes.create_string_buffer(512)
     ch = None
     if choice is not None:
-        ch = (ctypes.c_int * 16)(*pad_choice(choice))
+        ch = (ctypes.c_int * 17)(*pad_choice(choice))
     rc = emu.emu_plan_run(n, batch, ch, sign, x.ctypes.data, y.ctypes.data, err, len(err))
     return rc, err.value.decode(), y
 
 
 def candidates(emu, n, batch):
-    buf = (ctypes.c_int * (16 * 4096))()
+    buf = (ctypes.c_int * (17 * 4096))()
     k = emu.emu_plan_candidates(n, batch, buf, 4096)
-    return [list(buf[16 * i: 16 * i + 16]) for i in range(min(k, 4096))]
+    return [list(buf[17 * i: 17 * i + 17]) for i in range(min(k, 4096))]
 
 
 def describe(emu, n, batch, choice=None):
     buf = ctypes.create_string_buffer(2048)
-    ch = (ctypes.c_int * 16)(*pad_choice(choice)) if choice is not None else None
+    ch = (ctypes.c_int * 17)(*pad_choice(choice)) if choice is not None else None
     rc = emu.emu_plan_describe(n, batch, ch, buf, len(buf))
     assert rc == 0, buf.value
     return json.loads(buf.value.decode())
@@ -252,3 +253,34 @@ def test_exhaustive_small_sizes_and_batches(emu, logn):
             rc, msg, y = emu_run(emu, n, batch, x, sign)
             assert rc == 0, (n, batch, msg)
             assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL, (n, batch, sign)
+
+
+def cluster_candidates(emu, n):
+    return [c for c in candidates(emu, n, 2) if c[0] == 1 and c[16] > 0]
+
+
+def test_cluster_scheduler_orders_distributed_shared_memory(emu):
+    """The emulated cluster barrier orders another CTA's shared-memory writes
+    before this CTA's reads; __syncthreads alone does not (in one of the two
+    scheduling orders the neighbour's slot still holds the poison)."""
+    for ncta in (2, 4, 8):
+        assert emu.emu_cluster_barrier_selftest(ncta, 64, 1) == ncta * 64
+        assert emu.emu_cluster_barrier_selftest(ncta, 64, 0) < ncta * 64
+
+
+@pytest.mark.parametrize("logn", range(13, 18))
+def test_cluster_tiles(emu, logn):
+    """Every cluster tile (one transform per thread-block cluster, the
+    four-step transpose through distributed shared memory), both directions,
+    two transforms (two clusters: forward and reverse scheduling order)."""
+    n = 1 << logn
+    cands = cluster_candidates(emu, n)
+    assert cands, "no cluster tiles"
+    x = rand_c64((2, n), 50 + logn)
+    for c in cands:
+        for sign in (-1, +1):
+            rc, msg, y = emu_run(emu, n, 2, x, sign, c)
+            assert rc == 0, (c, msg)
+            assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < (TOL if n <= 1 << 20 else 1e-5), c
+        d = describe(emu, n, 2, c)
+        assert d["hbm_passes"] == 1 and d["kernels"][0]["cluster"] == c[16]

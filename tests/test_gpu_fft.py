@@ -362,6 +362,50 @@ def test_bulk_single_tiles(engine, logn, logr):
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
 
 
+@pytest.mark.parametrize("logn,loge,logr,rounds", [(12, 4, 4, 1), (13, 4, 4, 1), (13, 4, 4, 2), (13, 5, 5, 1),
+                                                   (13, 5, 5, 2), (14, 4, 4, 2), (14, 5, 5, 2), (14, 5, 4, 2)])
+def test_resident_single_tiles(engine, logn, loge, logr, rounds):
+    """Whole transforms on the persistent resident tiles (resident_core.cuh:
+    the next transform's bulk copy overlaps this one's passes; exchanges in a
+    whole or half tile), both directions, against the oracle.  The batch is
+    not a multiple of the grid, so CTAs run different tile counts."""
+    import torch
+    n = 1 << logn
+    x = uniform_c64(((1 << 23) // n + 3, n), 1400 + logn + 10 * rounds)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, x.shape[0], direction, mode="single",
+                        tiles={"single_loge": loge, "single_logc": 0, "single_logr": logr, "pipelined": 2 + rounds})
+        d = p.describe()
+        assert d["kernels"][0]["kind"] == "single" and d["kernels"][0]["pipe"] == 2 + rounds
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
+CLUSTER_TILES = [(13, 1, 7, 4), (14, 1, 7, 4), (14, 2, 7, 4), (14, 1, 7, 5), (15, 2, 7, 4), (15, 2, 8, 4),
+                 (15, 3, 8, 4), (15, 2, 8, 5), (16, 3, 8, 4), (16, 3, 8, 5), (17, 4, 8, 4)]
+
+
+@pytest.mark.parametrize("logn,lcl,logn2,loge", CLUSTER_TILES)
+def test_cluster_tiles(engine, logn, lcl, logn2, loge):
+    """One transform per thread-block cluster of 2^lcl CTAs (cluster_core.cuh:
+    column DFTs, the four-step transpose through distributed shared memory,
+    row DFTs; one HBM pass), both directions, against the oracle."""
+    import torch
+    n = 1 << logn
+    x = uniform_c64(((1 << 23) // n + 1, n), 1500 + logn + lcl)
+    xd = torch.from_numpy(x).cuda()
+    for direction in (-1, +1):
+        p = engine.Plan(n, x.shape[0], direction, mode="single",
+                        tiles={"single_loge": loge, "single_cluster_log2": lcl, "split_log2": logn2})
+        d = p.describe()
+        assert d["hbm_passes"] == 1 and d["kernels"][0]["cluster"] == lcl
+        y = p.execute(xd)
+        p.check()
+        assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
+
+
 @pytest.mark.parametrize("n,batch", [(4096, 4 * 2048 + 5), (1 << 18, 4 * 32 + 7), (1 << 13, 4 * 1024)])
 def test_execute_host_ramped_chunks(engine, n, batch):
     """Host pipelines long enough for the opening and closing ramp of smaller
