@@ -13,31 +13,42 @@
 //   phase A  CTA r owns the W = N1 / R adjacent columns n1 = r W + c: loads
 //            x[n1 + N1 n2] (runs of W complex), N2-point column DFTs (radix
 //            passes, exchanges in its own shared memory), twiddle
-//            w_N^{n1 k2}, writes Z[k2][c] into its own shared memory
-//   cluster barrier
+//            w_N^{n1 k2}, writes Z[c][k2] into its own shared memory
+//   cluster barrier (arrive with release, then the gather of the columns
+//            this CTA holds itself, then wait)
 //            CTA r gathers rows k2 = r H + c' (H = N2 / R) of all N1 columns:
-//            column n1 of row k2 lives in CTA n1 / W at Z[k2][n1 mod W]
-//   cluster barrier (every gather is done: Z may be reused)
-//   phase B  N1-point row DFTs, stores X[k2 + N2 k1] (runs of H complex)
+//            column n1 of row k2 lives in CTA n1 / W at Z[n1 mod W][k2]
+//   phase B  first radix pass in registers (it consumes every gathered
+//            value), cluster barrier (relaxed arrive: every read of a peer's
+//            Z has delivered its value; Z may be reused), the other passes,
+//            stores X[k2 + N2 k1] (runs of H complex)
 //
 // Remote traffic per element: (R - 1) / R of the data crosses CTAs once, 8 B
 // per element read through distributed shared memory; HBM traffic is the
-// compulsory 16 B per element.  Z rows are padded to W + 1 elements so that a
-// warp gathering down one column (lanes = consecutive rows) is conflict-free.
+// compulsory 16 B per element.  A warp's gather reads 32 consecutive k2 of one
+// column: one contiguous 256-byte run of the remote CTA's shared memory (the
+// same gather with lanes 8 B apart in scattered rows ran 3x slower).  Z rows
+// are padded to N2 + 1 elements so that phase A's writes (lanes = adjacent
+// columns, one row apart) are free of bank conflicts.
 #pragma once
 #include "bulk_core.cuh"
 
+// Cluster barrier, split into its arrive and its wait.  ESTL_CLUSTER_ARRIVE
+// releases this thread's earlier writes to the cluster; the relaxed form
+// orders nothing and is used only where every earlier read has delivered its
+// value into a register that later work has already consumed.
 #ifdef ESTL_EMU
-void estl_emu_cluster_sync();
+void estl_emu_cluster_arrive();
+void estl_emu_cluster_wait();
 // Shared memory of CTA `rank` of the emulated cluster; *n = its elements.
 estl::cf32* estl_emu_cluster_smem(int rank, long long* n);
-#define ESTL_CLUSTER_SYNC() estl_emu_cluster_sync()
+#define ESTL_CLUSTER_ARRIVE() estl_emu_cluster_arrive()
+#define ESTL_CLUSTER_ARRIVE_RELAXED() estl_emu_cluster_arrive()
+#define ESTL_CLUSTER_WAIT() estl_emu_cluster_wait()
 #else
-#define ESTL_CLUSTER_SYNC()                                                      \
-  do {                                                                           \
-    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");     \
-    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");       \
-  } while (0)
+#define ESTL_CLUSTER_ARRIVE() asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory")
+#define ESTL_CLUSTER_ARRIVE_RELAXED() asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory")
+#define ESTL_CLUSTER_WAIT() asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory")
 #endif
 
 namespace estl {
@@ -97,8 +108,8 @@ struct ClusterKernel {
   using TA = Tile<LOGN2, LOGE, 4>;                          // column DFTs (N2 points)
   using TB = Tile<LOGN1, LOGE, 4>;                          // row DFTs (N1 points)
   static constexpr int NT = TA::T * W;
-  static constexpr int ZS = W + 1;  // Z row stride
-  static constexpr int XA = TA::MP * W, XB = TB::MP * H, ZE = N2 * ZS;
+  static constexpr int ZS = N2 + 1;  // Z row stride (one row per column c)
+  static constexpr int XA = TA::MP * W, XB = TB::MP * H, ZE = W * ZS;
   static constexpr int SMEM_ELEMS = (((XA > XB ? XA : XB) > ZE ? (XA > XB ? XA : XB) : ZE) + 1) & ~1;
   static constexpr int MIN_BLOCKS = min_blocks(NT, TA::E);
   static constexpr int LOG_CLUSTER = LOGR;  // kernel tables: cluster of 2^LOG_CLUSTER CTAs
@@ -135,24 +146,39 @@ struct ClusterKernel {
       fourstep_twiddle<TA>(v, n1, t, LOGN, a.bank);
       ESTL_SYNC();  // the last exchange's reads are done: Z overwrites the buffer
 #pragma unroll
-      for (int j = 0; j < TA::E; ++j) sm[(t + TA::T * j) * ZS + c] = v[j];
+      for (int j = 0; j < TA::E; ++j) sm[c * ZS + t + TA::T * j] = v[j];
     }
-    ESTL_CLUSTER_SYNC();  // every CTA's Z is complete and visible to the cluster
+    ESTL_CLUSTER_ARRIVE();  // release: this CTA's Z to the cluster
+    ESTL_SYNC();            // ... and to this CTA
     const int c = tid & (H - 1), t = tid >> LOGH;
     const int k2 = rank * H + c;
     {
+      constexpr int SPAN = W / TB::T;  // slots per source CTA
+      // the columns this CTA holds first, while the other CTAs arrive
+#pragma unroll
+      for (int j = 0; j < TB::E; ++j)
+        if (j / SPAN == rank) v[j] = sm[((t + TB::T * j) & (W - 1)) * ZS + k2];
+      ESTL_CLUSTER_WAIT();  // every CTA's Z is complete and visible
       PeerBuf z[R];
 #pragma unroll
       for (int q = 0; q < R; ++q) z[q] = peer_buf(smraw, ZE, rank, q);
 #pragma unroll
-      for (int j = 0; j < TB::E; ++j) {
-        constexpr int SPAN = W / TB::T;  // slots per source CTA
-        const int n1 = t + TB::T * j;
-        v[j] = z[j / SPAN][k2 * ZS + (n1 & (W - 1))];
-      }
+      for (int j = 0; j < TB::E; ++j)
+        if (j / SPAN != rank) v[j] = z[j / SPAN][((t + TB::T * j) & (W - 1)) * ZS + k2];
     }
-    ESTL_CLUSTER_SYNC();  // every gather is done: the buffers become exchange space again
-    run_passes<TB, 0>(v, t, c, sm, a.bank.sub(1 << LOGN1, 1 << LOGN1), SidxB{});
+    const Ptr<const cf32> twb = a.bank.sub(1 << LOGN1, 1 << LOGN1);
+    TB::template compute<0>(v, t, twb);  // consumes every gathered value
+    ESTL_CLUSTER_ARRIVE_RELAXED();       // this CTA's reads of the cluster's Z are done
+    ESTL_CLUSTER_WAIT();                 // everyone's are: Z becomes exchange space again
+    if constexpr (TB::P > 1) {
+#pragma unroll
+      for (int j = 0; j < TB::E; ++j) sm[SidxB{}(c, TB::template out_pos<0>(t, j))] = v[j];
+      ESTL_SYNC();
+#pragma unroll
+      for (int j = 0; j < TB::E; ++j) v[j] = sm[SidxB{}(c, t + TB::T * j)];
+      ESTL_SYNC();
+    }
+    run_passes<TB, 1>(v, t, c, sm, twb, SidxB{});
 #pragma unroll
     for (int j = 0; j < TB::E; ++j) stcs(out, k2 + ((t + TB::T * j) << LOGN2), conj_if(v[j], a.sgn));
   }

@@ -112,7 +112,9 @@ const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int p
 // Cluster tiles that single-kernel plans use by default (measured on a
 // GB300, 1 GiB batches): log2 N -> (log2 CTAs per cluster, log2 N2, log2 E).
 static const TileCfg* default_cluster(int logn) {
-  static const int tuned[][4] = {{0, 0, 0, 0}};
+  // 2^14: 4097 vs 3955 GB/s for the single-CTA radix-32 tile; 2^15: 3566 vs
+  // 3017 GB/s for the two-pass four-step; 2^16 and 2^17 stay four-step
+  static const int tuned[][4] = {{14, 2, 7, 4}, {15, 3, 8, 4}};
   for (const auto& t : tuned)
     if (t[0] == logn)
       if (const TileCfg* c = find_tile(STEP_SINGLE, logn, t[3], 4, 0, 0, 0, t[1], t[2])) return c;
@@ -204,7 +206,7 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     mode = 4;
     three_default = true;
   }
-  const bool cluster_default = mode == 0 && !tc && logn > kSingleMaxLog && choice.single_cluster < 0 &&
+  const bool cluster_default = mode == 0 && !tc && choice.single_cluster < 0 && choice.single_loge < 0 &&
                                default_cluster(logn) != nullptr;
   if (mode == 0) mode = (logn <= (tc ? kTcSingleMaxLog : kSingleMaxLog) || cluster_default) ? 1 : 2;
 

@@ -151,6 +151,9 @@ struct FiberSched {
   // not value-initialised: pages a fiber never touches are never committed
   std::vector<std::unique_ptr<char[]>> stacks;
   std::vector<char> state;
+  std::vector<long long> arrivals;  // cluster barrier arrives of each fiber
+  std::vector<long long> waited;    // the phase of each fiber's last wait
+  long long completed = 0;          // cluster barrier phases completed
   ucontext_t main;
   int current = 0;
   const std::function<void(int)>* body = nullptr;
@@ -182,6 +185,9 @@ bool run_fibers(int nt, const std::function<void(int)>& body, bool reverse, int 
   }
   s.ctx.assign(total, ucontext_t{});
   s.state.assign(total, F_RUN);
+  s.arrivals.assign(total, 0);
+  s.waited.assign(total, 0);
+  s.completed = 0;
   s.body = &body;
   tl_sched = &s;
   for (int f = 0; f < total; ++f) {
@@ -216,17 +222,25 @@ bool run_fibers(int nt, const std::function<void(int)>& body, bool reverse, int 
         break;
       }
     }
-    int at_cluster = 0, at_cta = 0, done = 0;
+    int done = 0;
+    long long min_arrivals = -1;
     for (int f = 0; f < total; ++f) {
-      if (s.state[f] == F_AT_CLUSTER) at_cluster++;
-      else if (s.state[f] == F_AT_CTA) at_cta++;
-      else if (s.state[f] == F_DONE) done++;
+      if (s.state[f] == F_DONE) {
+        done++;
+        continue;
+      }
+      if (min_arrivals < 0 || s.arrivals[f] < min_arrivals) min_arrivals = s.arrivals[f];
     }
     if (done == total) break;
-    if (at_cluster && !at_cta && at_cluster + done == total) {
+    if (min_arrivals > s.completed) {  // every running thread arrived: phases up to min_arrivals complete
+      s.completed = min_arrivals;
+      bool woke = false;
       for (int f = 0; f < total; ++f)
-        if (s.state[f] == F_AT_CLUSTER) s.state[f] = F_RUN;
-      continue;
+        if (s.state[f] == F_AT_CLUSTER && s.waited[f] <= s.completed) {
+          s.state[f] = F_RUN;
+          woke = true;
+        }
+      if (woke) continue;
     }
     ok = false;  // mismatched barriers: nothing can run
     break;
@@ -294,11 +308,31 @@ void estl_emu_sync() {
   swapcontext(&s->ctx[s->current], &s->main);
 }
 
-// Cluster barrier: wait for every thread of every CTA of the cluster.
-void estl_emu_cluster_sync() {
+// Split cluster barrier.  An arrive counts the thread into the cluster's next
+// barrier phase; a wait blocks until every thread of the cluster has arrived
+// at the phase of the thread's last arrive.  A thread that arrived keeps
+// running until its wait, and a wait whose phase has completed returns at
+// once, as on the device: work between the two overlaps the other CTAs, and a
+// read of another CTA's shared memory before the phase completed sees the
+// poison in one of the two scheduling orders.
+void estl_emu_cluster_arrive() {
   FiberSched* s = tl_sched;
+  s->arrivals[s->current]++;
+}
+void estl_emu_cluster_wait() {
+  FiberSched* s = tl_sched;
+  const long long phase = s->arrivals[s->current];  // wait for phase `phase` to complete
+  if (phase < 1 || phase <= s->waited[s->current]) estl_emu_fail("cluster wait without an arrive", s->current, 0);
+  s->waited[s->current] = phase;
+  if (s->completed >= phase) return;
   s->state[s->current] = F_AT_CLUSTER;
   swapcontext(&s->ctx[s->current], &s->main);
+}
+
+// Cluster barrier: arrive and wait.
+void estl_emu_cluster_sync() {
+  estl_emu_cluster_arrive();
+  estl_emu_cluster_wait();
 }
 
 cf32* estl_emu_cluster_smem(int rank, long long* n) {

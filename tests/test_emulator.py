@@ -268,7 +268,7 @@ def test_cluster_scheduler_orders_distributed_shared_memory(emu):
         assert emu.emu_cluster_barrier_selftest(ncta, 64, 0) < ncta * 64
 
 
-@pytest.mark.parametrize("logn", range(13, 18))
+@pytest.mark.parametrize("logn", range(12, 18))
 def test_cluster_tiles(emu, logn):
     """Every cluster tile (one transform per thread-block cluster, the
     four-step transpose through distributed shared memory), both directions,
