@@ -91,6 +91,7 @@ SIGNATURES = {
     "estl_packed_plan_create": (_INT, [_P, _P, _I64, _INT, _INT, ctypes.POINTER(_P)]),
     "estl_packed_execute": (_INT, [_P, _P, _P, _P]),
     "estl_packed_check": (_INT, [_P]),
+    "estl_packed_plan_set_test_hook": (_INT, [_P, _INT, ctypes.c_uint64]),
     "estl_packed_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_packed_plan_destroy": (_INT, [_P]),
     "estl_execute_packed": (_INT, [_P, _P, _I64, _INT, _P, _P, _P]),

@@ -354,6 +354,9 @@ struct estl_plan_s {
   cf32* blue_a = nullptr;
   cf32* blue_c = nullptr;
   size_t blue_chirp_bytes = 0, blue_spec_bytes = 0, blue_work_bytes = 0;
+  // a bounded wait gave up with bulk copies possibly still in flight
+  // (estl_plan_check): later executes are refused
+  bool unusable = false;
   // per-launch profiling (estl_plan_set_profiling)
   bool profiling = false;
   struct Rec {
@@ -788,6 +791,14 @@ estl_status estl_plan_check(estl_plan plan) {
   if (s != ESTL_OK) return s;
   if (e) {
     cudaMemset(engine().dev_err, 0, sizeof(long long));
+    if (e & kErrCopiesInFlight) {
+      // a CTA left with copies that may still land in shared memory a later
+      // launch owns: this plan's results and its next executes are not trusted
+      plan->unusable = true;
+      return fail(ESTL_DEVICE_ERROR,
+                  "a bulk-load wait gave up (tile %lld) and its copies in flight did not drain; the plan is unusable",
+                  (e & ~kErrCopiesInFlight) - 1);
+    }
     return fail(ESTL_TIMEOUT, "a bulk-load wait gave up (tile %lld)", e - 1);
   }
   return ESTL_OK;
@@ -918,6 +929,7 @@ struct LayoutIO {
 static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
                                cudaStream_t stream, const LayoutIO* io = nullptr) {
   std::lock_guard<std::mutex> g(plan->mu);
+  if (plan->unusable) return fail(ESTL_DEVICE_ERROR, "the plan is unusable (estl_plan_check reported copies in flight)");
   estl_status s;
   // executes that touch device state of the plan (scratch, work lists,
   // staging, Bluestein buffers, profiling events) are ordered behind the
@@ -1049,6 +1061,7 @@ static std::vector<long long> host_schedule(long long batch, long long chunk) {
 
 estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
   if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
+  if (plan->unusable) return fail(ESTL_DEVICE_ERROR, "the plan is unusable (estl_plan_check reported copies in flight)");
   estl_status s = require_init();
   if (s != ESTL_OK) return s;
   s = check_buffers(h_in, h_out);

@@ -47,6 +47,9 @@ struct estl_packed_plan_s {
   const void* g_in = nullptr;
   void* g_out = nullptr;
   cudaStream_t cap_stream = nullptr;
+  // test hook (estl_packed_plan_set_test_hook)
+  int test_skip_kind = -1;
+  unsigned long long test_spin_limit = 0;
 };
 
 static size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -74,6 +77,8 @@ static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out,
     a.error = p->error;
     a.sgn = p->direction == ESTL_FORWARD ? 1.f : -1.f;
     a.persistent = L.persistent ? 1 : 0;
+    a.skip_kind = p->test_skip_kind;
+    a.spin_limit = p->test_spin_limit ? p->test_spin_limit : kPackedSpinLimit;
     const long long grid = L.persistent ? std::min<long long>(p->grid, L.launch_count[k]) : L.launch_count[k];
     if (grid < 1 || grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "packed grid of %lld CTAs", grid);
     packed_kernel<<<(unsigned)grid, kPackedThreads, p->smem, st>>>(a);
@@ -214,6 +219,20 @@ estl_status estl_packed_check(estl_packed_plan p) {
     cudaMemset(p->error, 0, sizeof(int));
     return fail(ESTL_TIMEOUT, "a row item gave up waiting for its column items");
   }
+  return ESTL_OK;
+}
+
+estl_status estl_packed_plan_set_test_hook(estl_packed_plan p, int skip_column_items, uint64_t spin_limit) {
+  if (!p) return fail(ESTL_INVALID_ARG, "NULL plan");
+  if (spin_limit > kPackedSpinLimit) return fail(ESTL_INVALID_ARG, "spin limit above the default %llu", kPackedSpinLimit);
+  std::lock_guard<std::mutex> g(p->mu);
+  p->test_skip_kind = skip_column_items ? PK_COL : -1;
+  p->test_spin_limit = spin_limit;
+  // the kernel arguments live in the captured graph: capture again
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
   return ESTL_OK;
 }
 

@@ -7,6 +7,11 @@
 
 namespace estl {
 
+// Iterations of the dependency wait before it gives up (~2^24 x 128 ns, a few
+// seconds): a row item whose column items never finish records the failure in
+// *error and is skipped instead of spinning forever.
+constexpr unsigned long long kPackedSpinLimit = 1ULL << 24;
+
 struct PackedArgs {
   Ptr<const PackedItem> items;
   long long item_base;  // first item of this launch
@@ -24,6 +29,10 @@ struct PackedArgs {
   int* error;          // set to 1 when a dependency wait gives up
   float sgn;
   int persistent;
+  // test hook (estl_packed_plan_set_test_hook): items of this kind are left
+  // out (-1: none), and the dependency wait gives up after spin_limit polls
+  int skip_kind = -1;
+  unsigned long long spin_limit = kPackedSpinLimit;
 };
 
 // Size-class tile bodies, all with 256 threads per CTA.
@@ -85,11 +94,6 @@ ESTL_HD void backoff() {
   __nanosleep(128);
 #endif
 }
-
-// Iterations of the dependency wait before it gives up (~2^24 x 128 ns, a few
-// seconds): a row item whose column items never finish records the failure in
-// *error and is skipped instead of spinning forever.
-constexpr unsigned long long kPackedSpinLimit = 1ULL << 24;
 
 template <class K>
 ESTL_HD void packed_single(const PackedArgs& a, const PackedItem& it, int tid, cf32* sm) {
@@ -175,14 +179,16 @@ ESTL_HD void packed_run(const PackedArgs& a, long long cta, int tid, cf32* sm, i
       if (idx >= a.nitems) return;
     }
     const PackedItem it = a.items[a.item_base + idx];
-    if (it.kind == PK_ROW) {
+    if (it.kind == a.skip_kind) {
+      // test hook: the item is left out (a skipped column item is never counted)
+    } else if (it.kind == PK_ROW) {
       // wait until every column item of this transform has been written
       if (tid == 0) {
         const unsigned int need = (unsigned int)a.ncol[it.tf];
         unsigned long long spins = 0;
         int ok = 1;
         while (load_acquire_u32(a.done + it.tf) < need) {
-          if (++spins > kPackedSpinLimit) {
+          if (++spins > a.spin_limit) {
             ok = 0;
             *a.error = 1;
             break;
@@ -198,7 +204,7 @@ ESTL_HD void packed_run(const PackedArgs& a, long long cta, int tid, cf32* sm, i
     } else {
       packed_dispatch(a, it, tid, sm);
     }
-    if (it.kind == PK_COL) {
+    if (it.kind == PK_COL && it.kind != a.skip_kind) {
       fence_gpu();  // this thread's scratch stores before the count
       ESTL_SYNC();
       if (tid == 0) atomic_add_u32(a.done + it.tf, 1u);

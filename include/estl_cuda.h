@@ -148,9 +148,12 @@ estl_status estl_plan_destroy(estl_plan plan);
  * scratch bytes.  Writes at most len bytes including the terminator. */
 estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len);
 
-/* Waits for the device; returns ESTL_TIMEOUT if a dependency wait inside a
- * streamed plan's persistent kernel gave up since the last check (the
- * outputs of that execute are then incomplete), else ESTL_OK. */
+/* Waits for the device; returns ESTL_TIMEOUT if a bounded device wait of a
+ * persistent kernel (a streamed plan's dependency wait, a bulk-load tile's
+ * copy wait) gave up since the last check (the outputs of that execute are
+ * then incomplete), else ESTL_OK.  If a bulk-load kernel also could not drain
+ * the copies it had in flight, the plan is marked unusable: this returns
+ * ESTL_DEVICE_ERROR and later executes of the plan are refused. */
 estl_status estl_plan_check(estl_plan plan);
 
 /* Number of kernel launches (and device copies) one execute issues. */
@@ -362,6 +365,14 @@ estl_status estl_packed_execute(estl_packed_plan plan, const void* d_in, void* d
  * incomplete), else ESTL_OK. */
 estl_status estl_packed_check(estl_packed_plan plan);
 estl_status estl_packed_plan_describe(estl_packed_plan plan, char* buf, size_t len);
+/* Test hook for the bounded dependency wait (the reference's error path is
+ * xCLErr / CLException, uOpenCL.h:21-55).  skip_column_items != 0 leaves the
+ * four-step column items out of later executes, so their row items' waits can
+ * never be satisfied; spin_limit (0 = the default of 2^24 polls of 128 ns)
+ * bounds those waits.  The wait then runs out on the device without a fault,
+ * the row items are skipped, and estl_packed_check returns ESTL_TIMEOUT.
+ * skip_column_items = 0, spin_limit = 0 restores normal executes. */
+estl_status estl_packed_plan_set_test_hook(estl_packed_plan plan, int skip_column_items, uint64_t spin_limit);
 estl_status estl_packed_plan_destroy(estl_packed_plan plan);
 /* One blocking call for a batch used once: plan (persistent mode), execute on
  * `stream`, wait, check, release. */

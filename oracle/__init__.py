@@ -52,6 +52,7 @@ def _load():
         lib.oracle_fft.argtypes = [P, P, I64, I64, ctypes.c_int, ctypes.c_int]
         lib.oracle_fft.restype = ctypes.c_int
         lib.oracle_dft_ld.argtypes = [P, P, I64, ctypes.c_int]
+        lib.oracle_dft_bins.argtypes = [P, P, I64, P, I64, ctypes.c_int]
         lib.oracle_conv_direct.argtypes = [P, I64, P, I64, P]
         lib.oracle_conv_fft.argtypes = [P, I64, P, I64, P, ctypes.c_int]
         lib.oracle_conv_fft.restype = ctypes.c_int
@@ -91,6 +92,18 @@ def dft_ld(x, sign=-1):
     x = np.ascontiguousarray(x, dtype=np.complex128).ravel()
     out = np.empty_like(x)
     _load().oracle_dft_ld(_ptr(x), _ptr(out), x.size, int(sign))
+    return out
+
+
+def dft_bins(x, bins, sign=-1):
+    """Bins `bins` of the direct DFT of one 1-D sequence of any length (O(n)
+    per bin; exactly reduced angles, roots re-seeded from long double,
+    compensated double sums): a reference independent of any FFT for long
+    transforms sampled at a few frequencies."""
+    x = np.ascontiguousarray(x, dtype=np.complex128).ravel()
+    bins = np.ascontiguousarray(bins, dtype=np.int64).ravel()
+    out = np.empty(bins.size, np.complex128)
+    _load().oracle_dft_bins(_ptr(x), _ptr(out), x.size, _ptr(bins), bins.size, int(sign))
     return out
 
 

@@ -188,6 +188,46 @@ void oracle_dft_ld(const double* in, double* out, int64_t n, int sign) {
   }
 }
 
+/* Selected bins of the direct DFT of one sequence of any length (the
+ * definition FFT_FFTW3.h:26-28 computes, evaluated term by term):
+ * out[b] = sum_j x_j exp(sign 2 pi i j k_b / n), O(n) per bin.  The root for
+ * bin k is re-seeded every 256 terms from long-double cosl/sinl of the exact
+ * integer angle (j k mod n) and stepped in double in between; the sums are
+ * compensated (Kahan) doubles.  Error near 1e-14 relative for n up to 2^23,
+ * far below the FP32 tolerances it checks, and fast on hosts whose long
+ * double is a software type. */
+static void kahan_add(double* s, double* c, double v) {
+  const double y = v - *c, t = *s + y;
+  *c = (t - *s) - y;
+  *s = t;
+}
+
+void oracle_dft_bins(const double* in, double* out, int64_t n, const int64_t* bins, int64_t nbins, int sign) {
+  const long double two_pi = 2.0L * 3.14159265358979323846264338327950288L;
+  for (int64_t b = 0; b < nbins; b++) {
+    const int64_t k = ((bins[b] % n) + n) % n;
+    const long double a1 = two_pi * (long double)k / (long double)n;
+    const double c1 = (double)cosl(a1), s1 = (double)(sign * sinl(a1));
+    double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0, wr = 1.0, wi = 0.0;
+    for (int64_t j = 0; j < n; j++) {
+      if ((j & 255) == 0) {
+        const int64_t m = (int64_t)(((__int128)j * k) % n);
+        const long double a = two_pi * (long double)m / (long double)n;
+        wr = (double)cosl(a);
+        wi = (double)(sign * sinl(a));
+      }
+      const double xr = in[2 * j], xi = in[2 * j + 1];
+      kahan_add(&sr, &cr, xr * wr - xi * wi);
+      kahan_add(&si, &ci, xr * wi + xi * wr);
+      const double t = wr * c1 - wi * s1;
+      wi = wr * s1 + wi * c1;
+      wr = t;
+    }
+    out[2 * b] = sr;
+    out[2 * b + 1] = si;
+  }
+}
+
 /* Direct linear convolution (and correlation) of real sequences in long
  * double: out[m] = sum_i a[i] b[m - i], length la + lb - 1. */
 void oracle_conv_direct(const double* a, int64_t la, const double* b, int64_t lb, double* out) {

@@ -86,10 +86,16 @@ def test_gpu_bluestein(engine, n, batch):
         y = p.execute(xd).cpu().numpy()
         if n <= 4096:
             ref = direct(x, sign)
+            assert rel(y, ref).max() < TOL, (n, sign)
         else:
-            x128 = x.astype(np.complex128)
-            ref = np.fft.fft(x128, axis=-1) if sign < 0 else np.fft.ifft(x128, axis=-1) * n
-        assert rel(y, ref).max() < TOL, (n, sign)
+            # the oracle's direct DFT (no FFT involved) on 24 sampled bins per
+            # transform (both ends and random ones), relative to the bins' norm
+            rng = np.random.default_rng(n)
+            bins = np.concatenate([[0, 1, n // 2, n - 1], rng.integers(0, n, 20)])
+            for b in range(batch):
+                ref_b = oracle.dft_bins(x[b], bins, sign)
+                e = np.sqrt(np.sum(np.abs(y[b, bins] - ref_b) ** 2) / np.sum(np.abs(ref_b) ** 2))
+                assert e < TOL, (n, sign, b, e)
 
 
 @pytest.mark.gpu

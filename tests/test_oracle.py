@@ -131,3 +131,21 @@ def test_reference_algorithm_port(logn):
         y = oracle.ref_contiguous_fft(x, sign, nthreads=4)
         e = oracle.rel_l2(y, oracle.fft(x, sign)).max()
         assert e < 3e-5, (n, sign, e)
+
+
+def test_dft_bins_matches_the_direct_dft_and_numpy():
+    """The sampled direct DFT (stepped roots re-seeded every 256 terms,
+    compensated sums) against the full long-double DFT at small n and
+    numpy's FP64 FFT at a length past many re-seeds."""
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(1000) + 1j * rng.standard_normal(1000)
+    bins = np.arange(1000)
+    for sign in (-1, +1):
+        got = oracle.dft_bins(x, bins, sign)
+        assert np.max(np.abs(got - oracle.dft_ld(x, sign))) < 1e-11
+    n = 123457
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    bins = np.array([0, 1, 2, 4097, n // 2, n - 1, 98765])
+    ref = np.fft.fft(x)[bins]
+    got = oracle.dft_bins(x, bins, -1)
+    assert np.max(np.abs(got - ref)) / np.sqrt(n) < 1e-11

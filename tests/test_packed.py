@@ -194,6 +194,54 @@ def test_gpu_python_packed_api(engine):
     assert np.array_equal(z.cpu().numpy()[mask], ref[mask])
 
 
+@pytest.mark.gpu
+def test_gpu_dependency_wait_gives_up_and_plan_recovers(engine):
+    """The bounded dependency wait of the persistent kernel, run out on the
+    GPU without a fault: the test hook leaves the four-step column items out
+    and bounds the row items' wait at 2^10 polls.  estl_packed_check reports
+    ESTL_TIMEOUT, the four-step transforms' outputs are untouched (their row
+    items gave up and were skipped), the small transforms are right, and with
+    the hook cleared the same plan computes every transform again.  The
+    reference's counterpart is its error path (uOpenCL.h:21-55)."""
+    import torch
+
+    from estl_gb300._lib import check, lib
+    L = lib()
+    # two 2^13-point four-step transforms among small single-tile ones
+    sizes = np.array([1 << 13, 64, 1 << 13, 256, 1024], np.int64)
+    offsets = np.concatenate([[0], np.cumsum(sizes[:-1])]).astype(np.int64)
+    rng = np.random.default_rng(21)
+    total = int(sizes.sum())
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    plan = ctypes.c_void_p()
+    check(L.estl_packed_plan_create(offsets.ctypes.data, sizes.ctypes.data, len(sizes), -1, 0, ctypes.byref(plan)))
+    st = torch.cuda.current_stream().cuda_stream
+    try:
+        check(L.estl_packed_plan_set_test_hook(plan, 1, 1 << 10))
+        y = torch.full_like(xd, float("nan"))
+        check(L.estl_packed_execute(plan, ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                    ctypes.c_void_p(st)))
+        assert L.estl_packed_check(plan) == 6  # ESTL_TIMEOUT
+        assert b"gave up" in L.estl_last_error()
+        yh = y.cpu().numpy()
+        for o, n in zip(offsets, sizes):
+            if n == 1 << 13:
+                assert np.all(np.isnan(yh[o:o + n].real)), "a skipped row item wrote its output"
+            else:
+                e = oracle.rel_l2(yh[o:o + n][None, :], oracle.fft(x[o:o + n][None, :], -1))[0]
+                assert e < tol(n)
+        # hook cleared: the plan runs every item again and reports no timeout
+        check(L.estl_packed_plan_set_test_hook(plan, 0, 0))
+        y2 = torch.full_like(xd, float("nan"))
+        check(L.estl_packed_execute(plan, ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(y2.data_ptr()),
+                                    ctypes.c_void_p(st)))
+        check(L.estl_packed_check(plan))
+        check_against_oracle(offsets, sizes, x, y2.cpu().numpy(), -1)
+    finally:
+        L.estl_packed_plan_destroy(plan)
+
+
 def test_python_packed_api_validates_before_the_engine():
     """Argument errors are raised on the host, before any engine call."""
     import torch
