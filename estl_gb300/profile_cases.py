@@ -1,0 +1,50 @@
+"""Small, self-contained FFT launches for profiling one kernel at a time.
+
+    python -m estl_gb300.profile_cases <case> [<case> ...]
+
+Each case plans one transform size on a batch of 2^24 complex64 elements
+(128 MiB per buffer: larger than the L2, small enough for a profiler's
+replays), executes it three times and checks the plan's device status, so
+that a profiler capture of launch 2 (`-s 1 -c 1`) sees a warm kernel.
+Cases: the planner default for a size (`n13`, `n14`, ... `n24`), or an
+explicit tile from CASES below.
+"""
+import sys
+
+CASES = {
+    # one transform per thread-block cluster (cluster_core.cuh)
+    "cluster15": (15, dict(mode="single", tiles={"single_loge": 4, "single_cluster_log2": 3, "split_log2": 8})),
+    "cluster16": (16, dict(mode="single", tiles={"single_loge": 4, "single_cluster_log2": 3, "split_log2": 8})),
+    # whole transforms in one CTA (fft_core.cuh SingleKernel, radix 32)
+    "single13": (13, dict(mode="single", tiles={"single_loge": 5, "single_logc": 0, "single_logr": 5})),
+    "single14": (14, dict(mode="single", tiles={"single_loge": 5, "single_logc": 0, "single_logr": 5})),
+}
+
+
+def run(case, elements_log=24):
+    import torch
+
+    import estl_gb300 as estl
+    if case in CASES:
+        logn, kw = CASES[case]
+    elif case.startswith("n") and case[1:].isdigit():
+        logn, kw = int(case[1:]), {}
+    else:
+        raise SystemExit(f"unknown case {case!r}; known: {sorted(CASES)} or n<log2 N>")
+    estl.init(0)
+    n = 1 << logn
+    batch = max(1, (1 << elements_log) // n)
+    x = torch.view_as_complex((torch.rand((n * batch, 2), device="cuda") * 2 - 1).contiguous())
+    y = torch.empty_like(x)
+    p = estl.Plan(n, batch, estl.FORWARD, **kw)
+    for _ in range(3):
+        p.execute(x, out=y)
+    torch.cuda.synchronize()
+    p.check()
+    print(case, p.describe(), flush=True)
+    p.close()
+
+
+if __name__ == "__main__":
+    for c in sys.argv[1:]:
+        run(c)
