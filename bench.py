@@ -49,6 +49,9 @@ def parse():
                     help="plan mode for every N (auto: autotuned / tuning cache / planner default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner pass that picks each N's plan before the timed region")
+    ap.add_argument("--chunk-log", type=int, default=0,
+                    help="four-step / three-pass modes: log2 of the elements per column/row launch pair "
+                         "(scratch chunk); 0 = the planner's 2^27")
     ap.add_argument("--elements-log", type=int, default=27,
                     help="log2 complex elements per direction (27 = the 1 GiB sweep; smaller for ncu captures)")
     return ap.parse_args()
@@ -438,13 +441,16 @@ def bench_uneven(estl, torch):
 
 
 CONV_NO_PAIRING = 4  # ESTL_CONV_NO_PAIRING
+CONV_COMPLEX = 8  # ESTL_CONV_COMPLEX
 
 
 def bench_conv_pairs(estl, torch):
-    """The real-input specialisation on the device (estl_conv_execute, device
+    """The real-input specialisations on the device (estl_conv_execute, device
     buffers, no host copies): batches of one padded length, each request its
-    own filter, two requests per complex transform (default) against one
-    (ESTL_CONV_NO_PAIRING); FP32 and split fp16."""
+    own filter.  Padded n <= 2^14: two requests per complex transform
+    (default) against one (ESTL_CONV_NO_PAIRING), FP32 and split fp16.
+    Padded n > 2^14: each request as an n/2-point complex transform (default)
+    against a full complex transform (ESTL_CONV_COMPLEX)."""
     import ctypes
     import numpy as np
     from estl_gb300._lib import ConvRequest, check, lib
@@ -453,7 +459,12 @@ def bench_conv_pairs(estl, torch):
            "method": "host clock around 5 blocking estl_conv_execute calls after 2 warm-up calls (request "
                      "layout, spectra and convolutions included)"}
     st = torch.cuda.Stream()
-    for L, K, count in ((3000, 100, 8192), (900, 125, 32768), (12000, 385, 2048)):
+    for L, K, count in ((3000, 100, 8192), (900, 125, 32768), (12000, 385, 2048), (100000, 2000, 512),
+                        (900000, 4000, 64)):
+        large = L + K - 1 > (1 << 14)
+        variants = ((("real_input", 0), ("complex", CONV_COMPLEX)) if large else
+                    (("paired", 0), ("unpaired", CONV_NO_PAIRING), ("paired_split_fp16", estl.PREC_SPLIT_FP16 << 8),
+                     ("unpaired_split_fp16", (estl.PREC_SPLIT_FP16 << 8) | CONV_NO_PAIRING)))
         g = torch.Generator(device="cuda").manual_seed(9)
         sig = torch.randn(L * count, device="cuda", generator=g)
         filt = torch.randn(K * count, device="cuda", generator=g)
@@ -461,8 +472,7 @@ def bench_conv_pairs(estl, torch):
         arr = (ConvRequest * count)(*[ConvRequest(L, K, i * L, i * K, i * (L + K - 1)) for i in range(count)])
         res = {}
         ref = None
-        for name, flags in (("paired", 0), ("unpaired", CONV_NO_PAIRING), ("paired_split_fp16", estl.PREC_SPLIT_FP16 << 8),
-                            ("unpaired_split_fp16", (estl.PREC_SPLIT_FP16 << 8) | CONV_NO_PAIRING)):
+        for name, flags in variants:
             ws = ctypes.c_size_t()
             check(Lb.estl_conv_workspace_size(arr, count, flags, ctypes.byref(ws)))
             wsb = torch.empty(ws.value + 256, dtype=torch.uint8, device="cuda")
@@ -488,8 +498,12 @@ def bench_conv_pairs(estl, torch):
             err = float(np.sqrt(np.sum((y - ref) ** 2) / np.sum(ref ** 2)))
             res[name] = {"ms": round(ms, 3), "req_per_s": round(count / (ms * 1e-3), 1), "rel_l2_first": float(f"{err:.3e}")}
             del wsb
-        res["paired_speedup"] = round(res["unpaired"]["ms"] / res["paired"]["ms"], 2)
-        res["paired_split_fp16_speedup"] = round(res["unpaired_split_fp16"]["ms"] / res["paired_split_fp16"]["ms"], 2)
+        if large:
+            res["real_input_speedup"] = round(res["complex"]["ms"] / res["real_input"]["ms"], 2)
+        else:
+            res["paired_speedup"] = round(res["unpaired"]["ms"] / res["paired"]["ms"], 2)
+            res["paired_split_fp16_speedup"] = round(res["unpaired_split_fp16"]["ms"] / res["paired_split_fp16"]["ms"],
+                                                     2)
         out[f"L{L}_K{K}_x{count}"] = res
     return out
 
@@ -831,8 +845,9 @@ def main():
     plans = {}
     for logn in logns:
         n = 1 << logn
-        plans[logn] = (estl.Plan(n, TOTAL // n, estl.FORWARD, mode=args.mode),
-                       estl.Plan(n, TOTAL // n, estl.BACKWARD, mode=args.mode))
+        chunk = max(1, (1 << args.chunk_log) // n) if args.chunk_log and args.mode != "auto" else 0
+        plans[logn] = (estl.Plan(n, TOTAL // n, estl.FORWARD, mode=args.mode, chunk=chunk),
+                       estl.Plan(n, TOTAL // n, estl.BACKWARD, mode=args.mode, chunk=chunk))
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
 

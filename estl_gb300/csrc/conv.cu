@@ -41,13 +41,19 @@ std::vector<ConvKernelDesc>& conv_table() {
   v.push_back(cdesc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C)); \
   v.push_back(cdesc<SpecPairKernel<M, E, R, C>>(CK_SPEC_PAIR, M, E, R, C));     \
   v.push_back(cdesc<ConvPairKernel<M, E, R, C>>(CK_CONV_PAIR, M, E, R, C));
-#define ESTL_XC_COL(M, E, R, C)                                           \
-  v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C)); \
-  v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));
-#define ESTL_XC_ROW(M, E, R, C)                                         \
-  v.push_back(cdesc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C)); \
-  v.push_back(cdesc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));
-#define ESTL_XC_OUT(M, E, R, C) v.push_back(cdesc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C));
+#define ESTL_XC_COL(M, E, R, C)                                                         \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C));               \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));               \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C, false, true>>(CK_COL_FILTER_H, M, E, R, C)); \
+  v.push_back(cdesc<ConvColKernel<M, E, R, C, false, true>>(CK_COL_SIGNAL_H, M, E, R, C));
+#define ESTL_XC_ROW(M, E, R, C)                                                \
+  v.push_back(cdesc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C));        \
+  v.push_back(cdesc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));             \
+  v.push_back(cdesc<SpecRowHalfKernel<M, E, R, C>>(CK_SPEC_ROW_H, M, E, R, C));  \
+  v.push_back(cdesc<ConvMidHalfKernel<M, E, R, C>>(CK_MID_H, M, E, R, C));
+#define ESTL_XC_OUT(M, E, R, C)                                            \
+  v.push_back(cdesc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C)); \
+  v.push_back(cdesc<ConvOutHalfKernel<M, E, R, C>>(CK_OUT_H, M, E, R, C));
 #include "conv_list.inc"
     // split-precision (tensor-core) variants of the 16-elements-per-thread tiles
 #define ESTL_XC_SINGLE(M, E, R, C)                                                        \

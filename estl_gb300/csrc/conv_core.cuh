@@ -386,7 +386,9 @@ struct SpecPairKernel : ConvPairKernel<LOGM, LOGE, LOGR, LOGC, TC> {
 // ---------------------------------------------------------------------------
 // A: column pass over the zero-padded real input of row f: C adjacent
 // columns n1, N2-point DFTs, times w_N^{n1 k2}, to s1[f*N + k2*N1 + n1].
-template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false>
+// HALF: the real-input form (below): the input is the N'-point complex
+// sequence z_m = x_{2m} + i x_{2m+1} and a.logn = log2 N'.
+template <int LOGM, int LOGE, int LOGR, int LOGC, bool TC = false, bool HALF = false>
 struct ConvColKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
@@ -417,7 +419,10 @@ struct ConvColKernel {
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int n = n1 + ((t + TL::T * j) << logn1);
-      v[j] = cf32{n < r.sig_len ? s[n] : 0.f, 0.f};
+      if constexpr (HALF)
+        v[j] = cf32{2 * n < r.sig_len ? s[2 * n] : 0.f, 2 * n + 1 < r.sig_len ? s[2 * n + 1] : 0.f};
+      else
+        v[j] = cf32{n < r.sig_len ? s[n] : 0.f, 0.f};
     }
     any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
     const Ptr<cf32> o = a.s1.sub(f * N, N);
@@ -578,6 +583,247 @@ struct ConvOutKernel {
       const int m = n1_0 + c2 + (n2 << logn1) - r.out_shift;
       const float val = sm[sidx(c2, n2)].x;
       if (m >= 0 && m < r.out_len) o[m] = val * g;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// N > 2^14, real input (the real-input specialisation of the four-step path,
+// after Convolution.h:106-120,146-148: real data in, real output).  A real
+// request x of padded length N is transformed as the N' = N/2-point complex
+// sequence z_m = x_{2m} + i x_{2m+1} (ConvColKernel<..., HALF>), so every
+// pass moves half the bytes of the complex path.  With Z = FFT_N'(z) and
+// Zm_k = conj(Z_{(N'-k) mod N'}):
+//   E_k = (Z_k + Zm_k) / 2,  O_k = (Z_k - Zm_k) / (2i),
+//   X_k = E_k + w_N^k O_k,   X_{N'-k} = conj(E_k - w_N^k O_k),
+// the spectrum of x for k in [0, N'] (X_{N'} from k = 0).  The product
+// Y = X H is Hermitian, and the real inverse is again a half-length complex
+// transform: v = IFFT_N'(V) with
+//   V_k = (Y_k + conj(Y_{N'-k})) + i conj(w_N^k) (Y_k - conj(Y_{N'-k})),
+// y_{2m} = Re v_m, y_{2m+1} = Im v_m.
+//
+// In the four-step layout N' = N1 * N2 the row pass holds row k2 (all k1 of
+// k = k2 + N2 k1), and the mirror N' - k lies in row (N2 - k2) mod N2 at k1'
+// = N1 - 1 - k1 (row 0: k1' = (N1 - k1) mod N1).  A CTA of C rows therefore
+// takes C/2 rows k2 = b C/2 + r and their mirror rows N2 - k2; row 0 and row
+// N2/2 are their own mirrors and share CTA 0.  One shared-memory exchange
+// brings each element's mirror into the thread.  The filter spectrum is kept
+// for k < N' in the permuted order Hp[k2 N1 + k1] = H_k, with H_{N'} (real)
+// in slot N'.
+// ---------------------------------------------------------------------------
+
+// Row k2 held by row c of CTA b (C = 2h rows per CTA) and the row of the CTA
+// holding its mirror.
+struct MirrorRows {
+  int k2, partner;
+};
+ESTL_HD MirrorRows mirror_rows(int b, int c, int h, int n2) {
+  const int r = c < h ? c : c - h;
+  const int base = b * h + r;  // in [0, N2/2)
+  if (c < h) return {base, base == 0 ? c : c + h};
+  return {base == 0 ? n2 / 2 : n2 - base, base == 0 ? c : c - h};
+}
+
+// Position k1' of the mirror of (k2, k1) in its row.
+ESTL_HD int mirror_k1(int k2, int k1, int n1) { return k2 == 0 ? (n1 - k1) & (n1 - 1) : n1 - 1 - k1; }
+
+// E and O of X_k = E + w O from Z_k and the mirror Z_{N'-k}.
+ESTL_HD void real_split(cf32 z, cf32 zmirror, cf32& e, cf32& o) {
+  const cf32 zc = cconj(zmirror);
+  e = cf32{0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y)};
+  const cf32 d = cf32{0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y)};
+  o = cf32{d.y, -d.x};  // d / i
+}
+
+// B (spectrum, real input): row DFTs of the filter's half-length transform,
+// then H_k (and H_{N'}) from each element and its mirror, scaled by
+// 1/N (conjugated for correlation), stored in the permuted order.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct SpecRowHalfKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, TL::T >= 16 ? 16 : TL::T * C >= 16 ? 16 / TL::T : C);
+  static constexpr int EXCH = C * CS;
+  static constexpr int SMEM_ELEMS = EXCH;
+  static_assert(NT <= 1024, "too many threads");
+  static_assert(C >= 2, "rows come in mirror pairs");
+  static constexpr int MINB = min_blocks(NT, TL::E);
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int NH = 1 << a.logn;  // N'
+    const int logn2 = a.logn - LOGM, n2 = 1 << logn2;
+    const int nblk = n2 >> LOGC;
+    const long long f = cta / nblk;
+    const int b = (int)(cta - f * nblk);
+    const MirrorRows mr = mirror_rows(b, c, C / 2, n2);
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, EXCH};
+    const Sidx sidx{};
+    const Ptr<cf32> s1 = a.s1.sub(f * NH + (long long)mr.k2 * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    if constexpr (TL::P == 1) ESTL_SYNC();
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const Ptr<cf32> o = a.spec_out.sub(r.spec_off, NH + 2);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k1 = t + TL::T * j;
+      const cf32 zm = sm[sidx(mr.partner, mirror_k1(mr.k2, k1, TL::M))];
+      cf32 e, od;
+      real_split(v[j], zm, e, od);
+      const cf32 w = twiddle_n(a.bank, a.logn + 1, mr.k2 + (k1 << logn2));
+      const cf32 wo = cmul(w, od);
+      const cf32 h = cadd(e, wo);
+      o[mr.k2 * TL::M + k1] = cf32{h.x * r.scale, h.y * r.scale * r.conj};
+      if (mr.k2 == 0 && k1 == 0) {
+        const cf32 hn = cconj(csub(e, wo));  // H_{N'} (real)
+        o[NH] = cf32{hn.x * r.scale, hn.y * r.scale * r.conj};
+      }
+    }
+  }
+};
+
+// B (convolution, real input): row DFT (Z), the spectrum of x from Z and
+// its mirror, times H, the half-length inverse's input V, conj, row DFT over
+// k1, times w_N'^{k2 n1}, stored to s2[f*N' + n1*N2 + k2] through shared
+// memory.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvMidHalfKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, C);
+  static constexpr int EXCH = C * CS;
+  static constexpr int SMEM_ELEMS = EXCH;
+  static_assert(NT <= 1024, "too many threads");
+  static_assert(C >= 2, "rows come in mirror pairs");
+  static constexpr int MINB = 1;  // two DFTs, the spectrum algebra and the twiddle epilogue
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int NH = 1 << a.logn;
+    const int logn2 = a.logn - LOGM, n2 = 1 << logn2;
+    const int nblk = n2 >> LOGC;
+    const long long f = cta / nblk;
+    const int b = (int)(cta - f * nblk);
+    const MirrorRows mr = mirror_rows(b, c, C / 2, n2);
+    const int k2p = mirror_rows(b, mr.partner, C / 2, n2).k2;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, EXCH};
+    const Sidx sidx{};
+    const Ptr<cf32> s1 = a.s1.sub(f * NH + (long long)mr.k2 * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    if constexpr (TL::P == 1) ESTL_SYNC();
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    cf32 zm[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) zm[j] = sm[sidx(mr.partner, mirror_k1(mr.k2, t + TL::T * j, TL::M))];
+    ESTL_SYNC();  // the buffer is the next passes' exchange space
+    const Ptr<const cf32> h = a.spec.sub(r.spec_off, NH + 2);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k1 = t + TL::T * j;
+      const int k1p = mirror_k1(mr.k2, k1, TL::M);
+      cf32 e, od;
+      real_split(v[j], zm[j], e, od);
+      const cf32 w = twiddle_n(a.bank, a.logn + 1, mr.k2 + (k1 << logn2));
+      const cf32 wo = cmul(w, od);
+      const cf32 xk = cadd(e, wo), xm = cconj(csub(e, wo));
+      const cf32 hk = ldg(h, mr.k2 * TL::M + k1);
+      const cf32 hm = (mr.k2 == 0 && k1 == 0) ? ldg(h, NH) : ldg(h, k2p * TL::M + k1p);
+      const cf32 yk = cmul(xk, hk), ymc = cconj(cmul(xm, hm));
+      const cf32 sum = cadd(yk, ymc), dif = csub(yk, ymc);
+      const cf32 id = cmul(cconj(w), cf32{-dif.y, dif.x});  // i conj(w) (Yk - conj(Ym))
+      v[j] = cconj(cadd(sum, id));
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    if constexpr (TL::P == 1) ESTL_SYNC();
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t + TL::T * j;
+      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logn, mr.k2 * n1));
+    }
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const int k2o = mirror_rows(b, c2, C / 2, n2).k2;
+    const Ptr<cf32> o = a.s2.sub(f * NH, NH);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t2 + TL::T * j;
+      o[(n1 << logn2) + k2o] = sm[sidx(c2, n1)];
+    }
+  }
+};
+
+// C (real input): as ConvOutKernel over the half-length transform; the
+// complex result v_m carries two real outputs, y_{2m} = Re v_m and
+// y_{2m+1} = Im v_m.
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct ConvOutHalfKernel {
+  using TL = Tile<LOGM, LOGE, LOGR>;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int NT = TL::T * C;
+  static constexpr int CS = row_stride(TL::MP, C);
+  static constexpr int EXCH = C * CS;
+  static constexpr int SMEM_ELEMS = EXCH;
+  static_assert(NT <= 1024, "too many threads");
+  static constexpr int MINB = min_blocks(NT, TL::E);
+  struct Sidx {
+    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+  };
+  ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int NH = 1 << a.logn;
+    const int logn1 = a.logn - LOGM;
+    const int nblk = 1 << (logn1 - LOGC);
+    const long long f = cta / nblk;
+    const int n1_0 = (int)(cta - f * nblk) * C;
+    const ConvRow r = a.rows[f];
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, EXCH};
+    const Sidx sidx{};
+    const Ptr<cf32> s2 = a.s2.sub(f * NH + (long long)(n1_0 + c) * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s2[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    if constexpr (TL::P == 1) ESTL_SYNC();
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const Ptr<float> o = a.out.sub(r.out_off, r.out_len);
+    // the reference's 1/K^[0] normalisation: 1 / (N * stored DC), N = 2 N'
+    const float g = r.dc_norm ? 1.f / ((float)(2 * NH) * ldg(a.spec, r.spec_off).x) : 1.f;
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n2 = t2 + TL::T * j;
+      const cf32 val = sm[sidx(c2, n2)];  // conj(v_m)
+      const int m = 2 * (n1_0 + c2 + (n2 << logn1)) - r.out_shift;
+      if (m >= 0 && m < r.out_len) o[m] = val.x * g;
+      if (m + 1 >= 0 && m + 1 < r.out_len) o[m + 1] = -val.y * g;
     }
   }
 };

@@ -90,6 +90,11 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
     const long long rb = (long long)L.sig_rows.size();
     const long long cnt = (long long)kv.second.size();
     const long long fb = (long long)L.filt_rows.size();
+    // four-step lengths run the real-input form (N/2-point complex transforms,
+    // spectrum of N/2 + 1 values, kept in N/2 + 2 slots) unless the caller asks
+    // for complex transforms or split precision
+    const bool half = logn > kSingleMaxLog && !(flags & CONV_COMPLEX) && conv_split(flags) == 0;
+    const long long spec_len = half ? N / 2 + 2 : N;
     for (int i : kv.second) {
       const ConvReq& q = reqs[i];
       const bool new_spectrum = !shared_filter || L.filt_rows.empty();
@@ -110,7 +115,7 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       s.conj = 1.f;
       if (new_spectrum) {
         L.filt_rows.push_back(f);
-        spec += N;
+        spec += spec_len;
       }
       L.sig_rows.push_back(s);
     }
@@ -119,7 +124,7 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       const int lc = single_logc(logn), le = std::min(4, logn);
       const long long grid = (cnt + (1LL << lc) - 1) >> lc;
       const long long fgrid = (fcnt + (1LL << lc) - 1) >> lc;
-      if (flags & CONV_NO_PAIRING) {
+      if (flags & (CONV_NO_PAIRING | CONV_COMPLEX)) {
         if (fcnt) L.launches.push_back(ConvLaunch{CK_SPEC_SINGLE, logn, le, 4, lc, fgrid, logn, fb, fcnt, 0});
         L.launches.push_back(ConvLaunch{CK_CONV_SINGLE, logn, le, 4, lc, grid, logn, rb, cnt, 0});
       } else {
@@ -133,6 +138,18 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
           L.launches.push_back(ConvLaunch{CK_SPEC_PAIR, logn, le, 4, lc, pfgrid, logn, fb, fcnt, 0});
         L.launches.push_back(ConvLaunch{CK_CONV_PAIR, logn, le, 4, lc, pgrid, logn, rb, cnt, 0});
       }
+    } else if (half) {
+      const int lh = logn - 1, logn2 = lh / 2, logn1 = lh - logn2;
+      const int cc = four_step_logc(logn2), cr = four_step_logc(logn1);
+      const long long s_off = scratch;
+      if (fcnt) {
+        L.launches.push_back(ConvLaunch{CK_COL_FILTER_H, logn2, 4, 4, cc, fcnt << (logn1 - cc), lh, fb, fcnt, s_off});
+        L.launches.push_back(ConvLaunch{CK_SPEC_ROW_H, logn1, 4, 4, cr, fcnt << (logn2 - cr), lh, fb, fcnt, s_off});
+      }
+      L.launches.push_back(ConvLaunch{CK_COL_SIGNAL_H, logn2, 4, 4, cc, cnt << (logn1 - cc), lh, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_MID_H, logn1, 4, 4, cr, cnt << (logn2 - cr), lh, rb, cnt, s_off});
+      L.launches.push_back(ConvLaunch{CK_OUT_H, logn2, 4, 4, cc, cnt << (logn1 - cc), lh, rb, cnt, s_off});
+      scratch += cnt * (N / 2);
     } else {
       const int logn2 = logn / 2, logn1 = logn - logn2;
       const int cc = four_step_logc(logn2), cr = four_step_logc(logn1);

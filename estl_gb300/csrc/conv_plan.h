@@ -12,11 +12,16 @@
 
 namespace estl {
 
-enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2, CONV_NO_PAIRING = 4 };
+// CONV_NO_PAIRING: padded lengths <= 2^14 run each request as its own
+// complex transform (no two real requests per transform).  CONV_COMPLEX:
+// every length runs complex transforms (neither pairing nor the real-input
+// four-step form of longer requests).
+enum ConvFlags { CONV_CORRELATE = 1, CONV_REFERENCE_COMPAT = 2, CONV_NO_PAIRING = 4, CONV_COMPLEX = 8 };
 // Bits 8-9 of the flags: the split precision of the FFT stages (SplitKind;
 // 0 = FP32), ESTL_CONV_PRECISION(p) in the C ABI.
 constexpr int kConvSplitShift = 8;
-constexpr int kConvFlagMask = CONV_CORRELATE | CONV_REFERENCE_COMPAT | CONV_NO_PAIRING | (3 << kConvSplitShift);
+constexpr int kConvFlagMask =
+    CONV_CORRELATE | CONV_REFERENCE_COMPAT | CONV_NO_PAIRING | CONV_COMPLEX | (3 << kConvSplitShift);
 inline int conv_split(int flags) { return (flags >> kConvSplitShift) & 3; }
 
 // One convolution request: offsets (in floats) into the caller's packed
@@ -36,11 +41,19 @@ enum ConvLaunchKind {
   CK_OUT = 6,          // column DFT -> real output
   CK_SPEC_PAIR = 7,    // two filters per complex FFT -> the A / B spectra of a request pair, N <= 2^14
   CK_CONV_PAIR = 8,    // two signals per complex FFT -> two outputs, N <= 2^14 (fused)
+  // N > 2^14, real input: every launch runs the N/2-point complex transform of
+  // the request (ConvLaunch::logn = log2 N - 1)
+  CK_COL_FILTER_H = 9,   // column pass of the filters (pairs of reals as complex)
+  CK_SPEC_ROW_H = 10,    // row pass of the filters -> permuted half spectrum + Nyquist term
+  CK_COL_SIGNAL_H = 11,  // column pass of the signals
+  CK_MID_H = 12,         // row DFT, spectrum split, multiply, inverse's input, row DFT, twiddle
+  CK_OUT_H = 13,         // column DFT -> two real outputs per complex value
 };
 
 // launches that read the filter rows (and write spectra)
 inline bool ck_is_filter(int kind) {
-  return kind == CK_SPEC_SINGLE || kind == CK_COL_FILTER || kind == CK_SPEC_ROW || kind == CK_SPEC_PAIR;
+  return kind == CK_SPEC_SINGLE || kind == CK_COL_FILTER || kind == CK_SPEC_ROW || kind == CK_SPEC_PAIR ||
+         kind == CK_COL_FILTER_H || kind == CK_SPEC_ROW_H;
 }
 // single-tile launches (N <= 2^14)
 inline bool ck_is_single(int kind) {

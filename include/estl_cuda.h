@@ -271,6 +271,12 @@ estl_status estl_execute_noalloc(int64_t n, int64_t batch, int direction, const 
  * one forward and one inverse FFT.  This flag runs every request as its own
  * complex transform instead. */
 #define ESTL_CONV_NO_PAIRING 4
+/* Real-input specialisation for padded lengths n > 2^14 (the default in
+ * FP32): each real request runs as an n/2-point complex transform whose
+ * spectrum is split and recombined in the middle kernel, half the bytes of a
+ * complex transform.  This flag (which implies ESTL_CONV_NO_PAIRING) runs
+ * every request of every length as a full complex transform. */
+#define ESTL_CONV_COMPLEX 8
 /* Split precision of the convolution's FFT stages (ESTL_PREC_SPLIT_*), or'd
  * into the flags; 0 = FP32. */
 #define ESTL_CONV_PRECISION(p) ((p) << 8)

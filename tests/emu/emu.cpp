@@ -365,13 +365,19 @@ const std::vector<EmuConvKernel>& emu_conv_kernels() {
   k.push_back(mkc<ConvSingleKernel<M, E, R, C>>(CK_CONV_SINGLE, M, E, R, C)); \
   k.push_back(mkc<SpecPairKernel<M, E, R, C>>(CK_SPEC_PAIR, M, E, R, C));     \
   k.push_back(mkc<ConvPairKernel<M, E, R, C>>(CK_CONV_PAIR, M, E, R, C));
-#define ESTL_XC_COL(M, E, R, C)                                       \
-  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C)); \
-  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));
-#define ESTL_XC_ROW(M, E, R, C)                                     \
-  k.push_back(mkc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C)); \
-  k.push_back(mkc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));
-#define ESTL_XC_OUT(M, E, R, C) k.push_back(mkc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C));
+#define ESTL_XC_COL(M, E, R, C)                                                       \
+  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_FILTER, M, E, R, C));               \
+  k.push_back(mkc<ConvColKernel<M, E, R, C>>(CK_COL_SIGNAL, M, E, R, C));               \
+  k.push_back(mkc<ConvColKernel<M, E, R, C, false, true>>(CK_COL_FILTER_H, M, E, R, C)); \
+  k.push_back(mkc<ConvColKernel<M, E, R, C, false, true>>(CK_COL_SIGNAL_H, M, E, R, C));
+#define ESTL_XC_ROW(M, E, R, C)                                              \
+  k.push_back(mkc<SpecRowKernel<M, E, R, C>>(CK_SPEC_ROW, M, E, R, C));        \
+  k.push_back(mkc<ConvMidKernel<M, E, R, C>>(CK_MID, M, E, R, C));             \
+  k.push_back(mkc<SpecRowHalfKernel<M, E, R, C>>(CK_SPEC_ROW_H, M, E, R, C));  \
+  k.push_back(mkc<ConvMidHalfKernel<M, E, R, C>>(CK_MID_H, M, E, R, C));
+#define ESTL_XC_OUT(M, E, R, C)                                          \
+  k.push_back(mkc<ConvOutKernel<M, E, R, C>>(CK_OUT, M, E, R, C)); \
+  k.push_back(mkc<ConvOutHalfKernel<M, E, R, C>>(CK_OUT_H, M, E, R, C));
 #include "conv_list.inc"
 #define ESTL_XC_SINGLE(M, E, R, C)                                                                       \
   if constexpr (E == 4 && M >= 4 && M <= kConvTcSingleMaxLog) {                                            \

@@ -106,6 +106,7 @@ def test_emulated_shared_filter(emu):
 
 
 NO_PAIRING = 4
+COMPLEX = 8
 
 
 @pytest.mark.parametrize("flags", [0, 1, 2, 3])
@@ -312,3 +313,31 @@ def test_emulated_request_validation(emu):
         arr = np.array([r], dtype=np.int64).ravel()
         rc = emu.emu_conv_run(arr.ctypes.data, 1, 0, 0, z.ctypes.data, z.ctypes.data, z.ctypes.data, err, len(err))
         assert rc == 2 and err.value, r
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2])
+def test_emulated_real_input_four_step(emu, flags):
+    """Padded lengths above 2^14 run the real-input four-step form (each real
+    request as an N/2-point complex transform, the spectrum split through
+    mirrored row pairs): 2^15, 2^16 and 2^17, convolution, correlation and
+    the reference-compatible mode, against the oracle and bit-for-bit
+    the complex form (ESTL_CONV_COMPLEX) within the tolerance."""
+    shapes = [(20000, 700), (16384, 2), (40000, 100), (70000, 33)]
+    reqs, sig, filt, _ = make_requests(shapes, 31)
+    compat = bool(flags & 2)
+    if compat:
+        filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L if compat else L + K - 1
+    half = emu_conv(emu, creqs, sig, filt, oo, flags=flags)
+    full = emu_conv(emu, creqs, sig, filt, oo, flags=flags | COMPLEX)
+    for L, K, so, fo, o in creqs:
+        s, f = sig[so:so + L], filt[fo:fo + K]
+        if compat:
+            ref, n = compat_reference(s, f), L
+        else:
+            ref, n = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1)), L + K - 1
+        assert rel(half[o:o + n], ref) < TOL, (L, K, flags)
+        assert rel(full[o:o + n], ref) < TOL, (L, K, flags)
