@@ -61,6 +61,8 @@ def compact_choice(c):
     """Short text form of an autotuner plan choice."""
     def r32(key):
         return " radix-32" if c.get(key, -1) == 5 else ""
+    if c["mode"] == 0:
+        return "planner default"
     if c["mode"] == 1 and c.get("single_cluster", -1) > 0:
         return f"cluster of {1 << c['single_cluster']} CTAs, N2 2^{c['logn2']}, E 2^{c['single_loge']}"
     if c["mode"] == 1:

@@ -350,6 +350,11 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     Step s{STEP_SINGLE, c->logm, c->loge, c->logr, c->logc, (batch + per - 1) / per, BUF_IN, BUF_OUT,
            0, total, 0, total, batch, logn};
     s.pipe = tc ? 0 : use_pipe(choice, c);
+    // planner default (measured on a GB300, 1 GiB batches): 2^13 runs the
+    // resident radix-32 tile (next transform's bulk copy under this one's
+    // passes), 4.5% faster than the plain tile
+    if (!tc && choice.mode == 0 && choice.pipe == 0 && logn == 13 && find_tile(STEP_SINGLE, 13, c->loge, c->logr, 0, 3))
+      s.pipe = 3;
     s.tc = tc ? 1 : 0;
     p.steps.push_back(s);
     p.hbm_passes = 1;
