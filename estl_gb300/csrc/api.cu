@@ -114,7 +114,7 @@ __global__ void bank_init_kernel(cf32* bank) {
 struct KernelTable {
   std::vector<KernelDesc> descs;
   std::vector<char> attr_set;
-  std::vector<int> resident;  // pipelined kernels: CTAs resident on the device
+  std::vector<int> resident;  // persistent kernels: CTAs resident on the device
 };
 
 static KernelTable& ktable() {
@@ -261,7 +261,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
       if (s != ESTL_OK) return s;
       continue;
     }
-    // pipelined kernels move 16-byte chunks: they need 16-byte aligned data
+    // persistent kernels move 16-byte bulk copies: they need 16-byte aligned data
     const bool aligned = !(((uintptr_t)(src + st.src_off) | (uintptr_t)(dst + st.dst_off)) & 15);
     const int pipe = aligned ? st.pipe : 0;
     const KernelDesc* d = nullptr;

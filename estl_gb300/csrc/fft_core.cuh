@@ -512,7 +512,7 @@ struct TileArgs {
   int logn;        // log2 of the full transform length
   int logn1;       // four-step: log2 N1 (N = N1 * N2)
   float sgn;       // +1 forward; -1 = backward via conj(FFT(conj(x)))
-  long long grid;  // CTAs launched (grid-stride kernels of pipe_core.cuh)
+  long long grid;  // CTAs launched (persistent kernels loop over rows / tiles grid apart)
   int split;       // tensor-core kernels: SplitKind of the radix-16 passes (tc_core.cuh)
   long long* err;  // bulk-load kernels: 1 + the tile whose bounded wait gave up (0 = none)
   const void* tmap = nullptr;  // tensor-map kernels: the CUtensorMap kernel parameter of the input

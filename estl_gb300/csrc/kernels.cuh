@@ -6,7 +6,6 @@
 
 #include "fft_core.cuh"
 #include "bulk_core.cuh"
-#include "pipe_core.cuh"
 #include "resident_core.cuh"
 #include "cluster_core.cuh"
 
@@ -21,7 +20,7 @@ struct KernelDesc {
   int nthreads;
   int smem_bytes;
   const void* fn;
-  int pipe;  // 1: grid-stride cp.async double-buffered variant (pipe_core.cuh); 2: bulk-load ring (bulk_core.cuh);
+  int pipe;  // 0: plain tile; 2: bulk-load ring (bulk_core.cuh);
              // 3 / 4: resident whole transforms with a whole / half exchange buffer (resident_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
   int tmap;  // launched with a 2D tensor map of its input as a second parameter (tma_tile_kernel)
@@ -66,9 +65,6 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_SINGLE(M, E, R, C) make_desc<SingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C)
 #define ESTL_COL(M, E, R, C) make_desc<ColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
 #define ESTL_ROW(M, E, R, C) make_desc<RowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C)
-#define ESTL_PIPE_SINGLE(M, E, R, C) make_desc<PipeSingleKernel<M, E, R, C>>(KIND_SINGLE, M, E, R, C, 1)
-#define ESTL_PIPE_COL(M, E, R, C) make_desc<PipeColKernel<M, E, R, C>>(KIND_COL, M, E, R, C, 1)
-#define ESTL_PIPE_ROW(M, E, R, C) make_desc<PipeRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 1)
 #define ESTL_BULK_ROW(M, E, R, C) make_desc<BulkRowKernel<M, E, R, C>>(KIND_ROW, M, E, R, C, 2)
 #define ESTL_BULK_COL(M, E, R, C) make_tma_desc<BulkColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
 #define ESTL_RES(M, E, R, H) make_desc<ResKernel<M, E, R, H>>(KIND_SINGLE, M, E, R, 0, 2 + H)

@@ -1,13 +1,6 @@
 // Registry of the col tile FFT kernels listed in kernel_list.inc.
 #include "kernels.cuh"
 
-// every pipelined variant must fit the shared memory of one SM
-#define ESTL_X_PIPE_SINGLE(M, E, R, C) \
-  static_assert(PipeSingleKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
-#define ESTL_X_PIPE_COL(M, E, R, C) \
-  static_assert(PipeColKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
-#define ESTL_X_PIPE_ROW(M, E, R, C) \
-  static_assert(PipeRowKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
 #define ESTL_X_TC_SINGLE(M, C) \
   static_assert(SingleKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
 #define ESTL_X_TC_COL(M, C) \
@@ -24,7 +17,6 @@ namespace estl {
 
 static const KernelDesc kTable[] = {
 #define ESTL_X_COL(M, E, R, C) ESTL_COL(M, E, R, C),
-#define ESTL_X_PIPE_COL(M, E, R, C) ESTL_PIPE_COL(M, E, R, C),
 #define ESTL_X_BULK_COL(M, E, R, C) ESTL_BULK_COL(M, E, R, C),
 #define ESTL_X_TC_COL(M, C) ESTL_TC_COL(M, C),
 #define ESTL_X_COLUMN(M, E, C) ESTL_COLUMN(M, E, C),

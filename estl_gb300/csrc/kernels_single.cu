@@ -1,13 +1,6 @@
 // Registry of the single tile FFT kernels listed in kernel_list.inc.
 #include "kernels.cuh"
 
-// every pipelined variant must fit the shared memory of one SM
-#define ESTL_X_PIPE_SINGLE(M, E, R, C) \
-  static_assert(PipeSingleKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
-#define ESTL_X_PIPE_COL(M, E, R, C) \
-  static_assert(PipeColKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
-#define ESTL_X_PIPE_ROW(M, E, R, C) \
-  static_assert(PipeRowKernel<M, E, R, C>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "pipelined tile too large");
 #define ESTL_X_TC_SINGLE(M, C) \
   static_assert(SingleKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
 #define ESTL_X_RES(M, E, R, H) \
@@ -26,7 +19,6 @@ namespace estl {
 
 static const KernelDesc kTable[] = {
 #define ESTL_X_SINGLE(M, E, R, C) ESTL_SINGLE(M, E, R, C),
-#define ESTL_X_PIPE_SINGLE(M, E, R, C) ESTL_PIPE_SINGLE(M, E, R, C),
 #define ESTL_X_TC_SINGLE(M, C) ESTL_TC_SINGLE(M, C),
 #define ESTL_X_RES(M, E, R, H) ESTL_RES(M, E, R, H),
 #define ESTL_X_CLUSTER(N, LR, N2, E) ESTL_CLUSTER_TILE(N, LR, N2, E),

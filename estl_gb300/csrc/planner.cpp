@@ -7,7 +7,6 @@
 #include "bluestein_core.cuh"
 #include "fft_core.cuh"
 #include "bulk_core.cuh"
-#include "pipe_core.cuh"
 #include "resident_core.cuh"
 #include "cluster_core.cuh"
 
@@ -26,9 +25,6 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_SINGLE(M, E, R, C) v.push_back(cfg_of<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
 #define ESTL_X_COL(M, E, R, C) v.push_back(cfg_of<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
 #define ESTL_X_ROW(M, E, R, C) v.push_back(cfg_of<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
-#define ESTL_X_PIPE_SINGLE(M, E, R, C) v.push_back(cfg_of<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
-#define ESTL_X_PIPE_COL(M, E, R, C) v.push_back(cfg_of<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
-#define ESTL_X_PIPE_ROW(M, E, R, C) v.push_back(cfg_of<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) v.push_back(cfg_of<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_BULK_COL(M, E, R, C) v.push_back(cfg_of<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_RES(M, E, R, H) v.push_back(cfg_of<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));
@@ -132,11 +128,11 @@ static const TileCfg* find_tc(int kind, int logm, int logc) {
 // Radix of a tile choice: -1 = radix 16.
 static int lr_of(int logr) { return logr < 0 ? 4 : logr; }
 
-// Whether a step of this configuration runs as its pipelined variant.
+// Which variant of a tile a step runs: ch.pipe (2 bulk-load, 3 / 4 resident)
+// where that variant exists, else the plain tile.
 static int use_pipe(const PlanChoice& ch, const TileCfg* c) {
-  if (ch.pipe == 0) return 0;
-  const int want = ch.pipe >= 2 ? ch.pipe : 1;
-  return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, want) ? want : 0;
+  if (ch.pipe < 2) return 0;
+  return find_tile(c->kind, c->logm, c->loge, c->logr, c->logc, ch.pipe) ? ch.pipe : 0;
 }
 
 int ilog2_exact(long long n) {
@@ -578,7 +574,7 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
         for (const TileCfg& r : tile_configs()) {
           if (r.kind != STEP_ROW || r.logm != logn1 || r.logc > logn2 || r.pipe || r.tc) continue;
           for (long long chunk : {0LL, 16LL << 20, 128LL << 20}) {
-           for (int pipe : {0, 1, 2}) {
+           for (int pipe : {0, 2}) {
             PlanChoice ch;
             ch.mode = 2;
             ch.logn2 = logn2;

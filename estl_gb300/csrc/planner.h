@@ -27,7 +27,7 @@ struct TileCfg {
   int logm, loge, logr, logc;
   int nthreads;
   int smem_bytes;
-  int pipe;  // pipelined (grid-stride, cp.async double-buffered) variant
+  int pipe;  // 0 plain; 2 bulk-load ring (bulk_core.cuh); 3 / 4 resident whole transforms (resident_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (split precision)
   int cluster = 0;  // cluster tiles (cluster_core.cuh): log2 CTAs per cluster, 0 otherwise
   int csplit = 0;   // cluster tiles: log2 of the column DFT length N2
@@ -51,7 +51,7 @@ struct Step {
   // and scratch ring (transforms)
   int rlogm = 0, rloge = 0, rlogc = 0;
   int lag = 0, ring = 0;
-  // pipelined variant (grid = tiles; the launcher runs min(tiles, resident CTAs))
+  // persistent variant (pipe >= 2; grid = tiles, the launcher runs min(tiles, resident CTAs))
   int pipe = 0;
   // tensor-core variant (radix-16 passes as split-precision GEMMs)
   int tc = 0;
@@ -83,7 +83,7 @@ struct PlanChoice {
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
   int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
-  int pipe = 0;         // tile kernels: 0 plain, 1 pipelined variant (where one exists), -1 pipelined if any
+  int pipe = 0;         // tile kernels: 0 plain, 2 bulk-load, 3 / 4 resident (where the variant exists)
   int split = 0;        // 0 FP32; else the SplitKind of tensor-core radix-16 passes (tc_core.cuh)
   // log2 of the largest radix of the single / column / row tiles (-1 = 4:
   // radix 16; 5: radix-32 passes, 32 elements per thread)

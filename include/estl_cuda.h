@@ -101,10 +101,10 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
  * explicit_tiles != 0 (modes 1 and 2) also fixes the tile kernels, each field
  * -1 for the planner's choice: split_log2 = log2 N2 of N = N1 * N2 (the column
  * DFT length), *_loge = log2 elements per thread, *_logc = log2 transforms
- * (single) or columns / rows (four-step) per CTA, pipelined = 1 for the
- * cp.async double-buffered variant where one exists, 2 for the persistent
- * bulk-load variants (row tiles by bulk copies, column tiles by 2D tensor
- * copies).  Mode 4 reads split_log2 as log2 R and split2_log2 as log2 Q
+ * (single) or columns / rows (four-step) per CTA, pipelined = 2 for the
+ * persistent bulk-load variants (row tiles by bulk copies, column tiles by 2D
+ * tensor copies), 3 / 4 for the resident single tiles (whole / half exchange
+ * buffer; 2^12..2^14).  Mode 4 reads split_log2 as log2 R and split2_log2 as log2 Q
  * (0 or -1 = default).  *_logr: log2 of the largest radix of the tile
  * (-1 or 4: radix 16; 5: radix-32 passes with 32 elements per thread).  A zero-initialised struct with mode = 0 is the
  * automatic plan. */

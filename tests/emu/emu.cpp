@@ -28,7 +28,6 @@
 #include "bulk_core.cuh"
 #include "conv2d_core.cuh"
 #include "estl_cuda.h"
-#include "pipe_core.cuh"
 #include "resident_core.cuh"
 #include "cluster_core.cuh"
 #include "stream_core.cuh"
@@ -81,9 +80,6 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_SINGLE(M, E, R, C) k.push_back(mk<SingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C));
 #define ESTL_X_COL(M, E, R, C) k.push_back(mk<ColKernel<M, E, R, C>>(STEP_COL, M, E, R, C));
 #define ESTL_X_ROW(M, E, R, C) k.push_back(mk<RowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C));
-#define ESTL_X_PIPE_SINGLE(M, E, R, C) k.push_back(mk<PipeSingleKernel<M, E, R, C>>(STEP_SINGLE, M, E, R, C, 1));
-#define ESTL_X_PIPE_COL(M, E, R, C) k.push_back(mk<PipeColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 1));
-#define ESTL_X_PIPE_ROW(M, E, R, C) k.push_back(mk<PipeRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 1));
 #define ESTL_X_BULK_ROW(M, E, R, C) k.push_back(mk<BulkRowKernel<M, E, R, C>>(STEP_ROW, M, E, R, C, 2));
 #define ESTL_X_BULK_COL(M, E, R, C) k.push_back(mk<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_RES(M, E, R, H) k.push_back(mk<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));

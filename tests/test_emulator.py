@@ -24,7 +24,7 @@ def rand_c64(shape, seed):
 
 def pad_choice(choice):
     """PlanChoice fields: mode, single_loge, single_logc, logn2, col_loge,
-    col_logc, row_loge, row_logc, chunk, lag, pipe (-1 = pipelined if available),
+    col_logc, row_loge, row_logc, chunk, lag, pipe (0 plain, 2 bulk-load, 3 / 4 resident),
     split (0 FP32, 1 fp16x2, 2 bf16x2, 3 bf16x3 tensor-core radix-16 passes),
     logn3 (three-pass: log2 of the second column DFT length, 0 = default),
     single_logr, col_logr, row_logr (log2 largest radix, -1 = 16),
@@ -91,7 +91,7 @@ def test_every_single_kernel_config(emu, logn):
 @pytest.mark.parametrize("logn", [14, 16, 19])
 def test_every_four_step_config(emu, logn):
     """Every column tile and every row tile the autotuner may pick (each at
-    least once, plain and pipelined), with a chunk of two transforms."""
+    least once, plain and bulk-load), with a chunk of two transforms."""
     n = 1 << logn
     cands = [c for c in candidates(emu, n, 2) if c[0] == 2]
     assert cands
