@@ -397,8 +397,10 @@ def bench_config1(estl, torch, autotune=True):
 
 def bench_uneven(estl, torch):
     """8192 transforms, lengths log-uniform over 2^6..2^16, complex N(0,1),
-    seed 3, packed with an offsets array: one persistent launch vs one launch
-    per size class (both replayed as CUDA graphs)."""
+    seed 3, packed with an offsets array: one persistent launch, one launch
+    of the packed kernel per size class, and the bucketed mode (the engine's
+    own autotuned plan per length through the offsets, buckets as parallel
+    graph branches); all replayed as CUDA graphs."""
     import ctypes
 
     import numpy as np
@@ -415,7 +417,9 @@ def bench_uneven(estl, torch):
     L = lib()
     res = {"workload": "8192 C2C FP32 transforms, N log-uniform 2^6..2^16, packed, N(0,1) seed 3",
            "elements": total}
-    for mode, name in ((0, "persistent"), (1, "per_size")):
+    for n in sorted(set(int(v) for v in sizes)):  # the bucketed mode's plans: the autotuner's choice per length
+        estl.autotune(n, int((sizes == n).sum()), iters=5)
+    for mode, name in ((0, "persistent"), (1, "per_size"), (2, "bucketed")):
         plan = ctypes.c_void_p()
         check(L.estl_packed_plan_create(offsets.ctypes.data, sizes.ctypes.data, 8192, -1, mode, ctypes.byref(plan)))
         st = torch.cuda.current_stream().cuda_stream
@@ -439,6 +443,7 @@ def bench_uneven(estl, torch):
                      "gflops": round(d["flops"] / (ms * 1e-3) / 1e9, 1), "launches": d["launches"]}
         L.estl_packed_plan_destroy(plan)
     res["persistent_speedup"] = round(res["per_size"]["ms"] / res["persistent"]["ms"], 3)
+    res["bucketed_vs_persistent"] = round(res["persistent"]["ms"] / res["bucketed"]["ms"], 3)
     return res
 
 

@@ -258,7 +258,7 @@ class PackedPlan:
     whose CTAs take work items from a device queue; "per_size": one launch per
     size class.  The reference has one FFT object per size (tests/Test.cpp:45-60)."""
 
-    MODES = {"persistent": 0, "per_size": 1}
+    MODES = {"persistent": 0, "per_size": 1, "bucketed": 2}
 
     def __init__(self, offsets, sizes, direction=FORWARD, mode="persistent"):
         import numpy as np

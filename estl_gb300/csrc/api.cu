@@ -242,8 +242,33 @@ static estl_status encode_column_map(CUtensorMap* map, const cf32* base, const S
   return ESTL_OK;
 }
 
+estl_status prepare_steps(const Plan1D& plan) {
+  for (const Step& st : plan.steps) {
+    if (st.kind == STEP_STREAM || st.kind == STEP_COPY) continue;
+    const KernelDesc* d = nullptr;
+    estl_status s = lookup_kernel(st, st.pipe, &d);
+    if (s != ESTL_OK) return s;
+    if (st.pipe) {
+      s = lookup_kernel(st, 0, &d);  // the plain tile, run when buffers are not 16-byte aligned
+      if (s != ESTL_OK) return s;
+    }
+  }
+  return ESTL_OK;
+}
+
+estl_status take_bulk_wait_error() {
+  long long e = 0;
+  estl_status s = check_cuda(cudaMemcpy(&e, engine().dev_err, sizeof(e), cudaMemcpyDeviceToHost), "cudaMemcpy(error word)");
+  if (s != ESTL_OK || !e) return s;
+  cudaMemset(engine().dev_err, 0, sizeof(long long));
+  if (e & kErrCopiesInFlight)
+    return fail(ESTL_DEVICE_ERROR, "a bulk-load wait gave up (tile %lld) and its copies in flight did not drain",
+                (e & ~kErrCopiesInFlight) - 1);
+  return fail(ESTL_TIMEOUT, "a bulk-load wait gave up (tile %lld)", e - 1);
+}
+
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream, const StreamAux* aux) {
+                         cudaStream_t stream, const StreamAux* aux, const long long* xoff, long long extent) {
   Engine& E = engine();
   for (const Step& st : plan.steps) {
     if (st.kind == STEP_STREAM) {
@@ -283,6 +308,16 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     a.err = E.dev_err;
     a.ologr = st.ologr;
     if (st.ologr) a.sgn = 1.f;  // middle pass of three: its input is conjugated already
+    if (xoff) {
+      // transforms at the caller's offsets: whole buffers, the step's transforms' offsets
+      if (d->tmap || st.src == BUF_OUT || st.ologr)
+        return fail(ESTL_UNSUPPORTED_SIZE, "a plan step that cannot read transforms through offsets");
+      const long long n = 1LL << st.logn;
+      const long long first = st.src == BUF_IN ? st.src_off / n : st.dst_off / n;
+      if (st.src == BUF_IN) a.in = Ptr<const cf32>{in, extent};
+      if (st.dst == BUF_OUT) a.out = Ptr<cf32>{out, extent};
+      a.xoff = Ptr<const long long>{xoff + first, st.rows};
+    }
     alignas(64) CUtensorMap map;
     if (d->tmap) {
       s = encode_column_map(&map, src + st.src_off, st);

@@ -175,7 +175,9 @@ struct BulkRowKernel {
     const long long N = 1LL << a.logn;
     bulk_fence_proxy();
     mbar_expect_tx(bar, (uint32_t)(C * TL::M * sizeof(cf32)));
-    for (int c = 0; c < C; ++c) bulk_load(stage, (long long)c * RS, a.in, f * N + (long long)(k2_0 + c) * TL::M, TL::M, bar);
+    // N2 = 1 (whole transforms): the rows are the caller's transforms
+    const long long base = logn2 == 0 ? xbase(a, f, N) : f * N;
+    for (int c = 0; c < C; ++c) bulk_load(stage, (long long)c * RS, a.in, base + (long long)(k2_0 + c) * TL::M, TL::M, bar);
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
@@ -216,7 +218,7 @@ struct BulkRowKernel {
       if (tid == 0 && tile + 2 * grid < nt) issue(a, tile + 2 * grid, stage, &bar[s]);
       const long long f = tile / nblk;
       const int k2_0 = (int)(tile - f * nblk) * C;
-      const Ptr<cf32> out = a.out.sub(f * N, N);
+      const Ptr<cf32> out = a.out.sub(xbase(a, f, N), N);
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) stcs(out, k2_0 + c + ((t + TL::T * j) << logn2), conj_if(v[j], a.sgn));
     }

@@ -131,8 +131,8 @@ struct ClusterKernel {
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
     const int rank = (int)(cta & (R - 1));
     const long long f = cta >> LOGR;  // the grid is exactly rows * R CTAs
-    const Ptr<const cf32> in = a.in.sub(f * N, N);
-    const Ptr<cf32> out = a.out.sub(f * N, N);
+    const Ptr<const cf32> in = a.in.sub(xbase(a, f, N), N);
+    const Ptr<cf32> out = a.out.sub(xbase(a, f, N), N);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
     cf32 v[TA::E];
     // phase A: column DFTs of this CTA's W columns

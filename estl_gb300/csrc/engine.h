@@ -66,10 +66,21 @@ estl_status stream_prepare(const Plan1D& plan, void* aux, size_t aux_bytes, Stre
 estl_status launch_stream(const Step& st, const cf32* in, cf32* out, cf32* scratch, long long scratch_elems,
                           const StreamAux& aux, float sgn, cudaStream_t stream);
 
+// Kernel attributes of every step of a plan set now (before a stream capture).
+estl_status prepare_steps(const Plan1D& plan);
+// Reads and clears the bulk-load kernels' wait-timeout word (after a device
+// synchronisation): ESTL_TIMEOUT if a wait gave up, ESTL_DEVICE_ERROR if its
+// copies in flight did not drain either, else ESTL_OK.
+estl_status take_bulk_wait_error();
+
 // Launches one plan's steps on `stream`.  in/out/scratch are device
 // pointers of interleaved complex64; sgn = +1 forward, -1 backward.  aux is
-// the work list of a streamed plan (else unused).
+// the work list of a streamed plan (else unused).  xoff (device, one element
+// offset per transform of the plan) places transform f at in/out + xoff[f]
+// instead of f * n, in buffers of `extent` elements (bucketed uneven
+// batches; single, column, row and resident tiles; no tensor-copy tiles).
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream, const StreamAux* aux = nullptr);
+                         cudaStream_t stream, const StreamAux* aux = nullptr, const long long* xoff = nullptr,
+                         long long extent = 0);
 
 }  // namespace estl

@@ -517,7 +517,15 @@ struct TileArgs {
   long long* err;  // bulk-load kernels: 1 + the tile whose bounded wait gave up (0 = none)
   const void* tmap = nullptr;  // tensor-map kernels: the CUtensorMap kernel parameter of the input
   int ologr = 0;  // column tiles: interleaved output of a three-pass plan's middle pass (planner.h Step::ologr)
+  // Uneven batches (bucketed packed plans): element offset of each transform
+  // of the step in the caller's input (single, column and resident tiles) and
+  // output (single, row and resident tiles) buffers; p == nullptr: transform
+  // f at f * N.  The four-step scratch stays dense.
+  Ptr<const long long> xoff{nullptr, 0};
 };
+
+// Element offset of transform f of a step in the caller's buffers.
+ESTL_HD long long xbase(const TileArgs& a, long long f, long long n) { return a.xoff.p ? a.xoff[f] : f * n; }
 
 ESTL_HD void atomic_max_ll(long long* p, long long v) {
 #if defined(__CUDA_ARCH__)
@@ -584,8 +592,9 @@ struct SingleKernel {
     const int c = tid >> TL::LOGT;
     const long long row = cta * C + c;
     const bool valid = row < a.rows;
-    const Ptr<const cf32> in = valid ? a.in.sub(row * TL::M, TL::M) : Ptr<const cf32>{a.in.p, 0};
-    const Ptr<cf32> out = valid ? a.out.sub(row * TL::M, TL::M) : Ptr<cf32>{a.out.p, 0};
+    const long long base = valid ? xbase(a, row, TL::M) : 0;
+    const Ptr<const cf32> in = valid ? a.in.sub(base, TL::M) : Ptr<const cf32>{a.in.p, 0};
+    const Ptr<cf32> out = valid ? a.out.sub(base, TL::M) : Ptr<cf32>{a.out.p, 0};
     body(in, out, valid, tid, smraw, a.bank, a.sgn, a.split);
   }
 };
@@ -699,7 +708,7 @@ struct ColKernel {
     const int nblk = (1 << logn1) >> LOGC;
     const long long f = cta / nblk;
     const int n1_0 = (int)(cta - f * nblk) * C;
-    body(a.in.sub(f * N, N), out_of(a.out, f, a.logn, a.ologr), n1_0, a.logn, tid, smraw, a.bank, a.sgn, a.split,
+    body(a.in.sub(xbase(a, f, N), N), out_of(a.out, f, a.logn, a.ologr), n1_0, a.logn, tid, smraw, a.bank, a.sgn, a.split,
          a.ologr);
   }
 };
@@ -759,7 +768,7 @@ struct RowKernel {
     // the scratch written by the column pass is read-only here
     const Ptr<cf32> in{const_cast<cf32*>(a.in.p) + f * N, N};
     ESTL_CHECK(f * N + N, a.in.n + 1, "row pass input range");
-    body(in, a.out.sub(f * N, N), k2_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
+    body(in, a.out.sub(xbase(a, f, N), N), k2_0, a.logn, tid, smraw, a.bank, a.sgn, a.split);
   }
 };
 

@@ -10,6 +10,7 @@
 
 #include "engine.h"
 #include "packed_core.cuh"
+#include "tuner.h"
 
 namespace estl {
 
@@ -50,11 +51,36 @@ struct estl_packed_plan_s {
   // test hook (estl_packed_plan_set_test_hook)
   int test_skip_kind = -1;
   unsigned long long test_spin_limit = 0;
+  // ESTL_PACKED_BUCKETED: one engine plan per length, branches of the graph
+  bool bucketed = false;
+  std::vector<PackedBucket> buckets;
+  std::vector<long long*> b_xoff;   // device offsets of each bucket (in the workspace)
+  std::vector<cf32*> b_scratch;     // dense four-step scratch of each bucket (in the workspace)
+  std::vector<cudaStream_t> b_streams;
+  std::vector<cudaEvent_t> b_events;  // [0] fork, [1 + k] join of bucket k
+  long long b_total = 0;              // extent of the caller's buffers (elements)
 };
 
 static size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Bucketed mode: every bucket's plan on its own stream, forked from and
+// joined back into `st` (parallel branches when captured in a graph).
+static estl_status bucketed_enqueue(estl_packed_plan p, const cf32* in, cf32* out, cudaStream_t st) {
+  const float sgn = p->direction == ESTL_FORWARD ? 1.f : -1.f;
+  estl_status s = check_cuda(cudaEventRecord(p->b_events[0], st), "cudaEventRecord(fork)");
+  for (size_t k = 0; k < p->buckets.size() && s == ESTL_OK; ++k) {
+    s = check_cuda(cudaStreamWaitEvent(p->b_streams[k], p->b_events[0], 0), "cudaStreamWaitEvent(fork)");
+    if (s == ESTL_OK)
+      s = launch_steps(p->buckets[k].plan, in, out, p->b_scratch[k], sgn, p->b_streams[k], nullptr, p->b_xoff[k],
+                       p->b_total);
+    if (s == ESTL_OK) s = check_cuda(cudaEventRecord(p->b_events[1 + k], p->b_streams[k]), "cudaEventRecord(join)");
+    if (s == ESTL_OK) s = check_cuda(cudaStreamWaitEvent(st, p->b_events[1 + k], 0), "cudaStreamWaitEvent(join)");
+  }
+  return s;
+}
+
 static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out, cudaStream_t st) {
+  if (p->bucketed) return bucketed_enqueue(p, in, out, st);
   Engine& E = engine();
   const PackedLayout& L = p->layout;
   estl_status s = check_cuda(cudaMemsetAsync(p->counters, 0, p->counter_bytes, st), "cudaMemsetAsync(counters)");
@@ -93,6 +119,10 @@ static void packed_release(estl_packed_plan p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  for (cudaStream_t s : p->b_streams)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : p->b_events)
+    if (e) cudaEventDestroy(e);
   dev_free(p->ws, p->ws_bytes);
   delete p;
 }
@@ -106,9 +136,59 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
   estl_status s = require_init();
   if (s != ESTL_OK) return s;
   if (direction != ESTL_FORWARD && direction != ESTL_BACKWARD) return fail(ESTL_INVALID_ARG, "bad direction %d", direction);
-  if (mode != ESTL_PACKED_PERSISTENT && mode != ESTL_PACKED_PER_SIZE) return fail(ESTL_INVALID_ARG, "bad mode %d", mode);
+  if (mode != ESTL_PACKED_PERSISTENT && mode != ESTL_PACKED_PER_SIZE && mode != ESTL_PACKED_BUCKETED)
+    return fail(ESTL_INVALID_ARG, "bad mode %d", mode);
   std::unique_ptr<estl_packed_plan_s> p(new estl_packed_plan_s);
   std::string err;
+  if (mode == ESTL_PACKED_BUCKETED) {
+    auto choose = [](long long n, long long c) {
+      PlanChoice ch;
+      tuner_lookup(n, c, &ch);
+      return ch;
+    };
+    if (!build_packed_buckets(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
+                              count, +choose, &p->buckets, &p->b_total, &err))
+      return fail(ESTL_INVALID_ARG, "%s", err.c_str());
+    p->bucketed = true;
+    p->direction = direction;
+    // workspace: per bucket its offsets, then its scratch
+    size_t off = 0;
+    std::vector<size_t> o_x, o_s;
+    for (const PackedBucket& b : p->buckets) {
+      o_x.push_back(off);
+      off = up256(off + b.xoff.size() * sizeof(long long));
+      o_s.push_back(off);
+      off = up256(off + (size_t)b.plan.scratch_elems * sizeof(cf32));
+    }
+    p->ws_bytes = std::max<size_t>(off, 256);
+    s = dev_alloc(&p->ws, p->ws_bytes, "bucketed packed plan workspace");
+    if (s != ESTL_OK) return s;
+    char* w = static_cast<char*>(p->ws);
+    for (size_t k = 0; k < p->buckets.size() && s == ESTL_OK; ++k) {
+      p->b_xoff.push_back(reinterpret_cast<long long*>(w + o_x[k]));
+      p->b_scratch.push_back(reinterpret_cast<cf32*>(w + o_s[k]));
+      s = check_cuda(cudaMemcpy(p->b_xoff[k], p->buckets[k].xoff.data(), p->buckets[k].xoff.size() * sizeof(long long),
+                                cudaMemcpyHostToDevice),
+                     "cudaMemcpy(bucket offsets)");
+      if (s == ESTL_OK) s = prepare_steps(p->buckets[k].plan);
+      cudaStream_t bs = nullptr;
+      if (s == ESTL_OK) s = check_cuda(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "cudaStreamCreate");
+      p->b_streams.push_back(bs);
+    }
+    for (size_t k = 0; k <= p->buckets.size() && s == ESTL_OK; ++k) {
+      cudaEvent_t e = nullptr;
+      s = check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+      p->b_events.push_back(e);
+    }
+    if (s == ESTL_OK)
+      s = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (s != ESTL_OK) {
+      packed_release(p.release());
+      return s;
+    }
+    *plan = p.release();
+    return ESTL_OK;
+  }
   if (!build_packed_layout(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
                            count, mode == ESTL_PACKED_PERSISTENT, &p->layout, &err))
     return fail(ESTL_INVALID_ARG, "%s", err.c_str());
@@ -212,6 +292,7 @@ estl_status estl_packed_check(estl_packed_plan p) {
   if (!p) return fail(ESTL_INVALID_ARG, "NULL plan");
   estl_status s = check_cuda(cudaDeviceSynchronize(), "packed execute");
   if (s != ESTL_OK) return s;
+  if (p->bucketed) return take_bulk_wait_error();
   int e = 0;
   s = check_cuda(cudaMemcpy(&e, p->error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
   if (s != ESTL_OK) return s;
@@ -238,6 +319,28 @@ estl_status estl_packed_plan_set_test_hook(estl_packed_plan p, int skip_column_i
 
 estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len) {
   if (!p || !buf || !len) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
+  if (p->bucketed) {
+    std::string d = "{\"mode\": \"bucketed\", \"buckets\": [";
+    long long elems = 0, launches = 0;
+    double flops = 0;
+    for (size_t k = 0; k < p->buckets.size(); ++k) {
+      const PackedBucket& b = p->buckets[k];
+      const long long c = (long long)b.xoff.size();
+      elems += c << b.logn;
+      flops += 5.0 * (double)(c << b.logn) * b.logn;
+      launches += (long long)b.plan.steps.size();
+      d += (k ? ", " : "") + b.plan.describe();
+    }
+    size_t ntf = 0;
+    for (const PackedBucket& b : p->buckets) ntf += b.xoff.size();
+    char tail[256];
+    std::snprintf(tail, sizeof tail, "], \"transforms\": %zu, \"launches\": %lld, \"elements\": %lld, \"flops\": %.6g}",
+                  ntf, launches, elems, flops);
+    d += tail;
+    if (d.size() + 1 > len) return fail(ESTL_INVALID_ARG, "describe buffer of %zu bytes is too small", len);
+    std::snprintf(buf, len, "%s", d.c_str());
+    return ESTL_OK;
+  }
   const PackedLayout& L = p->layout;
   std::snprintf(buf, len,
                 "{\"transforms\": %zu, \"items\": %zu, \"launches\": %zu, \"persistent\": %s, \"grid\": %d, "

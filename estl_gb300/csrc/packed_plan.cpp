@@ -134,4 +134,51 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
   return true;
 }
 
+bool build_packed_buckets(const long long* offsets, const long long* sizes, long long count,
+                          PlanChoice (*choose)(long long n, long long count), std::vector<PackedBucket>* out,
+                          long long* total_elems, std::string* err) {
+  PackedLayout L;  // the validation of the persistent layout (lengths, offsets, overlaps)
+  if (!build_packed_layout(offsets, sizes, count, false, &L, err)) return false;
+  std::vector<PackedBucket> buckets;
+  for (int l = kPackedMinLog; l <= kPackedMaxLog; ++l) {
+    PackedBucket b;
+    b.logn = l;
+    bool odd = false;
+    for (long long i = 0; i < count; ++i)
+      if (L.lognv[i] == l) {
+        b.xoff.push_back(offsets[i]);
+        odd = odd || (offsets[i] & 1);
+      }
+    if (b.xoff.empty()) continue;
+    const long long n = 1LL << l, c = (long long)b.xoff.size();
+    PlanChoice ch = choose ? choose(n, c) : PlanChoice{};
+    std::string e;
+    if (!make_plan(n, c, ch, &b.plan, &e) && !make_plan(n, c, PlanChoice{}, &b.plan, &e)) {
+      if (err) *err = e;
+      return false;
+    }
+    bool dense_only = false;  // steps that read a transform's columns through a 2D view
+    for (Step& st : b.plan.steps) {
+      if (st.kind == STEP_STREAM || st.ologr || st.src == BUF_OUT) dense_only = true;
+      if (st.kind == STEP_COL && st.pipe == 2) st.pipe = 0;  // plain column tile: loads through the offsets
+      if (odd && st.pipe >= 2) st.pipe = 0;                   // bulk copies need 16-byte aligned rows
+    }
+    if (dense_only) {
+      // plans of streamed or three passes: the default four-step instead
+      PlanChoice four;
+      four.mode = 2;
+      if (!make_plan(n, c, four, &b.plan, &e)) {
+        if (err) *err = e;
+        return false;
+      }
+      for (Step& st : b.plan.steps)
+        if (st.pipe && (st.kind == STEP_COL || odd)) st.pipe = 0;
+    }
+    buckets.push_back(std::move(b));
+  }
+  *total_elems = L.total_elems;
+  *out = std::move(buckets);
+  return true;
+}
+
 }  // namespace estl

@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include "planner.h"
+
 namespace estl {
 
 enum PackedItemKind { PK_SINGLE = 0, PK_COL = 1, PK_ROW = 2 };
@@ -53,5 +55,24 @@ struct PackedLayout {
 // transforms.
 bool build_packed_layout(const long long* offsets, const long long* sizes, long long count, bool persistent,
                          PackedLayout* out, std::string* err);
+
+// Bucketed uneven batches: one size class of the batch, run by the engine's
+// own plan for (2^logn, count) over the class's transforms through their
+// offsets (TileArgs::xoff), the four-step scratch dense per class.
+struct PackedBucket {
+  int logn = 0;
+  Plan1D plan;                  // planned for the class's transform count
+  std::vector<long long> xoff;  // element offset of each transform of the class, in class order
+};
+
+// Groups the batch by length and plans each class with choose(n, count)
+// (the autotuner's cache on the device, the planner default in the
+// emulator).  Column passes run their plain tiles (the tensor-copy variant
+// needs a regular 2D view of the input), and a class with an odd offset runs
+// no bulk-copy variant (16-byte aligned rows).  Validation as
+// build_packed_layout.
+bool build_packed_buckets(const long long* offsets, const long long* sizes, long long count,
+                          PlanChoice (*choose)(long long n, long long count), std::vector<PackedBucket>* out,
+                          long long* total_elems, std::string* err);
 
 }  // namespace estl

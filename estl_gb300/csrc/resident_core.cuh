@@ -91,7 +91,8 @@ struct ResKernel {
   ESTL_HD static void issue(const TileArgs& a, long long tile, const Ptr<cf32>& land, uint64_t* bar) {
     bulk_fence_proxy();
     mbar_expect_tx(bar, (uint32_t)(M * sizeof(cf32)));
-    for (int c = 0; c < M; c += COPY) bulk_load(land, c, a.in, tile * M + c, COPY, bar);
+    const long long base = xbase(a, tile, M);
+    for (int c = 0; c < M; c += COPY) bulk_load(land, c, a.in, base + c, COPY, bar);
   }
 
   ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
@@ -125,7 +126,7 @@ struct ResKernel {
       ESTL_SYNC();  // every thread holds its elements: the landing zone is free
       if (tid == 0 && tile + grid < nt) issue(a, tile + grid, land, bar);
       run_passes_halves<TL, 0, H>(v, t, xb, tw);
-      const Ptr<cf32> out = a.out.sub(tile * M, M);
+      const Ptr<cf32> out = a.out.sub(xbase(a, tile, M), M);
 #pragma unroll
       for (int j = 0; j < TL::E; ++j) stcs(out, t + TL::T * j, conj_if(v[j], a.sgn));
     }

@@ -362,6 +362,13 @@ estl_status estl_conv2d_plan_destroy(estl_conv2d_plan plan);
  *   (d_in, d_out) pair in a CUDA graph and replayed. */
 #define ESTL_PACKED_PERSISTENT 0
 #define ESTL_PACKED_PER_SIZE 1
+/* ESTL_PACKED_BUCKETED: one bucket per length, each run by the engine's own
+ * plan for (length, count) -- the autotuner's cached choice if there is one,
+ * else the planner default: single-CTA, resident or thread-block-cluster tiles
+ * in one pass, four-step through a dense per-bucket scratch above -- reading
+ * and writing the transforms through their offsets.  The buckets are parallel
+ * branches of the captured CUDA graph. */
+#define ESTL_PACKED_BUCKETED 2
 typedef struct estl_packed_plan_s* estl_packed_plan;
 estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
                                     int mode, estl_packed_plan* plan);

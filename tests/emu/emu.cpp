@@ -492,7 +492,8 @@ extern "C" {
 // choice: 16 ints (PlanChoice fields) or NULL for the planner default.
 // sign: -1 forward, +1 backward.  Returns 0 ok, 1 out-of-bounds access,
 // 2 plan error, 3 missing kernel.
-static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen);
+static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen,
+                    const long long* xoff = nullptr, long long extent = 0);
 
 int emu_plan_run(long long n, long long batch, const int* choice, int sign, const float* in, float* out, char* err,
                  int errlen) {
@@ -563,13 +564,14 @@ int emu_bluestein_run(long long n, long long batch, int sign, const float* in, f
   return 0;
 }
 
-static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen) {
+static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char* err, int errlen,
+                    const long long* xoff, long long extent) {
   const long long n = p.n, batch = p.batch;
   {
     std::lock_guard<std::mutex> g(g_msg_mu);
     g_msg.clear();
   }
-  const long long total = n * batch;
+  const long long total = xoff ? extent : n * batch;
   std::vector<cf32> scratch((size_t)std::max<long long>(p.scratch_elems, 1),
                             cf32{std::numeric_limits<float>::quiet_NaN(), 0.f});
   const cf32* cin = reinterpret_cast<const cf32*>(in);
@@ -648,6 +650,17 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
     a.sgn = sign < 0 ? 1.f : -1.f;
     a.ologr = st.ologr;
     if (st.ologr) a.sgn = 1.f;  // middle pass of three: its input is conjugated already
+    if (xoff) {
+      // transforms at the caller's offsets (bucketed uneven batches), as launch_steps
+      if (st.src == BUF_OUT || st.ologr || (k->pipe == 2 && st.kind == STEP_COL)) {
+        set_err(err, errlen, "a plan step that cannot read transforms through offsets");
+        return 2;
+      }
+      const long long first = st.src == BUF_IN ? st.src_off >> st.logn : st.dst_off >> st.logn;
+      if (st.src == BUF_IN) a.in = Ptr<const cf32>{cin, extent};
+      if (st.dst == BUF_OUT) a.out = Ptr<cf32>{cout, extent};
+      a.xoff = Ptr<const long long>{xoff + first, st.rows};
+    }
     // pipelined kernels are grid-stride: emulate one or two CTAs so that every
     // CTA loops over several tiles and uses both tile buffers
     const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
@@ -691,6 +704,25 @@ int emu_cluster_barrier_selftest(int ncta, int nt, int cluster_barrier) {
     worst = std::min(worst, ok);
   }
   return worst;
+}
+
+// Bucketed uneven batch (build_packed_buckets with the planner defaults):
+// every bucket's plan through the transforms' offsets.  Returns 0, 1 (out of
+// bounds), 2 (layout error) or 3 (missing kernel).
+int emu_packed_bucketed_run(const long long* offsets, const long long* sizes, long long count, int sign,
+                            const float* in, float* out, char* err, int errlen) {
+  std::vector<PackedBucket> buckets;
+  long long extent = 0;
+  std::string e;
+  if (!build_packed_buckets(offsets, sizes, count, nullptr, &buckets, &extent, &e)) {
+    set_err(err, errlen, e);
+    return 2;
+  }
+  for (const PackedBucket& b : buckets) {
+    const int rc = run_plan(b.plan, sign, in, out, err, errlen, b.xoff.data(), extent);
+    if (rc) return rc;
+  }
+  return 0;
 }
 
 // Plan description (JSON) for (n, batch, choice); returns 0 or 2.
