@@ -45,7 +45,7 @@ def parse():
                     help="comma-separated subset of the other configurations (plain_4096x256, uneven_8192, "
                          "split_precision, fft2d, conv2d, conv_pairs, bluestein, served_conv)")
     ap.add_argument("--logn", type=str, default=None, help="comma-separated subset of the sweep")
-    ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "stream", "three_pass"],
+    ap.add_argument("--mode", default="auto", choices=["auto", "single", "four_step", "three_pass"],
                     help="plan mode for every N (auto: autotuned / tuning cache / planner default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner pass that picks each N's plan before the timed region")
@@ -70,9 +70,9 @@ def compact_choice(c):
         return f"single {c['single_loge']}.{c['single_logc']}{r32('single_logr')}{pipe}"
     if c["mode"] == 4:
         return f"three-pass R 2^{c['logn2']} Q 2^{c.get('logn3', -1)} chunk {c['chunk']} pipe {c['pipe']}"
-    kind = "stream" if c["mode"] == 3 else "four-step"
+    kind = "four-step"
     return (f"{kind} col {c['logn2']}.{c['col_loge']}.{c['col_logc']}{r32('col_logr')} "
-            f"row {c['row_loge']}.{c['row_logc']}{r32('row_logr')} chunk {c['chunk']} lag {c['lag']} pipe {c['pipe']}")
+            f"row {c['row_loge']}.{c['row_logc']}{r32('row_logr')} chunk {c['chunk']} pipe {c['pipe']}")
 
 
 def dist_env():
@@ -436,7 +436,7 @@ def bench_uneven(estl, torch):
         torch.cuda.synchronize()
         check(L.estl_packed_check(plan))
         ms = e0.elapsed_time(e1) / 10
-        buf = ctypes.create_string_buffer(1024)
+        buf = ctypes.create_string_buffer(8192)
         check(L.estl_packed_plan_describe(plan, buf, len(buf)))
         d = json.loads(buf.value.decode())
         res[name] = {"ms": round(ms, 4), "gbs": round(16 * total / (ms * 1e-3) / 1e9, 1),

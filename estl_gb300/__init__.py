@@ -69,18 +69,18 @@ def _stream_handle(stream):
 class Plan:
     """`batch` transforms of length n, forward (-1) or backward (+1)."""
 
-    MODES = {"auto": 0, "single": 1, "four_step": 2, "stream": 3, "three_pass": 4}
+    MODES = {"auto": 0, "single": 1, "four_step": 2, "three_pass": 4}
 
     TILE_FIELDS = ("split_log2", "single_loge", "single_logc", "col_loge", "col_logc", "row_loge", "row_logc",
                    "pipelined", "split2_log2", "single_logr", "col_logr", "row_logr", "single_cluster_log2")
 
-    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", lag=0, chunk=0, tiles=None):
+    def __init__(self, n, batch=1, direction=FORWARD, precision=PREC_FP32, mode="auto", chunk=0, tiles=None):
         """tiles: optional dict of estl_plan_options tile fields (split_log2, col_loge, ...; modes
         single / four_step / three_pass), missing ones left to the planner."""
         _ensure_init()
         self.n, self.batch, self.direction = int(n), int(batch), int(direction)
         h = ctypes.c_void_p()
-        opts = PlanOptions(self.MODES[mode] if isinstance(mode, str) else int(mode), int(lag), int(chunk))
+        opts = PlanOptions(self.MODES[mode] if isinstance(mode, str) else int(mode), 0, int(chunk))
         if tiles:
             unknown = set(tiles) - set(self.TILE_FIELDS)
             if unknown:
@@ -102,7 +102,7 @@ class Plan:
         return json.loads(buf.value.decode())
 
     def check(self):
-        """Synchronise; raise if a streamed kernel's dependency wait gave up."""
+        """Synchronise; raise if a persistent kernel's bounded copy wait gave up."""
         check(lib().estl_plan_check(self._h))
 
     @property
@@ -151,7 +151,7 @@ class Plan:
         check(lib().estl_execute_host(self._h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(out.ctypes.data)))
         return out
 
-    KERNEL_KINDS = ("single", "col", "row", "copy", "stream", "column")
+    KERNEL_KINDS = ("single", "col", "row", "copy", "unused", "column")
 
     def set_profiling(self, enable=True):
         """Bracket every launch with CUDA events (per-kernel timers)."""
@@ -296,7 +296,7 @@ class PackedPlan:
         check(lib().estl_packed_check(self._h))
 
     def describe(self):
-        buf = ctypes.create_string_buffer(1024)
+        buf = ctypes.create_string_buffer(8192)
         check(lib().estl_packed_plan_describe(self._h, buf, len(buf)))
         return json.loads(buf.value.decode())
 

@@ -130,7 +130,7 @@ REQ_CONV = 1
 
 
 class PlanOptions(ctypes.Structure):
-    """estl_plan_options: mode 0 auto, 1 single tile, 2 four-step, 3 streamed four-step,
+    """estl_plan_options: mode 0 auto, 1 single tile (or cluster tile), 2 four-step,
     4 three-pass; explicit_tiles != 0 fixes the tile kernels (-1 fields: planner's choice)."""
     _fields_ = [("mode", ctypes.c_int), ("lag", ctypes.c_int), ("chunk", ctypes.c_int64),
                 ("explicit_tiles", ctypes.c_int), ("split_log2", ctypes.c_int),

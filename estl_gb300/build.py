@@ -29,7 +29,6 @@ SOURCES = [
     "packed_plan.cpp",
     "packed.cu",
     "serve.cu",
-    "stream.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -244,7 +244,7 @@ static estl_status encode_column_map(CUtensorMap* map, const cf32* base, const S
 
 estl_status prepare_steps(const Plan1D& plan) {
   for (const Step& st : plan.steps) {
-    if (st.kind == STEP_STREAM || st.kind == STEP_COPY) continue;
+    if (st.kind == STEP_COPY) continue;
     const KernelDesc* d = nullptr;
     estl_status s = lookup_kernel(st, st.pipe, &d);
     if (s != ESTL_OK) return s;
@@ -268,15 +268,9 @@ estl_status take_bulk_wait_error() {
 }
 
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream, const StreamAux* aux, const long long* xoff, long long extent) {
+                         cudaStream_t stream, const long long* xoff, long long extent) {
   Engine& E = engine();
   for (const Step& st : plan.steps) {
-    if (st.kind == STEP_STREAM) {
-      if (!aux) return fail(ESTL_DEVICE_ERROR, "streamed step without a work list");
-      estl_status s = launch_stream(st, in, out, scratch, plan.scratch_elems, *aux, sgn, stream);
-      if (s != ESTL_OK) return s;
-      continue;
-    }
     const cf32* src = st.src == BUF_IN ? in : (st.src == BUF_SCRATCH ? scratch : out);
     cf32* dst = st.dst == BUF_OUT ? out : scratch;
     if (st.kind == STEP_COPY) {
@@ -347,9 +341,6 @@ struct estl_plan_s {
   int direction = ESTL_FORWARD;
   cf32* scratch = nullptr;
   size_t scratch_bytes = 0;
-  void* aux = nullptr;  // streamed plans: work list and counters
-  size_t aux_bytes = 0;
-  StreamAux saux{};
   std::mutex mu;
   std::mutex host_mu;  // one host pipeline run at a time (staging buffers, chunk plans)
   cudaEvent_t done = nullptr;  // last execute of this plan (scratch reuse order)
@@ -363,16 +354,10 @@ struct estl_plan_s {
   size_t stage_bytes = 0;
   cudaStream_t st[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_h2d[2] = {}, ev_comp[2] = {}, ev_d2h[2] = {};
-  void* host_aux[2] = {nullptr, nullptr};  // streamed plans: work lists of the chunk plans
-  size_t host_aux_bytes[2] = {0, 0};
-  StreamAux host_saux[2] = {};
   // the smaller chunks that open and close a host pipeline (estl_execute_host):
   // chunk transforms -> plan (and its streamed work list)
   struct RampChunk {
     Plan1D lay;
-    void* aux = nullptr;
-    size_t aux_bytes = 0;
-    StreamAux saux{};
   };
   std::unordered_map<long long, RampChunk> ramp;
   // other host layouts (estl_execute_layout / estl_execute_host_layout):
@@ -411,9 +396,6 @@ static std::unordered_set<estl_plan> g_plans;
 static void plan_release(estl_plan p) {
   if (!p) return;
   dev_free(p->scratch, p->scratch_bytes);
-  dev_free(p->aux, p->aux_bytes);
-  for (int s = 0; s < 2; ++s) dev_free(p->host_aux[s], p->host_aux_bytes[s]);
-  for (auto& kv : p->ramp) dev_free(kv.second.aux, kv.second.aux_bytes);
   dev_free(p->blue_chirp, p->blue_chirp_bytes);
   dev_free(p->blue_spec, p->blue_spec_bytes);
   dev_free(p->blue_a, p->blue_work_bytes);
@@ -559,7 +541,8 @@ estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precis
 
 estl_status estl_plan_create_ex(int64_t n, int64_t batch, int direction, int precision,
                                 const estl_plan_options* options, estl_plan* plan) {
-  if (options && (options->mode < 0 || options->mode > 4 || options->lag < 0 || options->chunk < 0))
+  if (options && (options->mode < 0 || options->mode > 4 || options->mode == 3 || options->lag != 0 ||
+                  options->chunk < 0))
     return fail(ESTL_INVALID_ARG, "bad plan options (mode %d, lag %d, chunk %lld)", options->mode, options->lag,
                 (long long)options->chunk);
   return plan_create_impl(n, batch, direction, precision, options, plan);
@@ -631,7 +614,7 @@ static estl_status bluestein_setup(estl_plan_s* p) {
   blue_chirp_kernel<<<flat_grid(N), 256, 0, st>>>(p->blue_chirp, N);
   blue_kernel_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_chirp, p->blue_a, N, M);
   s = check_cuda(cudaGetLastError(), "Bluestein set-up");
-  if (s == ESTL_OK) s = launch_steps(one, p->blue_a, p->blue_spec, p->scratch, 1.f, st, nullptr);
+  if (s == ESTL_OK) s = launch_steps(one, p->blue_a, p->blue_spec, p->scratch, 1.f, st);
   if (s != ESTL_OK) return s;
   blue_scale_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_spec, M, 1.f / (float)M);
   s = check_cuda(cudaGetLastError(), "Bluestein set-up");
@@ -651,11 +634,11 @@ static estl_status run_bluestein(estl_plan p, long long count, const cf32* in, c
     if (!make_plan(M, c, PlanChoice{}, &inner, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
     blue_pre_kernel<<<flat_grid(c * M), 256, 0, st>>>(in + b0 * N, p->blue_a, p->blue_chirp, N, logm, c, p->sgn);
     estl_status s = check_cuda(cudaGetLastError(), "Bluestein pre-multiply");
-    if (s == ESTL_OK) s = launch_steps(inner, p->blue_a, p->blue_c, p->scratch, 1.f, st, nullptr);
+    if (s == ESTL_OK) s = launch_steps(inner, p->blue_a, p->blue_c, p->scratch, 1.f, st);
     if (s != ESTL_OK) return s;
     blue_mul_kernel<<<flat_grid(c * M), 256, 0, st>>>(p->blue_c, p->blue_spec, logm, c);
     s = check_cuda(cudaGetLastError(), "Bluestein spectrum multiply");
-    if (s == ESTL_OK) s = launch_steps(inner, p->blue_c, p->blue_a, p->scratch, -1.f, st, nullptr);
+    if (s == ESTL_OK) s = launch_steps(inner, p->blue_c, p->blue_a, p->scratch, -1.f, st);
     if (s != ESTL_OK) return s;
     blue_post_kernel<<<flat_grid(c * N), 256, 0, st>>>(p->blue_a, out + b0 * N, p->blue_chirp, N, logm, c, p->sgn);
     s = check_cuda(cudaGetLastError(), "Bluestein post-multiply");
@@ -692,7 +675,6 @@ static estl_status plan_create_impl(int64_t n, int64_t batch, int direction, int
   PlanChoice choice;
   if (opt && opt->mode != 0) {
     choice.mode = opt->mode;
-    choice.lag = opt->lag;
     choice.chunk = opt->chunk;
     if (opt->explicit_tiles) {
       choice.logn2 = opt->split_log2;
@@ -736,15 +718,6 @@ static estl_status plan_finish(std::unique_ptr<estl_plan_s> p, int direction, es
   if (s != ESTL_OK) return s;
   if (p->layout.blue_m > 0) {
     s = bluestein_setup(p.get());
-    if (s != ESTL_OK) {
-      plan_release(p.release());
-      return s;
-    }
-  }
-  p->aux_bytes = stream_aux_bytes(p->layout);
-  if (p->aux_bytes) {
-    s = dev_alloc(&p->aux, p->aux_bytes, "stream work list");
-    if (s == ESTL_OK) s = stream_prepare(p->layout, p->aux, p->aux_bytes, &p->saux);
     if (s != ESTL_OK) {
       plan_release(p.release());
       return s;
@@ -809,18 +782,6 @@ estl_status estl_plan_check(estl_plan plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan");
   estl_status s = check_cuda(cudaDeviceSynchronize(), "plan execute");
   if (s != ESTL_OK) return s;
-  std::vector<const StreamAux*> auxes = {&plan->saux, &plan->host_saux[0], &plan->host_saux[1]};
-  for (const auto& kv : plan->ramp) auxes.push_back(&kv.second.saux);
-  for (const StreamAux* a : auxes) {
-    if (!a->error) continue;
-    int e = 0;
-    s = check_cuda(cudaMemcpy(&e, a->error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
-    if (s != ESTL_OK) return s;
-    if (e) {
-      cudaMemset(a->error, 0, sizeof(int));
-      return fail(ESTL_TIMEOUT, "a dependency wait of the streamed kernel gave up");
-    }
-  }
   long long e = 0;
   s = check_cuda(cudaMemcpy(&e, engine().dev_err, sizeof(e), cudaMemcpyDeviceToHost), "cudaMemcpy(error word)");
   if (s != ESTL_OK) return s;
@@ -931,7 +892,7 @@ static estl_status resolve_profile(estl_plan p) {
   return ESTL_OK;
 }
 
-static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
+static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const cf32* in, cf32* out,
                                    cudaStream_t stream) {
   if (p->pending.size() > 65536) {
     estl_status s = resolve_profile(p);
@@ -944,7 +905,7 @@ static estl_status launch_profiled(estl_plan p, const Plan1D& layout, const Stre
     estl_status s = pool_event(p, &r.a);
     if (s == ESTL_OK) s = pool_event(p, &r.b);
     if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.a, stream), "cudaEventRecord");
-    if (s == ESTL_OK) s = launch_steps(one, in, out, p->scratch, p->sgn, stream, aux);
+    if (s == ESTL_OK) s = launch_steps(one, in, out, p->scratch, p->sgn, stream);
     if (s == ESTL_OK) s = check_cuda(cudaEventRecord(r.b, stream), "cudaEventRecord");
     if (s != ESTL_OK) return s;
     p->pending.push_back(r);
@@ -961,16 +922,15 @@ struct LayoutIO {
   long long total;  // complex elements
 };
 
-static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const StreamAux* aux, const cf32* in, cf32* out,
+static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const cf32* in, cf32* out,
                                cudaStream_t stream, const LayoutIO* io = nullptr) {
   std::lock_guard<std::mutex> g(plan->mu);
   if (plan->unusable) return fail(ESTL_DEVICE_ERROR, "the plan is unusable (estl_plan_check reported copies in flight)");
   estl_status s;
-  // executes that touch device state of the plan (scratch, work lists,
-  // staging, Bluestein buffers, profiling events) are ordered behind the
-  // previous one; a plan without such state (one tile launch in to out) is not
-  const bool stateful = layout.scratch_elems > 0 || layout.blue_m > 0 || io || plan->profiling ||
-                        (aux && aux->nitems > 0);
+  // executes that touch device state of the plan (scratch, staging,
+  // Bluestein buffers, profiling events) are ordered behind the previous one;
+  // a plan without such state (one tile launch in to out) is not
+  const bool stateful = layout.scratch_elems > 0 || layout.blue_m > 0 || io || plan->profiling;
   if (stateful && plan->done_recorded) {
     s = check_cuda(cudaStreamWaitEvent(stream, plan->done, 0), "cudaStreamWaitEvent");
     if (s != ESTL_OK) return s;
@@ -982,9 +942,9 @@ static estl_status run_plan_on(estl_plan plan, const Plan1D& layout, const Strea
   if (layout.blue_m > 0)
     s = run_bluestein(plan, layout.batch, in, out, stream);
   else if (plan->profiling)
-    s = launch_profiled(plan, layout, aux, in, out, stream);
+    s = launch_profiled(plan, layout, in, out, stream);
   else
-    s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream, aux);
+    s = launch_steps(layout, in, out, plan->scratch, plan->sgn, stream);
   if (s != ESTL_OK) return s;
   if (io) {
     s = launch_layout_out(io->layout, out, io->dst, io->total, stream);
@@ -1003,7 +963,7 @@ estl_status estl_execute(estl_plan plan, const void* d_in, void* d_out, void* st
   if (s != ESTL_OK) return s;
   s = check_buffers(d_in, d_out);
   if (s != ESTL_OK) return s;
-  return run_plan_on(plan, plan->layout, &plan->saux, (const cf32*)d_in, (cf32*)d_out, (cudaStream_t)stream);
+  return run_plan_on(plan, plan->layout, (const cf32*)d_in, (cf32*)d_out, (cudaStream_t)stream);
 }
 
 static estl_status host_pipeline_setup(estl_plan p) {
@@ -1020,15 +980,6 @@ static estl_status host_pipeline_setup(estl_plan p) {
     return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
   if ((size_t)p->host_plan_full.scratch_elems * sizeof(cf32) > p->scratch_bytes)
     return fail(ESTL_DEVICE_ERROR, "chunk plan needs more scratch than the plan holds");
-  const Plan1D* chunk_plans[2] = {&p->host_plan_full, tail ? &p->host_plan_tail : nullptr};
-  for (int k = 0; k < 2; ++k) {
-    if (!chunk_plans[k]) continue;
-    p->host_aux_bytes[k] = stream_aux_bytes(*chunk_plans[k]);
-    if (!p->host_aux_bytes[k]) continue;
-    estl_status s2 = dev_alloc(&p->host_aux[k], p->host_aux_bytes[k], "stream work list");
-    if (s2 == ESTL_OK) s2 = stream_prepare(*chunk_plans[k], p->host_aux[k], p->host_aux_bytes[k], &p->host_saux[k]);
-    if (s2 != ESTL_OK) return s2;
-  }
   p->stage_bytes = (size_t)(chunk * n) * sizeof(cf32);
   estl_status s;
   for (int i = 0; i < 2; ++i) {
@@ -1051,25 +1002,15 @@ static estl_status host_pipeline_setup(estl_plan p) {
 }
 
 // The plan of a ramp chunk of `cnt` transforms (made on first use).
-static estl_status ramp_chunk(estl_plan p, long long cnt, const Plan1D** lay, const StreamAux** aux) {
+static estl_status ramp_chunk(estl_plan p, long long cnt, const Plan1D** lay) {
   auto it = p->ramp.find(cnt);
   if (it == p->ramp.end()) {
     estl_plan_s::RampChunk rc;
     std::string err;
     if (!make_plan_like(p->layout, cnt, &rc.lay, &err)) return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
-    rc.aux_bytes = stream_aux_bytes(rc.lay);
-    if (rc.aux_bytes) {
-      estl_status s = dev_alloc(&rc.aux, rc.aux_bytes, "stream work list");
-      if (s == ESTL_OK) s = stream_prepare(rc.lay, rc.aux, rc.aux_bytes, &rc.saux);
-      if (s != ESTL_OK) {
-        dev_free(rc.aux, rc.aux_bytes);
-        return s;
-      }
-    }
     it = p->ramp.emplace(cnt, rc).first;
   }
   *lay = &it->second.lay;
-  *aux = &it->second.saux;
   return ESTL_OK;
 }
 
@@ -1114,12 +1055,10 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
     const long long cnt = sched[(size_t)i];
     const size_t bytes = (size_t)(cnt * n) * sizeof(cf32);
     const Plan1D* layp = &plan->host_plan_full;
-    const StreamAux* aux = &plan->host_saux[0];
     if (cnt != chunk) {
       if (cnt == batch % chunk) {
         layp = &plan->host_plan_tail;
-        aux = &plan->host_saux[1];
-      } else if ((s = ramp_chunk(plan, cnt, &layp, &aux)) != ESTL_OK) {
+      } else if ((s = ramp_chunk(plan, cnt, &layp)) != ESTL_OK) {
         return s;
       }
     }
@@ -1131,7 +1070,7 @@ estl_status estl_execute_host(estl_plan plan, const float* h_in, float* h_out) {
     if ((s = check_cuda(cudaEventRecord(plan->ev_h2d[k], sh), "record")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_h2d[k], 0), "wait")) != ESTL_OK) return s;
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_d2h[k], 0), "wait")) != ESTL_OK) return s;
-    if ((s = run_plan_on(plan, lay, aux, plan->din[k], plan->dout[k], sc)) != ESTL_OK) return s;
+    if ((s = run_plan_on(plan, lay, plan->din[k], plan->dout[k], sc)) != ESTL_OK) return s;
     if ((s = check_cuda(cudaEventRecord(plan->ev_comp[k], sc), "record")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaStreamWaitEvent(sd, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaMemcpyAsync(h_out + 2 * b0 * n, plan->dout[k], bytes, cudaMemcpyDeviceToHost, sd),
@@ -1167,7 +1106,7 @@ estl_status estl_execute_layout(estl_plan plan, int layout, const float* d_in, f
     }
   }
   LayoutIO io{layout, d_in, d_out, total};
-  return run_plan_on(plan, plan->layout, &plan->saux, plan->lay_in, plan->lay_out, (cudaStream_t)stream, &io);
+  return run_plan_on(plan, plan->layout, plan->lay_in, plan->lay_out, (cudaStream_t)stream, &io);
 }
 
 estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_in, float* h_out) {
@@ -1199,7 +1138,6 @@ estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_
     const int k = (int)(i & 1);
     const long long b0 = i * chunk, cnt = std::min(chunk, batch - b0), e0 = b0 * n, ce = cnt * n;
     const Plan1D& lay = cnt == chunk ? plan->host_plan_full : plan->host_plan_tail;
-    const StreamAux* aux = cnt == chunk ? &plan->host_saux[0] : &plan->host_saux[1];
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sh, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if (layout == ESTL_LAYOUT_BLOCK_PLANAR) {
       s = check_cuda(cudaMemcpyAsync(plan->hlay_in[k], h_in + 2 * e0, (size_t)layout_floats(layout, ce) * 4,
@@ -1218,7 +1156,7 @@ estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_
     if ((s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_h2d[k], 0), "wait")) != ESTL_OK) return s;
     if (i >= 2 && (s = check_cuda(cudaStreamWaitEvent(sc, plan->ev_d2h[k], 0), "wait")) != ESTL_OK) return s;
     LayoutIO io{layout, plan->hlay_in[k], plan->hlay_out[k], ce};
-    if ((s = run_plan_on(plan, lay, aux, plan->din[k], plan->dout[k], sc, &io)) != ESTL_OK) return s;
+    if ((s = run_plan_on(plan, lay, plan->din[k], plan->dout[k], sc, &io)) != ESTL_OK) return s;
     if ((s = check_cuda(cudaEventRecord(plan->ev_comp[k], sc), "record")) != ESTL_OK) return s;
     if ((s = check_cuda(cudaStreamWaitEvent(sd, plan->ev_comp[k], 0), "wait")) != ESTL_OK) return s;
     if (layout == ESTL_LAYOUT_BLOCK_PLANAR) {

@@ -51,21 +51,6 @@ estl_status launch_pdl(const void* fn, long long grid, int threads, void** args,
 estl_status dev_alloc(void** p, size_t bytes, const char* what);
 void dev_free(void* p, size_t bytes);
 
-// Device work list and counters of a streamed four-step plan.
-struct StreamAux {
-  PackedItem* items;
-  long long nitems;
-  unsigned int* counters;  // [0] work counter, then column and row counts per transform
-  size_t counter_bytes;
-  int* error;              // set when a dependency wait gave up
-};
-
-size_t stream_aux_bytes(const Plan1D& plan);
-// Builds the work list of a streamed plan into `aux` (device memory).
-estl_status stream_prepare(const Plan1D& plan, void* aux, size_t aux_bytes, StreamAux* out);
-estl_status launch_stream(const Step& st, const cf32* in, cf32* out, cf32* scratch, long long scratch_elems,
-                          const StreamAux& aux, float sgn, cudaStream_t stream);
-
 // Kernel attributes of every step of a plan set now (before a stream capture).
 estl_status prepare_steps(const Plan1D& plan);
 // Reads and clears the bulk-load kernels' wait-timeout word (after a device
@@ -74,13 +59,12 @@ estl_status prepare_steps(const Plan1D& plan);
 estl_status take_bulk_wait_error();
 
 // Launches one plan's steps on `stream`.  in/out/scratch are device
-// pointers of interleaved complex64; sgn = +1 forward, -1 backward.  aux is
-// the work list of a streamed plan (else unused).  xoff (device, one element
-// offset per transform of the plan) places transform f at in/out + xoff[f]
-// instead of f * n, in buffers of `extent` elements (bucketed uneven
-// batches; single, column, row and resident tiles; no tensor-copy tiles).
+// pointers of interleaved complex64; sgn = +1 forward, -1 backward.  xoff
+// (device, one element offset per transform of the plan) places transform f
+// at in/out + xoff[f] instead of f * n, in buffers of `extent` elements
+// (bucketed uneven batches; single, column, row and resident tiles; no
+// tensor-copy tiles).
 estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* scratch, float sgn,
-                         cudaStream_t stream, const StreamAux* aux = nullptr, const long long* xoff = nullptr,
-                         long long extent = 0);
+                         cudaStream_t stream, const long long* xoff = nullptr, long long extent = 0);
 
 }  // namespace estl

@@ -71,8 +71,7 @@ static estl_status bucketed_enqueue(estl_packed_plan p, const cf32* in, cf32* ou
   for (size_t k = 0; k < p->buckets.size() && s == ESTL_OK; ++k) {
     s = check_cuda(cudaStreamWaitEvent(p->b_streams[k], p->b_events[0], 0), "cudaStreamWaitEvent(fork)");
     if (s == ESTL_OK)
-      s = launch_steps(p->buckets[k].plan, in, out, p->b_scratch[k], sgn, p->b_streams[k], nullptr, p->b_xoff[k],
-                       p->b_total);
+      s = launch_steps(p->buckets[k].plan, in, out, p->b_scratch[k], sgn, p->b_streams[k], p->b_xoff[k], p->b_total);
     if (s == ESTL_OK) s = check_cuda(cudaEventRecord(p->b_events[1 + k], p->b_streams[k]), "cudaEventRecord(join)");
     if (s == ESTL_OK) s = check_cuda(cudaStreamWaitEvent(st, p->b_events[1 + k], 0), "cudaStreamWaitEvent(join)");
   }
@@ -329,7 +328,11 @@ estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len)
       elems += c << b.logn;
       flops += 5.0 * (double)(c << b.logn) * b.logn;
       launches += (long long)b.plan.steps.size();
-      d += (k ? ", " : "") + b.plan.describe();
+      char e[160];
+      const Step& s0 = b.plan.steps.front();
+      std::snprintf(e, sizeof e, "%s{\"logn\": %d, \"count\": %lld, \"passes\": %d, \"launches\": %zu, \"cluster\": %d, \"pipe\": %d}",
+                    k ? ", " : "", b.logn, c, b.plan.hbm_passes, b.plan.steps.size(), s0.cluster, s0.pipe);
+      d += e;
     }
     size_t ntf = 0;
     for (const PackedBucket& b : p->buckets) ntf += b.xoff.size();

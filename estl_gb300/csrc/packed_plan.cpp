@@ -159,12 +159,12 @@ bool build_packed_buckets(const long long* offsets, const long long* sizes, long
     }
     bool dense_only = false;  // steps that read a transform's columns through a 2D view
     for (Step& st : b.plan.steps) {
-      if (st.kind == STEP_STREAM || st.ologr || st.src == BUF_OUT) dense_only = true;
+      if (st.ologr || st.src == BUF_OUT) dense_only = true;
       if (st.kind == STEP_COL && st.pipe == 2) st.pipe = 0;  // plain column tile: loads through the offsets
       if (odd && st.pipe >= 2) st.pipe = 0;                   // bulk copies need 16-byte aligned rows
     }
     if (dense_only) {
-      // plans of streamed or three passes: the default four-step instead
+      // plans of three passes: the default four-step instead
       PlanChoice four;
       four.mode = 2;
       if (!make_plan(n, c, four, &b.plan, &e)) {

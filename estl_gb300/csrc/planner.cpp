@@ -86,16 +86,6 @@ const std::vector<TileCfg>& tile_configs() {
   return v;
 }
 
-const StreamCfg* find_stream_cfg(int logn) {
-  static const StreamCfg table[] = {
-#define ESTL_XS(LOGN, CM, CE, CC, RM, RE, RC) {LOGN, CM, CE, CC, RM, RE, RC},
-#include "stream_list.inc"
-  };
-  for (const StreamCfg& c : table)
-    if (c.logn == logn) return &c;
-  return nullptr;
-}
-
 const TileCfg* find_tile(int kind, int logm, int loge, int logr, int logc, int pipe, int tc, int cluster,
                          int csplit) {
   for (const TileCfg& c : tile_configs())
@@ -189,7 +179,11 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     set_err(err, "unknown split precision %lld", choice.split);
     return false;
   }
-  if (tc && (choice.mode == 3 || choice.pipe > 0)) {
+  if (choice.mode == 3 || choice.mode < 0 || choice.mode > 4) {
+    set_err(err, "unknown plan mode %lld", choice.mode);
+    return false;
+  }
+  if (tc && choice.pipe > 0) {
     set_err(err, "split precision runs the plain single / four-step tiles (mode %lld)", choice.mode);
     return false;
   }
@@ -205,32 +199,6 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
   const bool cluster_default = mode == 0 && !tc && choice.single_cluster < 0 && choice.single_loge < 0 &&
                                default_cluster(logn) != nullptr;
   if (mode == 0) mode = (logn <= (tc ? kTcSingleMaxLog : kSingleMaxLog) || cluster_default) ? 1 : 2;
-
-  if (mode == 3) {
-    const StreamCfg* sc = find_stream_cfg(logn);
-    if (!sc) {
-      set_err(err, "no streamed four-step configuration for log2 n = %lld", logn);
-      return false;
-    }
-    const int logn1 = logn - sc->cm, logn2 = sc->cm;
-    const long long ncol = 1LL << (logn1 - sc->cc), nrow = 1LL << (logn2 - sc->rc);
-    // lag: enough tiles between a transform's last column tile and its first
-    // row tile for ~1000 CTAs (every resident CTA of a GB300) to drain
-    int lag = choice.lag > 0 ? choice.lag : (int)std::max(1LL, (1024 + ncol + nrow - 1) / (ncol + nrow));
-    lag = (int)std::min<long long>(lag, batch);
-    Step s{STEP_STREAM, sc->cm, sc->ce, 4, sc->cc, 1, BUF_IN, BUF_OUT, 0, total, 0, total, batch, logn};
-    s.rlogm = sc->rm;
-    s.rloge = sc->re;
-    s.rlogc = sc->rc;
-    s.lag = lag;
-    s.ring = (int)std::min<long long>(batch, lag + 2);
-    p.steps.push_back(s);
-    p.scratch_elems = (long long)s.ring * n;
-    p.aux_items = batch * (ncol + nrow);
-    p.hbm_passes = 2;
-    *out = p;
-    return true;
-  }
 
   if (mode == 4) {
     // three passes, N = R * Q * P (x[n1 + P n2 + PQ n3]):
@@ -544,14 +512,6 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
     ch.logn2 = c.csplit;
     out.push_back(ch);
   }
-  if (find_stream_cfg(logn)) {
-    for (int lag : {0, 1, 2, 4, 8}) {
-      PlanChoice ch;
-      ch.mode = 3;
-      ch.lag = lag;
-      out.push_back(ch);
-    }
-  }
   for (int lr = 7; lr <= 9; ++lr)
     for (int lq = 7; lq <= 9; ++lq) {
       const int lp = logn - lr - lq;
@@ -607,7 +567,7 @@ std::string Plan1D::describe() const {
                 n, batch, blue_m, xdim, ydim, splits[(choice.split >= 0 && choice.split <= 3) ? choice.split : 0], hbm_passes,
                 steps.size(), scratch_elems * 8);
   s += buf;
-  const char* names[] = {"single", "col", "row", "copy", "stream", "column"};
+  const char* names[] = {"single", "col", "row", "copy", "unused", "column"};
   // the first two steps (one chunk), and for 2D plans the column step
   std::vector<size_t> idx;
   for (size_t i = 0; i < steps.size() && i < (size_t)(hbm_passes == 3 ? 3 : 2); ++i)

@@ -18,7 +18,8 @@ namespace estl {
 
 // STEP_COLUMN: the column pass of a 2D transform (strided column DFTs, no
 // four-step twiddle), in place on the output.
-enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_STREAM = 4, STEP_COLUMN = 5 };
+// (kind 4 is unused: it named the streamed four-step, which was removed)
+enum StepKind { STEP_SINGLE = 0, STEP_COL = 1, STEP_ROW = 2, STEP_COPY = 3, STEP_COLUMN = 5 };
 constexpr int kStepKinds = 6;
 enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_SCRATCH = 2 };
 
@@ -45,12 +46,8 @@ struct Step {
   int src, dst;
   long long src_off, src_len;  // complex elements
   long long dst_off, dst_len;
-  long long rows;  // STEP_SINGLE / STEP_STREAM: transforms; STEP_COPY: elements
+  long long rows;  // STEP_SINGLE / STEP_COL / STEP_ROW: transforms; STEP_COPY: elements
   int logn;
-  // STEP_STREAM: row tile (the column tile is logm/loge/logc above), queue lag
-  // and scratch ring (transforms)
-  int rlogm = 0, rloge = 0, rlogc = 0;
-  int lag = 0, ring = 0;
   // persistent variant (pipe >= 2; grid = tiles, the launcher runs min(tiles, resident CTAs))
   int pipe = 0;
   // tensor-core variant (radix-16 passes as split-precision GEMMs)
@@ -66,23 +63,16 @@ struct Step {
   int cluster = 0, csplit = 0;
 };
 
-// Streamed four-step configuration of a length (stream_list.inc), or nullptr.
-struct StreamCfg {
-  int logn, cm, ce, cc, rm, re, rc;
-};
-const StreamCfg* find_stream_cfg(int logn);
-
 // Tunable plan parameters (what the autotuner searches).  Zero / -1 fields
 // mean "planner default".
 struct PlanChoice {
-  int mode = 0;  // 0 default, 1 single kernel, 2 four-step, 3 streamed four-step, 4 three-pass
+  int mode = 0;  // 0 default, 1 single kernel, 2 four-step, 4 three-pass (3 is unused)
   int single_loge = -1, single_logc = -1;
   int logn2 = -1;  // four-step: log2 N2 (column DFT length); three-pass: log2 R (first column DFTs)
   int logn3 = -1;  // three-pass: log2 Q (second column DFTs); <= 0 = default
   int col_loge = -1, col_logc = -1;
   int row_loge = -1, row_logc = -1;
   long long chunk = 0;  // four-step: transforms per chunk (bounds the scratch)
-  int lag = 0;          // streamed four-step: row tiles lag the column tiles by this many transforms
   int pipe = 0;         // tile kernels: 0 plain, 2 bulk-load, 3 / 4 resident (where the variant exists)
   int split = 0;        // 0 FP32; else the SplitKind of tensor-core radix-16 passes (tc_core.cuh)
   // log2 of the largest radix of the single / column / row tiles (-1 = 4:
@@ -103,7 +93,6 @@ struct Plan1D {
   PlanChoice choice;
   std::vector<Step> steps;
   long long scratch_elems = 0;
-  long long aux_items = 0;  // STEP_STREAM: work items (the plan uploads them)
   int hbm_passes = 0;
   std::string describe() const;  // one-line JSON
 };
@@ -111,7 +100,6 @@ struct Plan1D {
 constexpr int kSingleMaxLog = 14;
 constexpr int kClusterMaxLog = 17;  // single-pass plans on cluster tiles: up to 2^17 points
 constexpr int kTcSingleMaxLog = 13;  // split precision: larger n run four-step
-constexpr int kStreamMinLog = 13;
 constexpr int kMaxLogN = 24;
 constexpr int kThreePassDefaultLog = 23;  // default plans of N >= 2^23 (FP32) run three passes
 // At most 2^40 complex elements per plan (8 TiB, beyond any device memory;

@@ -73,10 +73,10 @@ std::string choice_to_json(const PlanChoice& c) {
   char buf[448];
   std::snprintf(buf, sizeof buf,
                 "{\"mode\": %d, \"single_loge\": %d, \"single_logc\": %d, \"logn2\": %d, \"col_loge\": %d, "
-                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"lag\": %d, \"pipe\": %d, "
+                "\"col_logc\": %d, \"row_loge\": %d, \"row_logc\": %d, \"chunk\": %lld, \"pipe\": %d, "
                 "\"logn3\": %d, \"single_logr\": %d, \"col_logr\": %d, \"row_logr\": %d, \"single_cluster\": %d}",
                 c.mode, c.single_loge, c.single_logc, c.logn2, c.col_loge, c.col_logc, c.row_loge, c.row_logc, c.chunk,
-                c.lag, c.pipe, c.logn3, c.single_logr, c.col_logr, c.row_logr, c.single_cluster);
+                c.pipe, c.logn3, c.single_logr, c.col_logr, c.row_logr, c.single_cluster);
   return buf;
 }
 
@@ -101,7 +101,6 @@ void tuner_load_cache() {
     e.choice.row_loge = (int)json_int(line, "row_loge", -1);
     e.choice.row_logc = (int)json_int(line, "row_logc", -1);
     e.choice.chunk = json_int(line, "chunk", 0);
-    e.choice.lag = (int)json_int(line, "lag", 0);
     e.choice.pipe = (int)json_int(line, "pipe", 0);
     e.choice.logn3 = (int)json_int(line, "logn3", -1);
     e.choice.single_logr = (int)json_int(line, "single_logr", -1);
@@ -177,24 +176,11 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
   const Plan1D* best = nullptr;
   std::vector<std::pair<double, const Plan1D*>> timed;
   for (const Plan1D& p : plans) {
-    void* aux = nullptr;
-    const size_t aux_bytes = stream_aux_bytes(p);
-    StreamAux saux{};
-    if (aux_bytes) {
-      if (dev_alloc(&aux, aux_bytes, "autotune work list") != ESTL_OK) continue;
-      if (stream_prepare(p, aux, aux_bytes, &saux) != ESTL_OK) {
-        dev_free(aux, aux_bytes);
-        continue;
-      }
-    }
-    s = launch_steps(p, in, out, scr, 1.f, st, &saux);
-    if (s != ESTL_OK) {
-      dev_free(aux, aux_bytes);
-      continue;
-    }
-    launch_steps(p, in, out, scr, 1.f, st, &saux);
+    s = launch_steps(p, in, out, scr, 1.f, st);
+    if (s != ESTL_OK) continue;
+    launch_steps(p, in, out, scr, 1.f, st);
     cudaEventRecord(e0, st);
-    for (int i = 0; i < iters; ++i) launch_steps(p, in, out, scr, 1.f, st, &saux);
+    for (int i = 0; i < iters; ++i) launch_steps(p, in, out, scr, 1.f, st);
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) {
       s = check_cuda(cudaGetLastError(), "autotune run");
@@ -203,10 +189,7 @@ extern "C" estl_status estl_autotune(int64_t n, int64_t batch, int iters, char* 
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= iters;
-    int stream_error = 0;
-    if (saux.error) cudaMemcpy(&stream_error, saux.error, sizeof(int), cudaMemcpyDeviceToHost);
-    dev_free(aux, aux_bytes);
-    if (stream_error) continue;  // a dependency wait gave up: not a usable configuration
+    if (take_bulk_wait_error() != ESTL_OK) continue;  // a bounded wait gave up: not a usable configuration
     timed.push_back({ms, &p});
     if (ms < best_ms) {
       best_ms = ms;

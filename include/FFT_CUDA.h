@@ -160,7 +160,7 @@ class FFT_CUDA : public FFT<D>, public GpuAlgorithm {
   }
 
   virtual std::string getKernelInfo(int kernel) {
-    static const char* names[] = {"tile", "column", "row", "copy", "streamed four-step", "2D column"};
+    static const char* names[] = {"tile", "column", "row", "copy", "unused", "2D column"};
     return (kernel >= 0 && kernel < (int)kinds.size()) ? names[kinds[kernel]] : "";
   }
 

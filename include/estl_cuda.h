@@ -89,15 +89,14 @@ int64_t estl_max_batch(int64_t n);
 estl_status estl_plan_create(int64_t n, int64_t batch, int direction, int precision, estl_plan* plan);
 
 /* Explicit plan shape (what estl_autotune searches).  mode: 0 automatic
- * (tuning cache, else defaults), 1 single-tile kernel (n <= 2^14),
- * 2 four-step as a column launch and a row launch per chunk of transforms
- * (two HBM round trips), 3 streamed four-step: one persistent launch whose
- * column and row tiles share a scratch ring small enough to stay in L2,
- * 4 three-pass (N = R * Q * P, 2^21 <= N <= 2^24, each of R, Q, P in
- * 2^7..2^9): two column launches and a row launch per chunk, three HBM round
- * trips of wide runs instead of two of narrow ones.
- * lag (mode 3): transforms between a column tile and the row tiles that read
- * it (0 = default).  chunk (mode 2): transforms per launch pair (0 = default).
+ * (tuning cache, else defaults), 1 single kernel (n <= 2^14 in one CTA per
+ * transform, or one transform per thread-block cluster up to 2^17, see
+ * single_cluster_log2), 2 four-step as a column launch and a row launch per
+ * chunk of transforms (two HBM round trips), 4 three-pass (N = R * Q * P,
+ * 2^21 <= N <= 2^24, each of R, Q, P in 2^7..2^9): two column launches and a
+ * row launch per chunk, three HBM round trips of wide runs instead of two of
+ * narrow ones.  Mode 3 is not used.  lag must be 0.
+ * chunk (mode 2): transforms per launch pair (0 = default).
  * explicit_tiles != 0 (modes 1 and 2) also fixes the tile kernels, each field
  * -1 for the planner's choice: split_log2 = log2 N2 of N = N1 * N2 (the column
  * DFT length), *_loge = log2 elements per thread, *_logc = log2 transforms
@@ -149,8 +148,8 @@ estl_status estl_plan_destroy(estl_plan plan);
 estl_status estl_plan_describe(estl_plan plan, char* buf, size_t len);
 
 /* Waits for the device; returns ESTL_TIMEOUT if a bounded device wait of a
- * persistent kernel (a streamed plan's dependency wait, a bulk-load tile's
- * copy wait) gave up since the last check (the outputs of that execute are
+ * persistent kernel (a bulk-load or resident tile's copy wait) gave up since
+ * the last check (the outputs of that execute are
  * then incomplete), else ESTL_OK.  If a bulk-load kernel also could not drain
  * the copies it had in flight, the plan is marked unusable: this returns
  * ESTL_DEVICE_ERROR and later executes of the plan are refused. */
@@ -209,7 +208,7 @@ estl_status estl_execute_host_layout(estl_plan plan, int layout, const float* h_
 estl_status estl_plan_set_profiling(estl_plan plan, int enable);
 
 /* Per kernel kind (index 0 single-tile, 1 column pass, 2 row pass, 3 device
- * copy, 4 streamed four-step, 5 2D column pass): launches, summed device milliseconds and
+ * copy, 4 unused, 5 2D column pass): launches, summed device milliseconds and
  * summed algorithmic bytes (16 bytes per complex element read and written).
  * Waits for the profiled launches to finish.  Arrays have ESTL_KERNEL_KINDS
  * entries; any may be NULL. */

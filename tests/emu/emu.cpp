@@ -30,7 +30,6 @@
 #include "estl_cuda.h"
 #include "resident_core.cuh"
 #include "cluster_core.cuh"
-#include "stream_core.cuh"
 #include "planner.h"
 
 using namespace estl;
@@ -399,31 +398,6 @@ const std::vector<EmuConvKernel>& emu_conv_kernels() {
   return v;
 }
 
-// ---- streamed four-step kernels ----
-using StreamFn = void (*)(const StreamArgs&, long long, int, cf32*, int*);
-struct EmuStreamKernel {
-  int logn, nt;
-  long long smem;
-  StreamFn fn;
-};
-
-template <class CK, class RK>
-EmuStreamKernel mks(int logn) {
-  return EmuStreamKernel{logn, CK::NT, CK::SMEM_ELEMS > RK::SMEM_ELEMS ? CK::SMEM_ELEMS : RK::SMEM_ELEMS,
-                         &stream_run<CK, RK>};
-}
-
-const std::vector<EmuStreamKernel>& emu_stream_kernels() {
-  static const std::vector<EmuStreamKernel> v = [] {
-    std::vector<EmuStreamKernel> k;
-#define ESTL_XS(LOGN, CM, CE, CC, RM, RE, RC) \
-  k.push_back(mks<ColKernel<CM, CE, 4, CC>, RemapRowKernel<RM, RE, 4, RC>>(LOGN));
-#include "stream_list.inc"
-    return k;
-  }();
-  return v;
-}
-
 void set_err(char* err, int len, const std::string& s) {
   if (err && len > 0) std::snprintf(err, (size_t)len, "%s", s.c_str());
 }
@@ -440,7 +414,6 @@ PlanChoice choice_from(const int* f) {
   c.row_loge = f[6];
   c.row_logc = f[7];
   c.chunk = f[8];
-  c.lag = f[9];
   c.pipe = f[10];
   c.split = f[11];
   c.logn3 = f[12];
@@ -589,48 +562,6 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
       std::memcpy(dst + st.dst_off, src + st.src_off, (size_t)st.rows * sizeof(cf32));
       continue;
     }
-    if (st.kind == STEP_STREAM) {
-      // the persistent kernel as one CTA: it takes the work list in queue order
-      const EmuStreamKernel* sk = nullptr;
-      for (const EmuStreamKernel& c : emu_stream_kernels())
-        if (c.logn == st.logn) sk = &c;
-      if (!sk) {
-        set_err(err, errlen, "no emulated streamed kernel");
-        return 3;
-      }
-      std::vector<PackedItem> items((size_t)p.aux_items);
-      stream_items(p.batch, st.logn, st.logm, st.logc, st.rlogc, st.lag, items.data());
-      std::vector<unsigned int> counters(1 + 2 * (size_t)p.batch, 0u);
-      int error = 0;
-      StreamArgs a;
-      a.items = Ptr<const PackedItem>{items.data(), (long long)items.size()};
-      a.nitems = (long long)items.size();
-      a.in = Ptr<const cf32>{src + st.src_off, st.src_len};
-      a.out = Ptr<cf32>{dst + st.dst_off, st.dst_len};
-      a.scratch = Ptr<cf32>{scratch.data(), p.scratch_elems};
-      a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
-      a.next = counters.data();
-      a.col_done = counters.data() + 1;
-      a.row_done = counters.data() + 1 + p.batch;
-      a.error = &error;
-      a.sgn = sign < 0 ? 1.f : -1.f;
-      a.logn = st.logn;
-      a.ring = st.ring;
-      a.ncol = (int)(1LL << (st.logn - st.logm - st.logc));
-      a.nrow = (int)(1LL << (st.logm - st.rlogc));
-      int slot[2] = {0, 0};
-      auto fn = [&slot, sk](const StreamArgs& args, long long cta, int tid, cf32* sm) { sk->fn(args, cta, tid, sm, slot); };
-      if (!run_generic(sk->nt, sk->smem, fn, a, 1)) {
-        std::lock_guard<std::mutex> g(g_msg_mu);
-        set_err(err, errlen, g_msg);
-        return 1;
-      }
-      if (error) {
-        set_err(err, errlen, "streamed kernel: a dependency wait gave up");
-        return 4;
-      }
-      continue;
-    }
     const EmuKernel* k = nullptr;
     for (const EmuKernel& c : emu_kernels())
       if (c.kind == st.kind && c.logm == st.logm && c.loge == st.loge && c.logr == st.logr && c.logc == st.logc &&
@@ -754,7 +685,7 @@ int emu_plan_candidates(long long n, long long batch, int* out, int max) {
     f[6] = ch.row_loge;
     f[7] = ch.row_logc;
     f[8] = (int)ch.chunk;
-    f[9] = ch.lag;
+    f[9] = 0;  // formerly the streamed four-step's lag
     f[10] = ch.pipe;
     f[11] = ch.split;
     f[12] = ch.logn3;

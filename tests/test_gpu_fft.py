@@ -46,27 +46,6 @@ def test_parity_every_size(engine, logn):
         assert e.max() < tol(n), (n, direction, e.max())
 
 
-@pytest.mark.parametrize("logn", range(13, 25))
-def test_streamed_four_step(engine, logn):
-    """The persistent streamed four-step (one launch, L2-sized scratch ring):
-    a batch longer than the ring so that ring slots are reused, both
-    directions, against the oracle, and the dependency-wait flag clear."""
-    import torch
-    n = 1 << logn
-    batch = max(4, min(24, (1 << 24) // n))
-    x = uniform_c64((batch, n), 300 + logn)
-    xd = torch.from_numpy(x).cuda()
-    for direction, lag in ((-1, 0), (+1, 1)):
-        p = engine.Plan(n, batch, direction, mode="stream", lag=lag)
-        assert p.describe()["kernels"][0]["kind"] == "stream"
-        y = p.execute(xd).cpu().numpy()
-        p.check()
-        rows = range(batch) if n <= (1 << 20) else (0, batch - 1)
-        for b in rows:
-            e = oracle.rel_l2(y[b][None], oracle.fft(x[b][None], direction))[0]
-            assert e < tol(n), (n, direction, b, e)
-
-
 def test_config1_plain_4096x256(engine):
     """N = 4096, batch = 256, uniform[-1,1) seed 1: every transform vs the oracle."""
     x = uniform_c64((256, 4096), 1)

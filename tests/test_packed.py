@@ -115,7 +115,7 @@ def gpu_packed(offsets, sizes, x_dev, mode, direction):
         check(L.estl_packed_execute(plan, ctypes.c_void_p(x_dev.data_ptr()), ctypes.c_void_p(y.data_ptr()),
                                     ctypes.c_void_p(st)))
     check(L.estl_packed_check(plan))
-    buf = ctypes.create_string_buffer(1024)
+    buf = ctypes.create_string_buffer(8192)
     check(L.estl_packed_plan_describe(plan, buf, len(buf)))
     desc = json.loads(buf.value.decode())
     L.estl_packed_plan_destroy(plan)

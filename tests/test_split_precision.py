@@ -68,10 +68,12 @@ def test_split_small_sizes_run_fp32_tiles(emu):
         assert oracle.rel_l2(y, oracle.fft(x, -1)).max() < 1e-6
 
 
-def test_split_rejects_streamed_and_pipelined(emu):
+def test_split_rejects_persistent_variants(emu):
+    """Split precision runs the plain single / four-step tiles: a request for
+    the bulk-load variants is refused."""
     n = 1 << 16
     x = rand_c64((1, n), 1)
-    rc, msg, _ = emu_run(emu, n, 1, x, -1, [3, -1, -1, -1, -1, -1, -1, -1, 0, 0, 0, 1])
+    rc, msg, _ = emu_run(emu, n, 1, x, -1, [2, -1, -1, -1, -1, -1, -1, -1, 0, 0, 2, 1])
     assert rc == 2 and "split precision" in msg
 
 
