@@ -363,7 +363,8 @@ def test_resident_single_tiles(engine, logn, loge, logr, rounds):
 
 
 CLUSTER_TILES = [(12, 1, 6, 4), (12, 2, 6, 4), (13, 1, 7, 4), (14, 1, 7, 4), (14, 2, 7, 4), (14, 1, 7, 5), (15, 2, 7, 4), (15, 2, 8, 4),
-                 (15, 3, 8, 4), (15, 2, 8, 5), (16, 3, 8, 4), (16, 3, 8, 5), (16, 4, 8, 4), (17, 4, 8, 4)]
+                 (15, 3, 8, 4), (15, 2, 8, 5), (16, 3, 7, 4), (16, 3, 8, 4), (16, 3, 8, 5), (16, 4, 8, 4), (17, 4, 8, 4),
+                 (17, 4, 9, 4)]
 
 
 @pytest.mark.parametrize("logn,lcl,logn2,loge", CLUSTER_TILES)
