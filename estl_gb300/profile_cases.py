@@ -18,6 +18,8 @@ CASES = {
     # whole transforms in one CTA (fft_core.cuh SingleKernel, radix 32)
     "single13": (13, dict(mode="single", tiles={"single_loge": 5, "single_logc": 0, "single_logr": 5})),
     "single14": (14, dict(mode="single", tiles={"single_loge": 5, "single_logc": 0, "single_logr": 5})),
+    # the plain 4096 x 256 configuration (one small batch, latency-bound)
+    "c1": (12, dict(batch=256)),
 }
 
 
@@ -27,13 +29,14 @@ def run(case, elements_log=24):
     import estl_gb300 as estl
     if case in CASES:
         logn, kw = CASES[case]
+        kw = dict(kw)
     elif case.startswith("n") and case[1:].isdigit():
         logn, kw = int(case[1:]), {}
     else:
         raise SystemExit(f"unknown case {case!r}; known: {sorted(CASES)} or n<log2 N>")
     estl.init(0)
     n = 1 << logn
-    batch = max(1, (1 << elements_log) // n)
+    batch = kw.pop("batch", max(1, (1 << elements_log) // n))
     x = torch.view_as_complex((torch.rand((n * batch, 2), device="cuda") * 2 - 1).contiguous())
     y = torch.empty_like(x)
     p = estl.Plan(n, batch, estl.FORWARD, **kw)
