@@ -34,7 +34,9 @@ struct ConvRow {
   long long out_off;   // real output
   int sig_len;         // valid input samples; the rest of the N-point row is zero
   int out_len;         // output samples written
-  int out_shift;       // first sample of the circular result that is written
+  int out_shift;       // first sample of the circular result that is written; output m is
+                       // sample (m + out_shift) mod N (the reference's cyclic kernel shift,
+                       // Convolution.h:113-120, wraps when out_shift + out_len > N)
   float scale;         // spectrum kernels: multiplies the spectrum (1/N, or 1/(N*sum h))
   float conj;          // spectrum kernels: -1 stores conj(H) (correlation), +1 H
   int dc_norm;         // conv kernels: divide the output by N * spectrum[0] (= sum of the
@@ -132,8 +134,8 @@ struct ConvSingleKernel {
         const float g = dc_factor(a, r);
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) {
-          const int m = t + TL::T * j - r.out_shift;
-          if (m >= 0 && m < r.out_len) o[m] = v[j].x * g;
+          const int m = (t + TL::T * j - r.out_shift) & (TL::M - 1);
+          if (m < r.out_len) o[m] = v[j].x * g;
         }
       }
     }
@@ -358,16 +360,16 @@ struct ConvPairKernel : ConvSingleKernel<LOGM, LOGE, LOGR, LOGC, TC> {
         const Ptr<float> o1 = a.out.sub(r1.out_off, r1.out_len);
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) {
-          const int m = t + TL::T * j - r1.out_shift;
-          if (m >= 0 && m < r1.out_len) o1[m] = v[j].x * g1;
+          const int m = (t + TL::T * j - r1.out_shift) & (TL::M - 1);
+          if (m < r1.out_len) o1[m] = v[j].x * g1;
         }
       }
       if (has2) {
         const Ptr<float> o2 = a.out.sub(r2.out_off, r2.out_len);
 #pragma unroll
         for (int j = 0; j < TL::E; ++j) {
-          const int m = t + TL::T * j - r2.out_shift;
-          if (m >= 0 && m < r2.out_len) o2[m] = -v[j].y * g2;
+          const int m = (t + TL::T * j - r2.out_shift) & (TL::M - 1);
+          if (m < r2.out_len) o2[m] = -v[j].y * g2;
         }
       }
     }
@@ -580,9 +582,9 @@ struct ConvOutKernel {
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int n2 = t2 + TL::T * j;
-      const int m = n1_0 + c2 + (n2 << logn1) - r.out_shift;
+      const int m = (n1_0 + c2 + (n2 << logn1) - r.out_shift) & ((1 << a.logn) - 1);
       const float val = sm[sidx(c2, n2)].x;
-      if (m >= 0 && m < r.out_len) o[m] = val * g;
+      if (m < r.out_len) o[m] = val * g;
     }
   }
 };
@@ -821,9 +823,10 @@ struct ConvOutHalfKernel {
     for (int j = 0; j < TL::E; ++j) {
       const int n2 = t2 + TL::T * j;
       const cf32 val = sm[sidx(c2, n2)];  // conj(v_m)
-      const int m = 2 * (n1_0 + c2 + (n2 << logn1)) - r.out_shift;
-      if (m >= 0 && m < r.out_len) o[m] = val.x * g;
-      if (m + 1 >= 0 && m + 1 < r.out_len) o[m + 1] = -val.y * g;
+      const int pos = 2 * (n1_0 + c2 + (n2 << logn1));
+      const int m0 = (pos - r.out_shift) & (2 * NH - 1), m1 = (pos + 1 - r.out_shift) & (2 * NH - 1);
+      if (m0 < r.out_len) o[m0] = val.x * g;
+      if (m1 < r.out_len) o[m1] = -val.y * g;
     }
   }
 };

@@ -37,6 +37,15 @@ int conv_logn(long long signal_len, long long filter_len) {
   return l;
 }
 
+int conv_out_shift(long long filter_len, int logn, int flags) {
+  if (!(flags & CONV_REFERENCE_COMPAT)) return 0;
+  const long long n = 1LL << logn, off = (filter_len + 1) / 2;
+  // the kernel shifted by -off (Convolution.h:113-120) moves a convolution by
+  // -off and a correlation, whose kernel spectrum is conjugated after the
+  // shift (:125-137), by +off
+  return (int)((flags & CONV_CORRELATE) ? (n - off % n) % n : off % n);
+}
+
 long long conv_out_len(long long signal_len, long long filter_len, int flags) {
   return (flags & CONV_REFERENCE_COMPAT) ? signal_len : signal_len + filter_len - 1;
 }
@@ -109,7 +118,7 @@ bool build_conv_layout(const ConvReq* reqs, int count, int flags, ConvLayout* ou
       s.spec_off = new_spectrum ? spec : L.filt_rows[0].spec_off;
       s.out_off = q.out_off;
       s.out_len = (int)conv_out_len(q.signal_len, q.filter_len, flags);
-      s.out_shift = (flags & CONV_REFERENCE_COMPAT) ? (int)((q.filter_len + 1) / 2) : 0;
+      s.out_shift = conv_out_shift(q.filter_len, logn, flags);
       s.dc_norm = (flags & CONV_REFERENCE_COMPAT) ? 1 : 0;
       s.scale = 1.f;
       s.conj = 1.f;

@@ -97,6 +97,9 @@ constexpr long long kMaxConvSmemBytes = 227 * 1024;
 // in reference-compatible mode).
 long long conv_out_len(long long signal_len, long long filter_len, int flags);
 int conv_logn(long long signal_len, long long filter_len);
+// First circular sample of the output in reference-compatible mode (0
+// otherwise): output m is sample (m + shift) mod 2^logn of the result.
+int conv_out_shift(long long filter_len, int logn, int flags);
 
 // shared_filter: every request uses the filter of request 0 (one spectrum,
 // computed once); all requests must then pad to the same N.

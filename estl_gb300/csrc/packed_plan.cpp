@@ -19,15 +19,24 @@ int packed_col_logc(int logn) { return logc_for_m(packed_logn2(logn)); }
 int packed_row_logc(int logn) { return logc_for_m(logn - packed_logn2(logn)); }
 
 bool build_packed_layout(const long long* offsets, const long long* sizes, long long count, bool persistent,
-                         PackedLayout* out, std::string* err) {
+                         PackedLayout* out, std::string* err, const ConvReq* convs, long long nconv,
+                         int conv_flags) {
   PackedLayout L;
   L.persistent = persistent;
-  if (count < 1 || !offsets || !sizes) {
-    if (err) *err = "need at least one transform";
+  if (nconv < 0 || nconv > (1LL << 30) || (nconv > 0 && !convs)) {
+    if (err) *err = "bad convolution list";
+    return false;
+  }
+  if (count < 0 || (count > 0 && (!offsets || !sizes)) || (count == 0 && nconv == 0)) {
+    if (err) *err = "need at least one transform or convolution";
     return false;
   }
   if (count > (1LL << 30)) {
     if (err) *err = "too many transforms";
+    return false;
+  }
+  if (conv_flags & ~(CONV_CORRELATE | CONV_REFERENCE_COMPAT | CONV_NO_PAIRING | CONV_COMPLEX)) {
+    if (err) *err = "convolution flags of a mixed batch: CORRELATE, REFERENCE_COMPAT, NO_PAIRING, COMPLEX (FP32)";
     return false;
   }
   L.offsets.assign(offsets, offsets + count);
@@ -66,9 +75,57 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
   // class lists, smallest class first
   std::vector<std::vector<int>> cls(kPackedMaxLog + 1);
   for (long long i = 0; i < count; ++i) cls[L.lognv[i]].push_back((int)i);
-  std::vector<PackedItem> single_items, col_items, row_items;
+  std::vector<PackedItem> single_items, col_items, row_items, conv_items;
   std::vector<std::vector<PackedItem>> per_class(kPackedMaxLog + 1);
   std::vector<std::vector<PackedItem>> per_class_row(kPackedMaxLog + 1);
+  std::vector<std::vector<PackedItem>> per_class_conv(kPackedSingleMaxLog + 1);
+  // convolutions: padded lengths up to 2^12 are work items, C whole requests
+  // of one length per item (the single tiles' C); longer ones go to the engine
+  std::vector<std::vector<int>> ccls(kPackedSingleMaxLog + 1);
+  for (long long i = 0; i < nconv; ++i) {
+    const ConvReq& q = convs[i];
+    if (q.signal_len < 1 || q.filter_len < 1 || q.sig_off < 0 || q.filt_off < 0 || q.out_off < 0 ||
+        q.signal_len > (1LL << kConvMaxLogN) || q.filter_len > (1LL << kConvMaxLogN)) {
+      if (err) *err = "convolution " + std::to_string(i) + ": lengths must be in [1, 2^22] and offsets >= 0";
+      return false;
+    }
+    const int l = conv_logn(q.signal_len, q.filter_len);
+    if (l > kConvMaxLogN) {
+      if (err) *err = "convolution " + std::to_string(i) + ": padded length exceeds 2^" + std::to_string(kConvMaxLogN);
+      return false;
+    }
+    const long long olen = conv_out_len(q.signal_len, q.filter_len, conv_flags);
+    L.conv_sig_elems = std::max(L.conv_sig_elems, q.sig_off + q.signal_len);
+    L.conv_filt_elems = std::max(L.conv_filt_elems, q.filt_off + q.filter_len);
+    L.conv_out_elems = std::max(L.conv_out_elems, q.out_off + olen);
+    if (l > kPackedSingleMaxLog) {
+      L.conv_engine.push_back(q);
+      continue;
+    }
+    PackedConv pc;
+    pc.sig_off = q.sig_off;
+    pc.filt_off = q.filt_off;
+    pc.out_off = q.out_off;
+    pc.sig_len = (int)q.signal_len;
+    pc.filt_len = (int)q.filter_len;
+    pc.out_len = (int)olen;
+    pc.out_shift = conv_out_shift(q.filter_len, l, conv_flags);
+    pc.correlate = (conv_flags & CONV_CORRELATE) ? 1 : 0;
+    pc.dc_norm = (conv_flags & CONV_REFERENCE_COMPAT) ? 1 : 0;
+    ccls[l].push_back((int)L.convs.size());
+    L.convs.push_back(pc);
+    L.conv_flops += 10.0 * (double)(1LL << l) * l;
+  }
+  for (int l = 1; l <= kPackedSingleMaxLog; ++l) {
+    const int per = 1 << packed_single_logc(l);
+    const int base = (int)L.conv_class_list.size();
+    L.conv_class_list.insert(L.conv_class_list.end(), ccls[l].begin(), ccls[l].end());
+    for (int k = 0; k < (int)ccls[l].size(); k += per) {
+      PackedItem it{PK_CONV, l, base + k, std::min(per, (int)ccls[l].size() - k)};
+      conv_items.push_back(it);
+      per_class_conv[l].push_back(it);
+    }
+  }
   for (int l = kPackedMinLog; l <= kPackedMaxLog; ++l) {
     if (cls[l].empty()) continue;
     if (l <= kPackedSingleMaxLog) {
@@ -101,20 +158,24 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
     }
   }
   if (persistent) {
-    // Column items of the largest transforms first, then whole small
-    // transforms (they keep the SMs busy while the column items finish), then
-    // the row items in the same transform order: a row item is only taken
-    // after every column item has been taken by a running CTA, so its
-    // dependency wait ends.
+    // Column items of the largest transforms first, then convolutions and
+    // whole small transforms (they keep the SMs busy while the column items
+    // finish), then the row items in the same transform order: a row item is
+    // only taken after every column item has been taken by a running CTA, so
+    // its dependency wait ends.
     auto by_size_desc = [](const PackedItem& a, const PackedItem& b) { return a.logn > b.logn; };
     std::stable_sort(col_items.begin(), col_items.end(), by_size_desc);
     std::stable_sort(row_items.begin(), row_items.end(), by_size_desc);
     std::stable_sort(single_items.begin(), single_items.end(), by_size_desc);
+    std::stable_sort(conv_items.begin(), conv_items.end(), by_size_desc);
     L.items = col_items;
+    L.items.insert(L.items.end(), conv_items.begin(), conv_items.end());
     L.items.insert(L.items.end(), single_items.begin(), single_items.end());
     L.items.insert(L.items.end(), row_items.begin(), row_items.end());
-    L.launch_begin.push_back(0);
-    L.launch_count.push_back((int)L.items.size());
+    if (!L.items.empty()) {  // none when every convolution runs on the engine
+      L.launch_begin.push_back(0);
+      L.launch_count.push_back((int)L.items.size());
+    }
   } else {
     // one launch per size class (two for four-step classes: columns, then rows)
     for (int l = kPackedMinLog; l <= kPackedMaxLog; ++l) {
@@ -129,6 +190,12 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
         L.items.insert(L.items.end(), per_class_row[l].begin(), per_class_row[l].end());
       }
     }
+    for (int l = 1; l <= kPackedSingleMaxLog; ++l)
+      if (!per_class_conv[l].empty()) {
+        L.launch_begin.push_back((int)L.items.size());
+        L.launch_count.push_back((int)per_class_conv[l].size());
+        L.items.insert(L.items.end(), per_class_conv[l].begin(), per_class_conv[l].end());
+      }
   }
   *out = std::move(L);
   return true;

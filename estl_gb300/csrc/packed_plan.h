@@ -7,15 +7,31 @@
 // bodies of fft_core.cuh with a fixed CTA of 256 threads:
 //   n <= 2^12           one item = C whole transforms of one size
 //   2^13 <= n <= 2^18   four-step: column items then row items per transform
+// A mixed batch adds FFT convolutions (Convolution.h:95-154 in 1D): those of
+// padded length <= 2^12 are work items of the same launch (one item = C whole
+// convolutions), longer ones run the convolution engine's own launches.
 #pragma once
 #include <string>
 #include <vector>
 
+#include "conv_plan.h"
 #include "planner.h"
 
 namespace estl {
 
-enum PackedItemKind { PK_SINGLE = 0, PK_COL = 1, PK_ROW = 2 };
+enum PackedItemKind { PK_SINGLE = 0, PK_COL = 1, PK_ROW = 2, PK_CONV = 3 };
+
+// One convolution work item's request: real signal (sig_len floats at
+// sig_off) * real filter (filt_len floats at filt_off), zero-padded to the
+// item's length; output samples [out_shift, out_shift + out_len) of the
+// circular result go to out_off.  correlate: the filter spectrum is
+// conjugated (Convolution.h:125-137); dc_norm: the result is divided by the
+// filter's sum, the spectrum DC (Convolution.h:141-143).
+struct PackedConv {
+  long long sig_off, filt_off, out_off;
+  int sig_len, filt_len, out_len, out_shift;
+  int correlate, dc_norm;
+};
 
 struct PackedItem {
   int kind;   // PackedItemKind
@@ -48,13 +64,26 @@ struct PackedLayout {
   long long elements = 0;     // sum of lengths
   double flops = 0;           // sum of 5 n log2 n
   bool persistent = true;
+  // mixed batches: convolutions run as work items (padded length <= 2^12) ...
+  std::vector<PackedConv> convs;
+  std::vector<int> conv_class_list;  // convs grouped by padded length
+  // ... and the longer ones, run by the convolution engine
+  std::vector<ConvReq> conv_engine;
+  long long conv_sig_elems = 0, conv_filt_elems = 0, conv_out_elems = 0;  // float extents
+  double conv_flops = 0;  // 2 x 5 n log2 n per in-kernel convolution
 };
 
-// offsets / sizes: count transforms.  Returns false with *err on a size that
-// is not a power of two in [2^1, 2^18], a negative offset, or overlapping
-// transforms.
+// offsets / sizes: count transforms (count may be 0 when nconv > 0).
+// Returns false with *err on a size that is not a power of two in
+// [2^1, 2^18], a negative offset, or overlapping transforms.  convs / nconv:
+// the convolutions of a mixed batch, conv_flags the CONV_CORRELATE /
+// CONV_REFERENCE_COMPAT semantics of all of them (CONV_NO_PAIRING and
+// CONV_COMPLEX only shape the convolution engine's launches of the longer
+// ones); a request needs lengths >= 1, offsets >= 0 and a padded length of
+// at most 2^22.
 bool build_packed_layout(const long long* offsets, const long long* sizes, long long count, bool persistent,
-                         PackedLayout* out, std::string* err);
+                         PackedLayout* out, std::string* err, const ConvReq* convs = nullptr, long long nconv = 0,
+                         int conv_flags = 0);
 
 // Bucketed uneven batches: one size class of the batch, run by the engine's
 // own plan for (2^logn, count) over the class's transforms through their

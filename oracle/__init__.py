@@ -56,6 +56,8 @@ def _load():
         lib.oracle_conv_direct.argtypes = [P, I64, P, I64, P]
         lib.oracle_conv_fft.argtypes = [P, I64, P, I64, P, ctypes.c_int]
         lib.oracle_conv_fft.restype = ctypes.c_int
+        lib.oracle_conv_circular.argtypes = [P, I64, P, I64, I64, P, I64, ctypes.c_int]
+        lib.oracle_conv_circular.restype = ctypes.c_int
         lib.oracle_conv2d_fft.argtypes = [P, I64, I64, P, I64, I64, P, ctypes.c_int, ctypes.c_int]
         lib.oracle_conv2d_fft.restype = ctypes.c_int
         lib.oracle_conv2d_direct.argtypes = [P, I64, I64, P, I64, I64, P]
@@ -123,6 +125,36 @@ def conv_fft(a, b, correlate=False):
     out = np.empty(a.size + b.size - 1)
     _load().oracle_conv_fft(_ptr(a), a.size, _ptr(b), b.size, _ptr(out), int(bool(correlate)))
     return out
+
+
+def conv_circular(a, b, n, correlate=False):
+    """FP64 n-point circular convolution (correlation: product with the
+    conjugate spectrum) of two real sequences zero-padded to n."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.empty(n)
+    rc = _load().oracle_conv_circular(_ptr(a), a.size, _ptr(b), b.size, int(n), _ptr(out), int(n), int(bool(correlate)))
+    if rc:
+        raise ValueError("n must cover both sequences")
+    return out
+
+
+def conv_compat(s, h, correlate=False):
+    """1D restatement of Convolution2D_FFT::convolve's own result
+    (Convolution.h:95-148): both padded to n = nextPowerOf2(L + K - 1) (at
+    least 2, the engine's smallest transform; the padding beyond L + K - 1
+    holds zeros either way), the kernel shifted cyclically by (K + 1) / 2
+    (:113-120), so output m is circular sample (m + (K + 1) / 2) mod n of the
+    convolution -- of the correlation, whose spectrum is conjugated after the
+    shift (:125-137), sample (m - (K + 1) / 2) mod n -- divided by
+    sum(h) = K^[0] (:141-143), L samples kept (:146-148)."""
+    L, K = len(s), len(h)
+    n = 2
+    while n < L + K - 1:
+        n *= 2
+    circ = conv_circular(s, h, n, correlate)
+    off = -((K + 1) // 2) if correlate else (K + 1) // 2
+    return circ[(np.arange(L) + off) % n] / np.sum(np.asarray(h, np.float64))
 
 
 def conv2d_fft(a, k, correlate=False, compat=False):

@@ -244,9 +244,22 @@ void oracle_conv_direct(const double* a, int64_t la, const double* b, int64_t lb
  * n = nextPow2(la + lb - 1) (Convolution.h:89-97), forward FFT, pointwise
  * product (Convolution.h:132-136; conj(B) when correlate, :125-130), inverse
  * FFT, scale 1/n, keep the real part of the first la + lb - 1 samples. */
+int oracle_conv_circular(const double* a, int64_t la, const double* b, int64_t lb, int64_t n, double* out,
+                         int64_t keep, int correlate);
+
 int oracle_conv_fft(const double* a, int64_t la, const double* b, int64_t lb, double* out, int correlate) {
   int64_t len = la + lb - 1, n = 1;
   while (n < len) n *= 2;
+  return oracle_conv_circular(a, la, b, lb, n, out, len, correlate);
+}
+
+/* The first `keep` samples of the n-point circular convolution (correlation:
+ * the product with the conjugate spectrum) of a and b, both zero-padded to n
+ * (n >= la, lb), by FP64 FFTs. */
+int oracle_conv_circular(const double* a, int64_t la, const double* b, int64_t lb, int64_t n, double* out,
+                         int64_t keep, int correlate) {
+  const int64_t len = keep;
+  if (n < la || n < lb || keep > n) return 1;
   c64* A = (c64*)calloc((size_t)n, sizeof(c64));
   c64* B = (c64*)calloc((size_t)n, sizeof(c64));
   for (int64_t i = 0; i < la; i++) A[i].re = a[i];

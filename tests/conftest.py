@@ -63,6 +63,9 @@ def emu():
     lib.emu_cluster_barrier_selftest.restype = ctypes.c_int
     lib.emu_packed_bucketed_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
     lib.emu_packed_bucketed_run.restype = ctypes.c_int
+    lib.emu_packed_mixed_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, P, P, P,
+                                         ctypes.c_longlong, ctypes.c_int, P, P, P, ctypes.c_char_p, ctypes.c_int]
+    lib.emu_packed_mixed_run.restype = ctypes.c_int
     lib.emu_bank.argtypes = [P]
     lib.emu_bank.restype = ctypes.c_longlong
     return lib

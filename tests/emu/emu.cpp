@@ -824,11 +824,38 @@ int emu_packed_run(const long long* offsets, const long long* sizes, long long c
 // column items (non-persistent mode): the row items' dependency waits then
 // wait for counts that nothing raises, give up after their iteration limit,
 // set the error word and skip their work (return 4, output untouched).
+static int packed_emulate(const long long* offsets, const long long* sizes, long long count, int persistent,
+                          int sign, const float* in, float* out, int skip_columns, const long long* convs,
+                          long long nconv, int conv_flags, const float* sig, const float* filt, float* cout,
+                          char* err, int errlen);
+
 int emu_packed_run_launches(const long long* offsets, const long long* sizes, long long count, int persistent,
                             int sign, const float* in, float* out, int skip_columns, char* err, int errlen) {
+  return packed_emulate(offsets, sizes, count, persistent, sign, in, out, skip_columns, nullptr, 0, 0, nullptr,
+                        nullptr, nullptr, err, errlen);
+}
+
+// Mixed uneven batch: count transforms (as emu_packed_run) and nconv FFT
+// convolutions (5 values each: signal_len, filter_len, signal, filter and
+// output offsets in floats, as estl_conv_request), conv_flags as
+// estl_conv_execute.  Convolutions of padded length <= 2^12 run as work items
+// of the packed kernel, longer ones through the convolution engine's launches
+// (as emu_conv_run).  Returns as emu_packed_run.
+int emu_packed_mixed_run(const long long* offsets, const long long* sizes, long long count, int persistent, int sign,
+                         const float* in, float* out, const long long* convs, long long nconv, int conv_flags,
+                         const float* sig, const float* filt, float* cout, char* err, int errlen) {
+  return packed_emulate(offsets, sizes, count, persistent, sign, in, out, 0, convs, nconv, conv_flags, sig, filt, cout,
+                        err, errlen);
+}
+
+static int packed_emulate(const long long* offsets, const long long* sizes, long long count, int persistent,
+                          int sign, const float* in, float* out, int skip_columns, const long long* convs,
+                          long long nconv, int conv_flags, const float* sig, const float* filt, float* cout,
+                          char* err, int errlen) {
   PackedLayout L;
   std::string e;
-  if (!build_packed_layout(offsets, sizes, count, persistent != 0, &L, &e)) {
+  if (!build_packed_layout(offsets, sizes, count, persistent != 0, &L, &e,
+                           reinterpret_cast<const ConvReq*>(convs), nconv, conv_flags)) {
     set_err(err, errlen, e);
     return 2;
   }
@@ -858,6 +885,11 @@ int emu_packed_run_launches(const long long* offsets, const long long* sizes, lo
     a.error = &error;
     a.sgn = sign < 0 ? 1.f : -1.f;
     a.persistent = persistent ? 1 : 0;
+    a.convs = Ptr<const PackedConv>{L.convs.data(), (long long)L.convs.size()};
+    a.conv_class_list = Ptr<const int>{L.conv_class_list.data(), (long long)L.conv_class_list.size()};
+    a.csig = Ptr<const float>{sig, L.conv_sig_elems};
+    a.cfilt = Ptr<const float>{filt, L.conv_filt_elems};
+    a.cout = Ptr<float>{cout, L.conv_out_elems};
     counters[0] = 0;
     if (skip_columns && !persistent && a.nitems > 0 && L.items[(size_t)a.item_base].kind == PK_COL) continue;
     int slot[2] = {0, 0};
@@ -873,6 +905,9 @@ int emu_packed_run_launches(const long long* offsets, const long long* sizes, lo
     set_err(err, errlen, "dependency wait gave up");
     return 4;
   }
+  if (!L.conv_engine.empty())
+    return emu_conv_run(reinterpret_cast<const long long*>(L.conv_engine.data()), (int)L.conv_engine.size(),
+                        conv_flags, 0, sig, filt, cout, err, errlen);
   return 0;
 }
 

@@ -41,13 +41,11 @@ def make_requests(shapes, seed):
     return reqs, np.concatenate(sigs), np.concatenate(filts), oo
 
 
-def compat_reference(s, f):
-    """Convolution.h's normalisation and crop in 1D: centre the kernel by
-    (K+1)/2 (:113-120), divide by sum(h) (= K^[0], :141-143), keep L samples."""
-    L, K = len(s), len(f)
-    full = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))
-    sh = (K + 1) // 2
-    return full[sh: sh + L] / np.sum(f.astype(np.float64))
+def compat_reference(s, f, correlate=False):
+    """Convolution.h's normalisation and crop in 1D: the kernel shifted
+    cyclically by (K+1)/2 (:113-120), divided by sum(h) (= K^[0], :141-143),
+    L samples kept (:146-148) -- oracle.conv_compat."""
+    return oracle.conv_compat(s, f, correlate)
 
 
 def emu_conv(emu, reqs, sig, filt, out_len, flags=0, shared=False):
@@ -131,11 +129,7 @@ def test_emulated_pairs_odd_buckets(emu, flags):
     for L, K, so, fo, o in creqs:
         s, f = sig[so:so + L], filt[fo:fo + K]
         if compat:
-            ref = compat_reference(s, f)
-            if flags & 1:
-                full = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=True)
-                sh = (K + 1) // 2
-                ref = full[sh: sh + L] / np.sum(f.astype(np.float64))
+            ref = compat_reference(s, f, correlate=bool(flags & 1))
         else:
             ref = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1))
         n_out = L if compat else L + K - 1
@@ -336,8 +330,29 @@ def test_emulated_real_input_four_step(emu, flags):
     for L, K, so, fo, o in creqs:
         s, f = sig[so:so + L], filt[fo:fo + K]
         if compat:
-            ref, n = compat_reference(s, f), L
+            ref, n = compat_reference(s, f, correlate=bool(flags & 1)), L
         else:
             ref, n = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1)), L + K - 1
         assert rel(half[o:o + n], ref) < TOL, (L, K, flags)
         assert rel(full[o:o + n], ref) < TOL, (L, K, flags)
+
+
+@pytest.mark.parametrize("flags", [2, 3])
+def test_emulated_compat_crop_wraps(emu, flags):
+    """Reference-compatible mode when the crop runs past the padded length:
+    a 1-tap filter on a power-of-two signal pads to n = L, so the kernel's
+    cyclic shift by (K+1)/2 = 1 (Convolution.h:113-120) makes the last output
+    sample circular sample 0.  Single-tile (paired and unpaired), real-input
+    four-step and complex four-step paths."""
+    shapes = [(4, 1), (16, 1), (1024, 1), (16384, 1), (32768, 1), (5, 1)]
+    reqs, sig, filt, _ = make_requests(shapes, 71)
+    filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L
+    for extra in (0, NO_PAIRING, COMPLEX):
+        out = emu_conv(emu, creqs, sig, filt, oo, flags=flags | extra)
+        for L, K, so, fo, o in creqs:
+            ref = compat_reference(sig[so:so + L], filt[fo:fo + K], correlate=bool(flags & 1))
+            assert rel(out[o:o + L], ref) < TOL, (L, K, flags, extra)

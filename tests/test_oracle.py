@@ -149,3 +149,35 @@ def test_dft_bins_matches_the_direct_dft_and_numpy():
     ref = np.fft.fft(x)[bins]
     got = oracle.dft_bins(x, bins, -1)
     assert np.max(np.abs(got - ref)) / np.sqrt(n) < 1e-11
+
+
+def test_conv_compat_follows_the_reference_loops():
+    """oracle.conv_compat against a literal 1D restatement of the loops of
+    Convolution2D_FFT::convolve (Convolution.h:95-148) in long double: the
+    kernel written at (x + (K+1)/2) % width (:113-120), the product of the
+    spectra (with the conjugate for correlation, :125-137), and the first L
+    samples of the inverse scaled by 1 / (width * K^[0]) (:141-148); the
+    spectra are taken as direct DFTs."""
+    rng = np.random.default_rng(5)
+    for L, K in [(4, 1), (5, 1), (7, 3), (8, 2), (13, 6), (16, 16)]:
+        s = rng.standard_normal(L)
+        h = np.abs(rng.standard_normal(K)) + 0.1
+        width = 1
+        while width < L + K - 1:
+            width *= 2
+        width = max(width, 2)
+        data = np.zeros(width, np.clongdouble)
+        data[:L] = s
+        kern = np.zeros(width, np.clongdouble)
+        off = (K + 1) // 2
+        for x in range(width):
+            src = (x + off) % width
+            kern[x] = h[src] if src < K else 0
+        q = np.arange(width)
+        W = np.exp(-2j * np.pi * np.outer(q, q).astype(np.longdouble) / width)
+        D, H = W @ data, W @ kern
+        for correlate in (False, True):
+            prod = D * (np.conj(H) if correlate else H)
+            inv = (np.conj(W) @ prod).real / (width * H[0].real)
+            ref = oracle.conv_compat(s, h, correlate)
+            assert np.allclose(ref, inv[:L].astype(np.float64), rtol=1e-12, atol=1e-12), (L, K, correlate)

@@ -298,3 +298,113 @@ def test_gpu_bucketed(engine, gap):
         for o, n in zip(offsets, sizes):
             mask[o:o + n] = False
         assert np.all(np.isnan(y[mask].real))
+
+
+# ---------------------------------------------------------------------------
+# Mixed batches: transforms and FFT convolutions (Convolution.h:95-154 in 1D)
+# in one packed plan.  Convolutions of padded length <= 2^12 are work items of
+# the packed kernel (signal and filter as the halves of one complex transform,
+# spectra split with X_{-k}); longer ones run the convolution engine's launches.
+# ---------------------------------------------------------------------------
+CONV_TOL = 1e-6
+
+
+def conv_rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
+
+
+def make_convs(shapes, seed, flags=0, scales=None):
+    """Requests for (L, K) pairs, packed with gaps of one float; filters
+    positive in reference-compatible mode (sum(h) away from zero); optional
+    per-request (signal, filter) scales."""
+    rng = np.random.default_rng(seed)
+    compat = bool(flags & 2)
+    reqs, sigs, filts = [], [], []
+    so = fo = oo = 0
+    for i, (L, K) in enumerate(shapes):
+        ss, fs = scales[i] if scales else (1.0, 1.0)
+        s = (rng.standard_normal(L) * ss).astype(np.float32)
+        f = rng.standard_normal(K).astype(np.float32)
+        f = ((np.abs(f) + 0.1) if compat else f) * fs
+        reqs.append((L, K, so, fo, oo))
+        sigs.append(np.append(s, np.float32(np.nan)))
+        filts.append(np.append(f.astype(np.float32), np.float32(np.nan)))
+        so += L + 1
+        fo += K + 1
+        oo += (L if compat else L + K - 1) + 1
+    return np.array(reqs, np.int64), np.concatenate(sigs), np.concatenate(filts), oo
+
+
+def conv_reference(s, f, flags):
+    if flags & 2:  # Convolution.h:113-148: cyclic kernel shift by (K+1)/2, / sum(h), L samples
+        return oracle.conv_compat(s, f, correlate=bool(flags & 1))
+    return oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1))
+
+
+def check_convs(reqs, sig, filt, cout, flags):
+    for i, (L, K, so, fo, oo) in enumerate(reqs):
+        ref = conv_reference(sig[so:so + L], filt[fo:fo + K], flags)
+        got = cout[oo:oo + len(ref)]
+        assert conv_rel(got, ref) < CONV_TOL, (i, L, K, conv_rel(got, ref))
+        assert np.isnan(cout[oo + len(ref)]), (i, "wrote past its output")
+
+
+def emu_mixed(emu, offsets, sizes, x, persistent, sign, reqs, sig, filt, olen, flags):
+    y = np.full_like(x, np.nan + 1j * np.nan)
+    cout = np.full(olen, np.nan, np.float32)
+    err = ctypes.create_string_buffer(512)
+    rc = emu.emu_packed_mixed_run(offsets.ctypes.data, sizes.ctypes.data, len(sizes), int(persistent), sign,
+                                  x.ctypes.data, y.ctypes.data, reqs.ctypes.data, len(reqs), flags, sig.ctypes.data,
+                                  filt.ctypes.data, cout.ctypes.data, err, len(err))
+    return rc, err.value.decode(), y, cout
+
+
+# padded lengths 2^1..2^12 in the kernel, 2^13 and 2^15 through the engine
+MIXED_CONV_SHAPES = [(1, 1), (2, 1), (3, 2), (5, 4), (9, 8), (20, 13), (33, 32), (100, 17), (200, 57), (300, 212),
+                     (1000, 25), (1500, 549), (3000, 1000), (2048, 2049), (5000, 300), (20000, 100)]
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_emulated_mixed_transforms_and_convolutions(emu, flags, persistent):
+    """A mixed batch through the bounds-checked emulator: transforms of 2^1..2^15
+    against oracle.fft and convolutions of every in-kernel padded length (and
+    two engine ones) against oracle.conv_fft, every flag combination; the
+    floats between requests stay untouched."""
+    offsets, sizes, x = make_batch(24, 1, 15, 51, gap=3)
+    reqs, sig, filt, olen = make_convs(MIXED_CONV_SHAPES, 52 + flags, flags)
+    rc, msg, y, cout = emu_mixed(emu, offsets, sizes, x, persistent, -1, reqs, sig, filt, olen, flags)
+    assert rc == 0, msg
+    check_against_oracle(offsets, sizes, x, y, -1)
+    check_convs(reqs, sig, filt, cout, flags)
+
+
+def test_emulated_mixed_convolutions_only_and_magnitudes(emu):
+    """Only convolutions (no transforms), and requests whose signal and filter
+    differ by up to 10^9 in scale: the power-of-two balance of the two halves
+    keeps every request at the FP32 tolerance."""
+    shapes = [(700, 90), (1000, 20), (60, 3), (2000, 2000), (4, 4)]
+    scales = [(1e4, 1e-3), (1e-3, 1e2), (1.0, 1e-5), (1e-4, 1e5), (1.0, 1.0)]
+    reqs, sig, filt, olen = make_convs(shapes, 61, 0, scales)
+    empty = np.zeros(0, np.int64)
+    x = np.zeros(1, np.complex64)
+    rc, msg, _, cout = emu_mixed(emu, empty, empty, x, 1, -1, reqs, sig, filt, olen, 0)
+    assert rc == 0, msg
+    check_convs(reqs, sig, filt, cout, 0)
+
+
+def test_emulated_mixed_validation(emu):
+    offsets, sizes, x = make_batch(2, 4, 6, 1)
+    empty = np.zeros(0, np.int64)
+    for bad in ([(0, 5, 0, 0, 0)], [(5, 5, -1, 0, 0)], [(1 << 22, 2, 0, 0, 0)]):
+        reqs = np.array(bad, np.int64)
+        sig = np.zeros(8, np.float32)
+        rc, msg, _, _ = emu_mixed(emu, offsets, sizes, x, 1, -1, reqs, sig, sig, 16, 0)
+        assert rc == 2 and "convolution 0" in msg, (bad, msg)
+    rc, msg, _, _ = emu_mixed(emu, empty, empty, x, 1, -1, np.zeros((0, 5), np.int64), x.real, x.real, 1, 0)
+    assert rc == 2 and "at least one" in msg
+    reqs, sig, filt, olen = make_convs([(10, 3)], 1)
+    rc, msg, _, _ = emu_mixed(emu, offsets, sizes, x, 1, -1, reqs, sig, filt, olen, 1 << 8)
+    assert rc == 2 and "FP32" in msg
