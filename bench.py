@@ -374,6 +374,33 @@ def bench_config1(estl, torch, autotune=True):
     d = plan.describe()["kernels"]
     del g  # the graph holds the plan's ordering event
     plan.close()
+    # where the time goes: the same graph method over other batch counts (one
+    # CTA per transform: 1 = one CTA's latency, 152 = one per SM), and with
+    # one buffer pair (the data stays in L2)
+    curve = {}
+    for b in (1, 152, 256, 1024):
+        xb = [torch.view_as_complex(torch.rand((b * n, 2), device="cuda") * 2 - 1) for _ in range(rot)]
+        yb = [torch.empty(b * n, dtype=torch.complex64, device="cuda") for _ in range(rot)]
+        pb = estl.Plan(n, b, estl.FORWARD)
+        row = {}
+        for name, nrot in (("cold_us", rot), ("l2_resident_us", 1)):
+            gb = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gb, stream=s):
+                for i in range(reps):
+                    pb.execute_ptr(xb[i % nrot].data_ptr(), yb[i % nrot].data_ptr(), s.cuda_stream)
+            for _ in range(3):
+                gb.replay()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(replays):
+                gb.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            row[name] = round(1e3 * e0.elapsed_time(e1) / (replays * reps), 3)
+            del gb
+        pb.close()
+        curve[str(b)] = row
+        del xb, yb
     # the reference's algorithm (FP32 restatement) on the host cores, same workload
     import oracle
     threads = os.cpu_count() or 1
@@ -390,7 +417,7 @@ def bench_config1(estl, torch, autotune=True):
     return {"workload": "C2C FP32 forward, N=4096, batch=256, uniform[-1,1) seed 1", "cpu_baseline": cpu,
             "method": "CUDA graph of 64 executes over 32 rotating buffer pairs (512 MiB > L2), "
                       "16 replays timed (1024 executes)",
-            "plan": d, "autotune_fastest": tuned,
+            "plan": d, "autotune_fastest": tuned, "us_per_execute_by_batch": curve,
             "us_per_transform_batch": round(1e3 * ms, 3), "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1),
             "gflops": round(5 * n * 12 * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": err}
 
@@ -444,6 +471,79 @@ def bench_uneven(estl, torch):
         L.estl_packed_plan_destroy(plan)
     res["persistent_speedup"] = round(res["per_size"]["ms"] / res["persistent"]["ms"], 3)
     res["bucketed_vs_persistent"] = round(res["persistent"]["ms"] / res["bucketed"]["ms"], 3)
+    res["mixed"] = bench_uneven_mixed(estl, torch, offsets, sizes, x, y)
+    return res
+
+
+def bench_uneven_mixed(estl, torch, offsets, sizes, x, y):
+    """The same 8192 transforms plus 4096 FFT convolutions in one plan
+    (estl_packed_mixed_plan_create): padded lengths log-uniform 2^6..2^12
+    (work items of the packed kernel in the persistent and per-size modes)
+    and 64 of 2^13..2^16 (the convolution engine, a branch of the graph);
+    N(0,1) signals and filters, seed 4.  Bytes counted: 16 per transform
+    element, 4 per signal, filter and output float."""
+    import ctypes
+
+    import numpy as np
+
+    from estl_gb300._lib import check, lib
+    rng = np.random.default_rng(4)
+    shapes = []
+    for lg in list(rng.integers(6, 13, 4032)) + list(rng.integers(13, 17, 64)):
+        total = int(rng.integers((1 << (lg - 1)) + 1, (1 << lg) + 1))
+        K = int(rng.integers(1, max(2, total // 4)))
+        shapes.append((total - K + 1, K))
+    reqs = np.zeros((len(shapes), 5), np.int64)
+    so = fo = oo = 0
+    for i, (L_, K_) in enumerate(shapes):
+        reqs[i] = (L_, K_, so, fo, oo)
+        so, fo, oo = so + L_, fo + K_, oo + L_ + K_ - 1
+    g = torch.Generator(device="cuda").manual_seed(4)
+    sig = torch.randn(so, device="cuda", generator=g)
+    filt = torch.randn(fo, device="cuda", generator=g)
+    cout = torch.empty(oo, device="cuda")
+    conv_bytes = 4 * (so + fo + oo)
+    tf_bytes = 16 * int(sizes.sum())
+    Lb = lib()
+    res = {"workload": "the 8192 transforms + 4096 real FFT convolutions (padded 2^6..2^12, 64 of 2^13..2^16), "
+                       "N(0,1) seed 4",
+           "convolutions": len(shapes), "bytes_counted": tf_bytes + conv_bytes}
+    st = torch.cuda.current_stream().cuda_stream
+    args = lambda: (ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),  # noqa: E731
+                    ctypes.c_void_p(sig.data_ptr()), ctypes.c_void_p(filt.data_ptr()),
+                    ctypes.c_void_p(cout.data_ptr()), ctypes.c_void_p(st))
+    for mode, name in ((0, "persistent"), (1, "per_size"), (2, "bucketed")):
+        plan = ctypes.c_void_p()
+        check(Lb.estl_packed_mixed_plan_create(offsets.ctypes.data, sizes.ctypes.data, len(sizes), -1,
+                                               reqs.ctypes.data, len(reqs), 0, mode, ctypes.byref(plan)))
+        for _ in range(3):
+            check(Lb.estl_packed_mixed_execute(plan, *args()))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            check(Lb.estl_packed_mixed_execute(plan, *args()))
+        e1.record()
+        torch.cuda.synchronize()
+        check(Lb.estl_packed_check(plan))
+        ms = e0.elapsed_time(e1) / 10
+        buf = ctypes.create_string_buffer(8192)
+        check(Lb.estl_packed_plan_describe(plan, buf, len(buf)))
+        d = json.loads(buf.value.decode())
+        res[name] = {"ms": round(ms, 4), "gbs": round((tf_bytes + conv_bytes) / (ms * 1e-3) / 1e9, 1),
+                     "launches": d["launches"], "conv_items": d["conv_items"], "conv_engine": d["conv_engine"]}
+        Lb.estl_packed_plan_destroy(plan)
+    # accuracy: every 64th convolution against numpy's FP64 FFT convolution
+    s_h, f_h, o_h = sig.cpu().numpy(), filt.cpu().numpy(), cout.cpu().numpy()
+    worst = 0.0
+    for L_, K_, so_, fo_, oo_ in reqs[::64]:
+        nfft = 1 << int(L_ + K_ - 2).bit_length()
+        ref = np.fft.irfft(np.fft.rfft(s_h[so_:so_ + L_].astype(np.float64), nfft) *
+                           np.fft.rfft(f_h[fo_:fo_ + K_].astype(np.float64), nfft), nfft)[:L_ + K_ - 1]
+        got = o_h[oo_:oo_ + L_ + K_ - 1].astype(np.float64)
+        worst = max(worst, float(np.sqrt(np.sum((got - ref) ** 2) / np.sum(ref ** 2))))
+    res["rel_l2_max_sampled"] = worst
+    res["persistent_vs_bucketed"] = round(res["bucketed"]["ms"] / res["persistent"]["ms"], 3)
     return res
 
 

@@ -256,25 +256,60 @@ class PackedPlan:
     [2, 2^18]) at complex-element offset offsets[i] of both the input and the
     output buffer, transforms not overlapping.  mode "persistent": one launch
     whose CTAs take work items from a device queue; "per_size": one launch per
-    size class.  The reference has one FFT object per size (tests/Test.cpp:45-60)."""
+    size class; "bucketed": the engine's own plan per length.  The reference
+    has one FFT object per size (tests/Test.cpp:45-60).
+
+    convolutions: optional (n, 5) integers per FFT convolution -- signal
+    length, filter length, and the signal, filter and output offsets in
+    floats (estl_conv_request) -- run in the same plan (a mixed batch,
+    estl_packed_mixed_plan_create) with conv_flags (CONV_CORRELATE,
+    CONV_REFERENCE_COMPAT, ...); offsets / sizes may then be empty.  A mixed
+    plan runs through execute_mixed."""
 
     MODES = {"persistent": 0, "per_size": 1, "bucketed": 2}
 
-    def __init__(self, offsets, sizes, direction=FORWARD, mode="persistent"):
+    def __init__(self, offsets, sizes, direction=FORWARD, mode="persistent", convolutions=None, conv_flags=0):
         import numpy as np
         self._offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         self._sizes = np.ascontiguousarray(sizes, dtype=np.int64)
-        if self._offsets.ndim != 1 or self._offsets.shape != self._sizes.shape or self._sizes.size == 0:
+        mixed = convolutions is not None
+        if self._offsets.ndim != 1 or self._offsets.shape != self._sizes.shape or (
+                self._sizes.size == 0 and not mixed):
             raise EstlError(1, "offsets and sizes must be 1-D arrays of one non-zero length")
         if mode not in self.MODES:
             raise EstlError(1, f"mode must be one of {sorted(self.MODES)}")
+        if mixed:
+            self._convs = np.ascontiguousarray(convolutions, dtype=np.int64).reshape(-1, 5)
         _ensure_init()
         self.direction = int(direction)
-        self.extent = int((self._offsets + self._sizes).max())
+        self.extent = int((self._offsets + self._sizes).max()) if self._sizes.size else 0
         h = ctypes.c_void_p()
-        check(lib().estl_packed_plan_create(self._offsets.ctypes.data, self._sizes.ctypes.data, self._sizes.size,
-                                            self.direction, self.MODES[mode], ctypes.byref(h)))
+        if mixed:
+            check(lib().estl_packed_mixed_plan_create(self._offsets.ctypes.data, self._sizes.ctypes.data,
+                                                      self._sizes.size, self.direction, self._convs.ctypes.data,
+                                                      len(self._convs), int(conv_flags), self.MODES[mode],
+                                                      ctypes.byref(h)))
+        else:
+            check(lib().estl_packed_plan_create(self._offsets.ctypes.data, self._sizes.ctypes.data, self._sizes.size,
+                                                self.direction, self.MODES[mode], ctypes.byref(h)))
         self._h = h
+
+    def execute_mixed(self, x, out, signals, filters, conv_out, stream=None):
+        """A mixed batch: x / out as execute (None when there are no
+        transforms); signals, filters, conv_out: contiguous float32 CUDA
+        tensors holding the convolutions' offsets."""
+        import torch
+        for name, t in (("signals", signals), ("filters", filters), ("conv_out", conv_out)):
+            if t is not None and (t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous()):
+                raise EstlError(1, f"{name} must be a contiguous float32 CUDA tensor")
+        for name, t in (("x", x), ("out", out)):
+            if t is not None and (t.dtype != torch.complex64 or not t.is_cuda or not t.is_contiguous()
+                                  or t.numel() < self.extent):
+                raise EstlError(1, f"{name} must be a contiguous complex64 CUDA tensor of >= {self.extent} elements")
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr() if t is not None else None)  # noqa: E731
+        check(lib().estl_packed_mixed_execute(self._h, ptr(x), ptr(out), ptr(signals), ptr(filters), ptr(conv_out),
+                                              ctypes.c_void_p(_stream_handle(stream))))
+        return out, conv_out
 
     def execute(self, x, out=None, stream=None):
         """x: contiguous complex64 CUDA tensor of at least `extent` elements;

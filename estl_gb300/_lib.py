@@ -95,6 +95,8 @@ SIGNATURES = {
     "estl_packed_plan_describe": (_INT, [_P, ctypes.c_char_p, _SZ]),
     "estl_packed_plan_destroy": (_INT, [_P]),
     "estl_execute_packed": (_INT, [_P, _P, _I64, _INT, _P, _P, _P]),
+    "estl_packed_mixed_plan_create": (_INT, [_P, _P, _I64, _INT, _P, _I64, _INT, _INT, ctypes.POINTER(_P)]),
+    "estl_packed_mixed_execute": (_INT, [_P, _P, _P, _P, _P, _P, _P]),
     "estl_serve_start": (_INT, [_P, ctypes.POINTER(_P)]),
     "estl_serve_submit": (_INT, [_P, _P, ctypes.POINTER(ctypes.c_uint64)]),
     "estl_serve_poll": (_INT, [_P, ctypes.c_uint64, _INT, _P]),

@@ -1,5 +1,6 @@
-// packed.cu — uneven batches (packed transforms of mixed lengths): the
-// persistent work-queue kernel, its CUDA graph, and the C ABI.
+// packed.cu — uneven batches (packed transforms of mixed lengths, and FFT
+// convolutions beside them): the persistent work-queue kernel, its CUDA
+// graph, and the C ABI.
 #include <algorithm>
 #include <climits>
 #include <cstdio>
@@ -8,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "conv_exec.h"
 #include "engine.h"
 #include "packed_core.cuh"
 #include "tuner.h"
@@ -47,7 +49,21 @@ struct estl_packed_plan_s {
   cudaGraphExec_t exec = nullptr;
   const void* g_in = nullptr;
   void* g_out = nullptr;
+  const float* g_sig = nullptr;
+  const float* g_filt = nullptr;
+  float* g_cout = nullptr;
   cudaStream_t cap_stream = nullptr;
+  // mixed batches: convolution items of the packed kernel (device tables) ...
+  long long nconv = 0;
+  PackedConv* convs = nullptr;
+  int* conv_class_list = nullptr;
+  // ... and the convolutions the convolution engine runs, as a graph branch
+  std::vector<ConvReq> conv_engine_reqs;
+  ConvLayout conv_layout;
+  void* conv_ws = nullptr;  // in ws
+  long long conv_sig_elems = 0, conv_filt_elems = 0;
+  cudaStream_t conv_stream = nullptr;
+  cudaEvent_t conv_fork = nullptr, conv_join = nullptr;
   // test hook (estl_packed_plan_set_test_hook)
   int test_skip_kind = -1;
   unsigned long long test_spin_limit = 0;
@@ -78,8 +94,40 @@ static estl_status bucketed_enqueue(estl_packed_plan p, const cf32* in, cf32* ou
   return s;
 }
 
-static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out, cudaStream_t st) {
-  if (p->bucketed) return bucketed_enqueue(p, in, out, st);
+struct ConvIO {
+  const float* sig;
+  const float* filt;
+  float* out;
+};
+
+static estl_status transforms_enqueue(estl_packed_plan p, const cf32* in, cf32* out, const ConvIO& cio,
+                                      cudaStream_t st);
+
+// The whole batch on `st`: the convolution engine's launches (if any) on a
+// branch forked from and joined back into `st`, beside the transforms.
+static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out, const ConvIO& cio,
+                                  cudaStream_t st) {
+  const bool branch = !p->conv_engine_reqs.empty();
+  estl_status s = ESTL_OK;
+  if (branch) {
+    s = check_cuda(cudaEventRecord(p->conv_fork, st), "cudaEventRecord(fork)");
+    if (s == ESTL_OK) s = check_cuda(cudaStreamWaitEvent(p->conv_stream, p->conv_fork, 0), "cudaStreamWaitEvent(fork)");
+    if (s == ESTL_OK) {
+      ConvBuffers b = conv_buffers(p->conv_layout, p->conv_ws, cio.sig, p->conv_sig_elems, cio.filt,
+                                   p->conv_filt_elems, cio.out);
+      s = launch_conv(p->conv_layout, b, 3, p->conv_stream);
+    }
+    if (s == ESTL_OK) s = check_cuda(cudaEventRecord(p->conv_join, p->conv_stream), "cudaEventRecord(join)");
+    if (s != ESTL_OK) return s;
+  }
+  s = p->bucketed ? bucketed_enqueue(p, in, out, st) : transforms_enqueue(p, in, out, cio, st);
+  if (s == ESTL_OK && branch) s = check_cuda(cudaStreamWaitEvent(st, p->conv_join, 0), "cudaStreamWaitEvent(join)");
+  return s;
+}
+
+static estl_status transforms_enqueue(estl_packed_plan p, const cf32* in, cf32* out, const ConvIO& cio,
+                                      cudaStream_t st) {
+  if (p->layout.launch_begin.empty()) return ESTL_OK;  // every convolution runs on the engine
   Engine& E = engine();
   const PackedLayout& L = p->layout;
   estl_status s = check_cuda(cudaMemsetAsync(p->counters, 0, p->counter_bytes, st), "cudaMemsetAsync(counters)");
@@ -104,6 +152,11 @@ static estl_status packed_enqueue(estl_packed_plan p, const cf32* in, cf32* out,
     a.persistent = L.persistent ? 1 : 0;
     a.skip_kind = p->test_skip_kind;
     a.spin_limit = p->test_spin_limit ? p->test_spin_limit : kPackedSpinLimit;
+    a.convs = Ptr<const PackedConv>{p->convs, (long long)L.convs.size()};
+    a.conv_class_list = Ptr<const int>{p->conv_class_list, (long long)L.conv_class_list.size()};
+    a.csig = Ptr<const float>{cio.sig, L.conv_sig_elems};
+    a.cfilt = Ptr<const float>{cio.filt, L.conv_filt_elems};
+    a.cout = Ptr<float>{cio.out, L.conv_out_elems};
     const long long grid = L.persistent ? std::min<long long>(p->grid, L.launch_count[k]) : L.launch_count[k];
     if (grid < 1 || grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "packed grid of %lld CTAs", grid);
     packed_kernel<<<(unsigned)grid, kPackedThreads, p->smem, st>>>(a);
@@ -122,14 +175,18 @@ static void packed_release(estl_packed_plan p) {
     if (s) cudaStreamDestroy(s);
   for (cudaEvent_t e : p->b_events)
     if (e) cudaEventDestroy(e);
+  if (p->conv_stream) cudaStreamDestroy(p->conv_stream);
+  if (p->conv_fork) cudaEventDestroy(p->conv_fork);
+  if (p->conv_join) cudaEventDestroy(p->conv_join);
   dev_free(p->ws, p->ws_bytes);
   delete p;
 }
 
-extern "C" {
+static_assert(sizeof(estl_conv_request) == sizeof(ConvReq), "request layout");
 
-estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
-                                    int mode, estl_packed_plan* plan) {
+// Plan of a mixed batch (nconv = 0: transforms only).
+static estl_status packed_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                 const ConvReq* reqs, int64_t nconv, int conv_flags, int mode, estl_packed_plan* plan) {
   if (!plan) return fail(ESTL_INVALID_ARG, "NULL plan pointer");
   *plan = nullptr;
   estl_status s = require_init();
@@ -139,18 +196,62 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
     return fail(ESTL_INVALID_ARG, "bad mode %d", mode);
   std::unique_ptr<estl_packed_plan_s> p(new estl_packed_plan_s);
   std::string err;
+  // every request is validated by the layout, which also splits the
+  // convolutions into work items and engine requests
+  PackedLayout L;
+  if (!build_packed_layout(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
+                           count, mode == ESTL_PACKED_PERSISTENT, &L, &err, reqs, nconv, conv_flags))
+    return fail(ESTL_INVALID_ARG, "%s", err.c_str());
+  p->direction = direction;
+  p->nconv = nconv;
+  // bucketed: every convolution runs the convolution engine's own launches
+  if (mode == ESTL_PACKED_BUCKETED)
+    p->conv_engine_reqs.assign(reqs, reqs + nconv);
+  else
+    p->conv_engine_reqs = L.conv_engine;
+  if (!p->conv_engine_reqs.empty()) {
+    if (p->conv_engine_reqs.size() > (size_t)INT_MAX) return fail(ESTL_INVALID_ARG, "too many convolutions");
+    if (!build_conv_layout(p->conv_engine_reqs.data(), (int)p->conv_engine_reqs.size(), conv_flags, &p->conv_layout,
+                           &err))
+      return fail(ESTL_UNSUPPORTED_SIZE, "%s", err.c_str());
+    conv_extents(p->conv_engine_reqs.data(), (int)p->conv_engine_reqs.size(), &p->conv_sig_elems,
+                 &p->conv_filt_elems);
+  }
+  // the convolution engine's part of the workspace: its rows, spectra, scratch
+  auto conv_region = [&](size_t& off) {
+    const size_t o = off;
+    if (!p->conv_engine_reqs.empty()) off = up256(off + p->conv_layout.workspace_bytes);
+    return o;
+  };
+  auto conv_setup = [&](char* w, size_t o_conv) -> estl_status {
+    if (p->conv_engine_reqs.empty()) return ESTL_OK;
+    p->conv_ws = w + o_conv;
+    char* cw = static_cast<char*>(p->conv_ws);
+    const ConvLayout& C = p->conv_layout;
+    estl_status r = check_cuda(cudaMemcpy(cw + C.off_filt_rows, C.filt_rows.data(), C.filt_rows.size() * sizeof(ConvRow),
+                                          cudaMemcpyHostToDevice),
+                               "cudaMemcpy(convolution rows)");
+    if (r == ESTL_OK)
+      r = check_cuda(cudaMemcpy(cw + C.off_sig_rows, C.sig_rows.data(), C.sig_rows.size() * sizeof(ConvRow),
+                                cudaMemcpyHostToDevice),
+                     "cudaMemcpy(convolution rows)");
+    if (r == ESTL_OK) r = check_cuda(cudaStreamCreateWithFlags(&p->conv_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (r == ESTL_OK) r = check_cuda(cudaEventCreateWithFlags(&p->conv_fork, cudaEventDisableTiming), "cudaEventCreate");
+    if (r == ESTL_OK) r = check_cuda(cudaEventCreateWithFlags(&p->conv_join, cudaEventDisableTiming), "cudaEventCreate");
+    return r;
+  };
   if (mode == ESTL_PACKED_BUCKETED) {
     auto choose = [](long long n, long long c) {
       PlanChoice ch;
       tuner_lookup(n, c, &ch);
       return ch;
     };
-    if (!build_packed_buckets(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
+    if (count > 0 &&
+        !build_packed_buckets(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
                               count, +choose, &p->buckets, &p->b_total, &err))
       return fail(ESTL_INVALID_ARG, "%s", err.c_str());
     p->bucketed = true;
-    p->direction = direction;
-    // workspace: per bucket its offsets, then its scratch
+    // workspace: per bucket its offsets, then its scratch; then the convolution engine's
     size_t off = 0;
     std::vector<size_t> o_x, o_s;
     for (const PackedBucket& b : p->buckets) {
@@ -159,6 +260,7 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
       o_s.push_back(off);
       off = up256(off + (size_t)b.plan.scratch_elems * sizeof(cf32));
     }
+    const size_t o_conv = conv_region(off);
     p->ws_bytes = std::max<size_t>(off, 256);
     s = dev_alloc(&p->ws, p->ws_bytes, "bucketed packed plan workspace");
     if (s != ESTL_OK) return s;
@@ -179,6 +281,7 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
       s = check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
       p->b_events.push_back(e);
     }
+    if (s == ESTL_OK) s = conv_setup(w, o_conv);
     if (s == ESTL_OK)
       s = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     if (s != ESTL_OK) {
@@ -188,30 +291,33 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
     *plan = p.release();
     return ESTL_OK;
   }
-  if (!build_packed_layout(reinterpret_cast<const long long*>(offsets), reinterpret_cast<const long long*>(sizes),
-                           count, mode == ESTL_PACKED_PERSISTENT, &p->layout, &err))
-    return fail(ESTL_INVALID_ARG, "%s", err.c_str());
-  p->direction = direction;
-  const PackedLayout& L = p->layout;
-  // workspace: items | class list | offsets | scratch offsets | ncol | counters | error | scratch
+  p->layout = std::move(L);
+  const PackedLayout& PL = p->layout;
+  // workspace: items | class list | offsets | scratch offsets | ncol | counters | error | scratch |
+  //            convolution items | their class list | the convolution engine's
   size_t off = 0;
   const size_t o_items = off;
-  off = up256(off + L.items.size() * sizeof(PackedItem));
+  off = up256(off + std::max<size_t>(PL.items.size(), 1) * sizeof(PackedItem));
   const size_t o_cls = off;
-  off = up256(off + std::max<size_t>(L.class_list.size(), 1) * sizeof(int));
+  off = up256(off + std::max<size_t>(PL.class_list.size(), 1) * sizeof(int));
   const size_t o_off = off;
-  off = up256(off + L.offsets.size() * sizeof(long long));
+  off = up256(off + PL.offsets.size() * sizeof(long long));
   const size_t o_soff = off;
-  off = up256(off + L.scratch_off.size() * sizeof(long long));
+  off = up256(off + PL.scratch_off.size() * sizeof(long long));
   const size_t o_ncol = off;
-  off = up256(off + L.ncol.size() * sizeof(int));
+  off = up256(off + PL.ncol.size() * sizeof(int));
   const size_t o_cnt = off;
-  p->counter_bytes = (1 + L.offsets.size()) * sizeof(unsigned int);
+  p->counter_bytes = (1 + PL.offsets.size()) * sizeof(unsigned int);
   off = up256(off + p->counter_bytes);
   const size_t o_err = off;
   off = up256(off + sizeof(int));
   const size_t o_scr = off;
-  off = up256(off + (size_t)L.scratch_elems * sizeof(cf32));
+  off = up256(off + (size_t)PL.scratch_elems * sizeof(cf32));
+  const size_t o_convs = off;
+  off = up256(off + PL.convs.size() * sizeof(PackedConv));
+  const size_t o_ccls = off;
+  off = up256(off + PL.conv_class_list.size() * sizeof(int));
+  const size_t o_conv = conv_region(off);
   p->ws_bytes = off;
   s = dev_alloc(&p->ws, p->ws_bytes, "packed plan workspace");
   if (s != ESTL_OK) return s;
@@ -224,15 +330,19 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
   p->counters = reinterpret_cast<unsigned int*>(w + o_cnt);
   p->error = reinterpret_cast<int*>(w + o_err);
   p->scratch = reinterpret_cast<cf32*>(w + o_scr);
+  p->convs = reinterpret_cast<PackedConv*>(w + o_convs);
+  p->conv_class_list = reinterpret_cast<int*>(w + o_ccls);
   struct Up {
     void* dst;
     const void* src;
     size_t bytes;
-  } ups[] = {{p->items, L.items.data(), L.items.size() * sizeof(PackedItem)},
-             {p->class_list, L.class_list.data(), L.class_list.size() * sizeof(int)},
-             {p->offsets, L.offsets.data(), L.offsets.size() * sizeof(long long)},
-             {p->scratch_off, L.scratch_off.data(), L.scratch_off.size() * sizeof(long long)},
-             {p->ncol, L.ncol.data(), L.ncol.size() * sizeof(int)}};
+  } ups[] = {{p->items, PL.items.data(), PL.items.size() * sizeof(PackedItem)},
+             {p->class_list, PL.class_list.data(), PL.class_list.size() * sizeof(int)},
+             {p->offsets, PL.offsets.data(), PL.offsets.size() * sizeof(long long)},
+             {p->scratch_off, PL.scratch_off.data(), PL.scratch_off.size() * sizeof(long long)},
+             {p->ncol, PL.ncol.data(), PL.ncol.size() * sizeof(int)},
+             {p->convs, PL.convs.data(), PL.convs.size() * sizeof(PackedConv)},
+             {p->conv_class_list, PL.conv_class_list.data(), PL.conv_class_list.size() * sizeof(int)}};
   for (const Up& u : ups) {
     if (!u.bytes) continue;
     s = check_cuda(cudaMemcpy(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice), "cudaMemcpy(packed tables)");
@@ -249,6 +359,7 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
   if (s == ESTL_OK)
     s = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, packed_kernel, kPackedThreads, p->smem),
                    "occupancy");
+  if (s == ESTL_OK) s = conv_setup(w, o_conv);
   if (s == ESTL_OK)
     s = check_cuda(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
   if (s != ESTL_OK) {
@@ -260,22 +371,21 @@ estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes
   return ESTL_OK;
 }
 
-estl_status estl_packed_execute(estl_packed_plan p, const void* d_in, void* d_out, void* stream) {
-  if (!p || !d_in || !d_out) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
-  if (d_in == d_out) return fail(ESTL_INVALID_ARG, "in-place execution is not supported");
-  if (((uintptr_t)d_in & 7) || ((uintptr_t)d_out & 7)) return fail(ESTL_INVALID_ARG, "buffers must be 8-byte aligned");
+// Replays the plan's graph, captured again when a buffer changes.
+static estl_status packed_run(estl_packed_plan p, const void* d_in, void* d_out, const ConvIO& cio, void* stream) {
   estl_status s = require_init();
   if (s != ESTL_OK) return s;
   std::lock_guard<std::mutex> g(p->mu);
-  if (!p->exec || p->g_in != d_in || p->g_out != d_out) {
-    // capture the launch sequence once per (input, output) pair
+  if (!p->exec || p->g_in != d_in || p->g_out != d_out || p->g_sig != cio.sig || p->g_filt != cio.filt ||
+      p->g_cout != cio.out) {
+    // capture the launch sequence once per set of buffers
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     p->exec = nullptr;
     p->graph = nullptr;
     s = check_cuda(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     if (s != ESTL_OK) return s;
-    estl_status s2 = packed_enqueue(p, static_cast<const cf32*>(d_in), static_cast<cf32*>(d_out), p->cap_stream);
+    estl_status s2 = packed_enqueue(p, static_cast<const cf32*>(d_in), static_cast<cf32*>(d_out), cio, p->cap_stream);
     s = check_cuda(cudaStreamEndCapture(p->cap_stream, &p->graph), "cudaStreamEndCapture");
     if (s2 != ESTL_OK) return s2;
     if (s != ESTL_OK) return s;
@@ -283,8 +393,58 @@ estl_status estl_packed_execute(estl_packed_plan p, const void* d_in, void* d_ou
     if (s != ESTL_OK) return s;
     p->g_in = d_in;
     p->g_out = d_out;
+    p->g_sig = cio.sig;
+    p->g_filt = cio.filt;
+    p->g_cout = cio.out;
   }
   return check_cuda(cudaGraphLaunch(p->exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+static bool has_transforms(estl_packed_plan p) {
+  return p->bucketed ? !p->buckets.empty() : !p->layout.offsets.empty();
+}
+
+extern "C" {
+
+estl_status estl_packed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                    int mode, estl_packed_plan* plan) {
+  if (count < 1) {
+    if (plan) *plan = nullptr;
+    return fail(ESTL_INVALID_ARG, "need at least one transform");
+  }
+  return packed_create(offsets, sizes, count, direction, nullptr, 0, 0, mode, plan);
+}
+
+estl_status estl_packed_mixed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                          const estl_conv_request* reqs, int64_t nconv, int conv_flags, int mode,
+                                          estl_packed_plan* plan) {
+  return packed_create(offsets, sizes, count, direction, reinterpret_cast<const ConvReq*>(reqs), nconv, conv_flags,
+                       mode, plan);
+}
+
+estl_status estl_packed_execute(estl_packed_plan p, const void* d_in, void* d_out, void* stream) {
+  if (!p || !d_in || !d_out) return fail(ESTL_INVALID_ARG, "NULL plan or buffer");
+  if (p->nconv) return fail(ESTL_INVALID_ARG, "the plan has convolutions: run it with estl_packed_mixed_execute");
+  if (d_in == d_out) return fail(ESTL_INVALID_ARG, "in-place execution is not supported");
+  if (((uintptr_t)d_in & 7) || ((uintptr_t)d_out & 7)) return fail(ESTL_INVALID_ARG, "buffers must be 8-byte aligned");
+  return packed_run(p, d_in, d_out, ConvIO{nullptr, nullptr, nullptr}, stream);
+}
+
+estl_status estl_packed_mixed_execute(estl_packed_plan p, const void* d_in, void* d_out, const float* d_signals,
+                                      const float* d_filters, float* d_conv_out, void* stream) {
+  if (!p) return fail(ESTL_INVALID_ARG, "NULL plan");
+  if (has_transforms(p)) {
+    if (!d_in || !d_out) return fail(ESTL_INVALID_ARG, "NULL transform buffer");
+    if (d_in == d_out) return fail(ESTL_INVALID_ARG, "in-place execution is not supported");
+    if (((uintptr_t)d_in & 7) || ((uintptr_t)d_out & 7))
+      return fail(ESTL_INVALID_ARG, "transform buffers must be 8-byte aligned");
+  }
+  if (p->nconv) {
+    if (!d_signals || !d_filters || !d_conv_out) return fail(ESTL_INVALID_ARG, "NULL convolution buffer");
+    if (((uintptr_t)d_signals | (uintptr_t)d_filters | (uintptr_t)d_conv_out) & 3)
+      return fail(ESTL_INVALID_ARG, "signal, filter and output buffers must be 4-byte aligned");
+  }
+  return packed_run(p, d_in, d_out, ConvIO{d_signals, d_filters, d_conv_out}, stream);
 }
 
 estl_status estl_packed_check(estl_packed_plan p) {
@@ -336,20 +496,27 @@ estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len)
     }
     size_t ntf = 0;
     for (const PackedBucket& b : p->buckets) ntf += b.xoff.size();
-    char tail[256];
-    std::snprintf(tail, sizeof tail, "], \"transforms\": %zu, \"launches\": %lld, \"elements\": %lld, \"flops\": %.6g}",
-                  ntf, launches, elems, flops);
+    char tail[384];
+    std::snprintf(tail, sizeof tail,
+                  "], \"transforms\": %zu, \"launches\": %lld, \"elements\": %lld, \"flops\": %.6g, "
+                  "\"convolutions\": %lld, \"conv_items\": 0, \"conv_engine\": %zu, \"conv_launches\": %zu}",
+                  ntf, launches + (long long)p->conv_layout.launches.size(), elems, flops, p->nconv,
+                  p->conv_engine_reqs.size(), p->conv_layout.launches.size());
     d += tail;
     if (d.size() + 1 > len) return fail(ESTL_INVALID_ARG, "describe buffer of %zu bytes is too small", len);
     std::snprintf(buf, len, "%s", d.c_str());
     return ESTL_OK;
   }
   const PackedLayout& L = p->layout;
-  std::snprintf(buf, len,
-                "{\"transforms\": %zu, \"items\": %zu, \"launches\": %zu, \"persistent\": %s, \"grid\": %d, "
-                "\"elements\": %lld, \"flops\": %.6g, \"scratch_bytes\": %lld, \"smem_bytes\": %zu}",
-                L.offsets.size(), L.items.size(), L.launch_begin.size(), L.persistent ? "true" : "false",
-                L.persistent ? p->grid : 0, L.elements, L.flops, L.scratch_elems * 8, p->smem);
+  const int n = std::snprintf(
+      buf, len,
+      "{\"transforms\": %zu, \"items\": %zu, \"launches\": %zu, \"persistent\": %s, \"grid\": %d, "
+      "\"elements\": %lld, \"flops\": %.6g, \"scratch_bytes\": %lld, \"smem_bytes\": %zu, \"convolutions\": %lld, "
+      "\"conv_items\": %zu, \"conv_engine\": %zu, \"conv_launches\": %zu, \"conv_flops\": %.6g}",
+      L.offsets.size(), L.items.size(), L.launch_begin.size() + p->conv_layout.launches.size(),
+      L.persistent ? "true" : "false", L.persistent ? p->grid : 0, L.elements, L.flops, L.scratch_elems * 8, p->smem,
+      p->nconv, L.convs.size(), p->conv_engine_reqs.size(), p->conv_layout.launches.size(), L.conv_flops);
+  if (n < 0 || (size_t)n >= len) return fail(ESTL_INVALID_ARG, "describe buffer of %zu bytes is too small", len);
   return ESTL_OK;
 }
 

@@ -71,14 +71,17 @@ struct PackedConvTile {
     const int t = tid & (TL::T - 1);
     const int c = tid >> TL::LOGT;
     const bool valid = c < it.blk;
-    PackedConv r{};
-    if (valid) r = a.convs[a.conv_class_list[(long long)it.tf + c]];
+    // the request's descriptor is read where it is used (here, then at the
+    // store) rather than held in registers across the transforms
+    const long long ri = valid ? a.conv_class_list[(long long)it.tf + c] : 0;
     const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
     const Ptr<cf32> sm{smraw, SMEM_ELEMS};
     const Sidx sidx{};
     cf32 v[TL::E];
     float ex = 0.f, eh = 0.f;
     {
+      PackedConv r{};
+      if (valid) r = a.convs[ri];
       const Ptr<const float> xs = valid ? a.csig.sub(r.sig_off, r.sig_len) : Ptr<const float>{a.csig.p, 0};
       const Ptr<const float> hs = valid ? a.cfilt.sub(r.filt_off, r.filt_len) : Ptr<const float>{a.cfilt.p, 0};
 #pragma unroll
@@ -102,7 +105,7 @@ struct PackedConvTile {
     for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();
     const float h0 = sm[sidx(c, 0)].y;  // Im Z_0 = 2^k * sum of the filter
-    const float cj = r.correlate ? -1.f : 1.f;
+    const float cj = valid && a.convs[ri].correlate ? -1.f : 1.f;
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const cf32 zm = sm[sidx(c, (TL::M - (t + TL::T * j)) & (TL::M - 1))];
@@ -113,6 +116,7 @@ struct PackedConvTile {
     ESTL_SYNC();  // before the passes reuse the exchange buffer
     run_passes<TL, 0>(v, t, c, sm, tw, sidx);
     if (valid) {
+      const PackedConv r = a.convs[ri];
       const Ptr<float> o = a.cout.sub(r.out_off, r.out_len);
       const float g = r.dc_norm ? 1.f / ((float)TL::M * h0) : pow2_f(-k) / (float)TL::M;
 #pragma unroll
@@ -237,8 +241,15 @@ ESTL_HD void packed_row(const PackedArgs& a, const PackedItem& it, int tid, cf32
   K::body(a.scratch.sub(a.scratch_off[it.tf], n), a.out.sub(off, n), it.blk, it.logn, tid, sm, a.bank, a.sgn);
 }
 
+// Convolution items run as separate device functions: inlined beside every
+// transform tile, their register demand made the whole kernel spill.
 template <class K>
-ESTL_HD void packed_conv(const PackedArgs& a, const PackedItem& it, int tid, cf32* sm) {
+#if defined(__CUDA_ARCH__)
+__device__ __noinline__
+#else
+inline
+#endif
+void packed_conv(const PackedArgs& a, const PackedItem& it, int tid, cf32* sm) {
   static_assert(K::NT == kPackedThreads, "packed tiles run with 256 threads");
   K::body(a, it, tid, sm);
 }

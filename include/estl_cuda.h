@@ -386,6 +386,33 @@ estl_status estl_packed_plan_describe(estl_packed_plan plan, char* buf, size_t l
  * skip_column_items = 0, spin_limit = 0 restores normal executes. */
 estl_status estl_packed_plan_set_test_hook(estl_packed_plan plan, int skip_column_items, uint64_t spin_limit);
 estl_status estl_packed_plan_destroy(estl_packed_plan plan);
+
+/* Mixed uneven batches: the count transforms above (count may be 0) and
+ * nconv FFT convolutions (estl_conv_request, offsets in floats into the
+ * caller's signal / filter / output arrays; conv_flags: ESTL_CONV_CORRELATE,
+ * ESTL_CONV_REFERENCE_COMPAT, ESTL_CONV_NO_PAIRING, ESTL_CONV_COMPLEX; FP32)
+ * in one plan, one graph.  The semantics per request are estl_conv_execute's
+ * (Convolution.h:95-154 in 1D).
+ * ESTL_PACKED_PERSISTENT / PER_SIZE: a convolution of padded length <= 2^12
+ *   is a work item of the packed kernel (with the transforms in the one
+ *   persistent launch, or one launch per padded length): one CTA computes
+ *   the request whole -- signal and filter as the real and imaginary parts of
+ *   one complex transform, their spectra separated with X_{n-k}, product,
+ *   inverse transform -- reading the signal and the filter once and writing
+ *   the output once.  Longer convolutions run the convolution engine's
+ *   launches on a branch of the same graph.
+ * ESTL_PACKED_BUCKETED: every convolution runs the convolution engine's own
+ *   launches (grouped by padded length, two requests per transform, the
+ *   real-input four-step above 2^14) on a branch beside the buckets.
+ * The plan's graph is captured again when a buffer changes. */
+estl_status estl_packed_mixed_plan_create(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,
+                                          const estl_conv_request* reqs, int64_t nconv, int conv_flags, int mode,
+                                          estl_packed_plan* plan);
+/* d_in / d_out: the transforms' buffers (may be NULL when count is 0);
+ * d_signals, d_filters, d_conv_out: the convolutions' float arrays (4-byte
+ * aligned).  A plan with convolutions runs only through this call. */
+estl_status estl_packed_mixed_execute(estl_packed_plan plan, const void* d_in, void* d_out, const float* d_signals,
+                                      const float* d_filters, float* d_conv_out, void* stream);
 /* One blocking call for a batch used once: plan (persistent mode), execute on
  * `stream`, wait, check, release. */
 estl_status estl_execute_packed(const int64_t* offsets, const int64_t* sizes, int64_t count, int direction,

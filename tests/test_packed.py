@@ -344,10 +344,22 @@ def conv_reference(s, f, flags):
 
 
 def check_convs(reqs, sig, filt, cout, flags):
+    """rel-L2 per request; in reference-compatible mode relative to the whole
+    circular result (the FP32 transforms' rounding is relative to it, and
+    the L kept samples of a correlation can be its small tail)."""
     for i, (L, K, so, fo, oo) in enumerate(reqs):
-        ref = conv_reference(sig[so:so + L], filt[fo:fo + K], flags)
+        s, f = sig[so:so + L], filt[fo:fo + K]
+        ref = conv_reference(s, f, flags)
         got = cout[oo:oo + len(ref)]
-        assert conv_rel(got, ref) < CONV_TOL, (i, L, K, conv_rel(got, ref))
+        if flags & 2:
+            n = 2
+            while n < L + K - 1:
+                n *= 2
+            full = oracle.conv_circular(s, f, n, bool(flags & 1)) / np.sum(f.astype(np.float64))
+            err = float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(full))
+        else:
+            err = conv_rel(got, ref)
+        assert err < CONV_TOL, (i, L, K, err)
         assert np.isnan(cout[oo + len(ref)]), (i, "wrote past its output")
 
 
@@ -408,3 +420,74 @@ def test_emulated_mixed_validation(emu):
     reqs, sig, filt, olen = make_convs([(10, 3)], 1)
     rc, msg, _, _ = emu_mixed(emu, offsets, sizes, x, 1, -1, reqs, sig, filt, olen, 1 << 8)
     assert rc == 2 and "FP32" in msg
+
+
+def random_conv_shapes(count, seed, max_log=12, engine=()):
+    """(L, K) pairs whose padded lengths cover 2^1..2^max_log, plus the given
+    longer ones (run by the convolution engine)."""
+    rng = np.random.default_rng(seed)
+    shapes = []
+    for _ in range(count):
+        lg = int(rng.integers(1, max_log + 1))
+        total = int(rng.integers((1 << (lg - 1)) + 1, (1 << lg) + 1)) if lg > 1 else 1
+        K = int(rng.integers(1, total + 1))
+        shapes.append((total - K + 1, K))
+    return shapes + list(engine)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,flags", [(0, 0), (0, 3), (1, 1), (1, 2), (2, 0), (2, 3)])
+def test_gpu_mixed_transforms_and_convolutions(engine, mode, flags):
+    """A mixed batch on the GPU (estl_packed_mixed_plan_create / _execute):
+    300 transforms of 2^1..2^16 against oracle.fft and 404 convolutions
+    (padded 2^1..2^12 as work items, 2^13..2^17 on the convolution engine)
+    against oracle.conv_fft / oracle.conv_compat, every request checked, in
+    each execution mode; the gaps between outputs stay untouched; a second
+    execute replays the captured graph."""
+    import torch
+    offsets, sizes, x = make_batch(300, 1, 16, 81 + mode, gap=1)
+    shapes = random_conv_shapes(400, 82 + flags, engine=[(5000, 300), (9000, 3000), (30000, 700), (100000, 31)])
+    reqs, sig, filt, olen = make_convs(shapes, 83, flags)
+    p = engine.PackedPlan(offsets, sizes, -1, ["persistent", "per_size", "bucketed"][mode], convolutions=reqs,
+                          conv_flags=flags)
+    d = p.describe()
+    assert d["convolutions"] == len(reqs)
+    if mode != 2:
+        assert d["conv_items"] == len(reqs) - 4 and d["conv_engine"] == 4
+    xd = torch.from_numpy(x).cuda()
+    sd, fd = torch.from_numpy(sig).cuda(), torch.from_numpy(filt).cuda()
+    for rep in range(2):
+        yd = torch.full_like(xd, float("nan"))
+        cd = torch.full((olen,), float("nan"), dtype=torch.float32, device="cuda")
+        p.execute_mixed(xd, yd, sd, fd, cd)
+        p.check()
+    y, cout = yd.cpu().numpy(), cd.cpu().numpy()
+    check_against_oracle(offsets, sizes, x, y, -1)
+    check_convs(reqs, sig, filt, cout, flags)
+    mask = np.ones(len(x), bool)
+    for o, n in zip(offsets, sizes):
+        mask[o:o + n] = False
+    assert np.all(np.isnan(y[mask].real))
+    p.close()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_convolutions_only_and_errors(engine):
+    """A plan of convolutions alone (no transform buffers), its describe, and
+    the refusals: a mixed plan through estl_packed_execute, NULL convolution
+    buffers, split precision."""
+    import torch
+    reqs, sig, filt, olen = make_convs(random_conv_shapes(50, 91), 92)
+    p = engine.PackedPlan([], [], -1, "persistent", convolutions=reqs)
+    sd, fd = torch.from_numpy(sig).cuda(), torch.from_numpy(filt).cuda()
+    cd = torch.full((olen,), float("nan"), dtype=torch.float32, device="cuda")
+    p.execute_mixed(None, None, sd, fd, cd)
+    p.check()
+    check_convs(reqs, sig, filt, cd.cpu().numpy(), 0)
+    with pytest.raises(engine.EstlError):
+        p.execute(torch.zeros(4, dtype=torch.complex64, device="cuda"))
+    with pytest.raises(engine.EstlError):
+        p.execute_mixed(None, None, sd, fd, None)
+    p.close()
+    with pytest.raises(engine.EstlError):
+        engine.PackedPlan([], [], -1, "persistent", convolutions=reqs, conv_flags=1 << 8)
