@@ -856,10 +856,11 @@ def bench_bluestein(estl, torch):
     C2C FP32 forward, about 2^26 elements per size, uniform[-1,1) seed 7;
     rel-L2 of the first transforms against numpy's FP64 FFT."""
     import numpy as np
-    out = {"workload": "C2C FP32 forward, N in {1000, 12288, 1000000}, batch = 2^26 // N, uniform[-1,1) seed 7",
+    out = {"workload": "C2C FP32 forward, N in {1000, 3000, 6000, 12288, 1000000}, batch = 2^26 // N, "
+                       "uniform[-1,1) seed 7",
            "bytes_counted": "16 B per element (compulsory read + write)"}
     st = torch.cuda.Stream()
-    for n in (1000, 12288, 1000000):
+    for n in (1000, 3000, 6000, 12288, 1000000):
         batch = (1 << 26) // n
         g = torch.Generator(device="cuda").manual_seed(7)
         x = torch.view_as_complex((torch.rand((n * batch, 2), device="cuda", generator=g) * 2 - 1).contiguous())
@@ -878,7 +879,8 @@ def bench_bluestein(estl, torch):
         rows = max(1, min(batch, (1 << 21) // n))
         x0 = x[: rows * n].view(rows, n).cpu().numpy().astype(np.complex128)
         err = float(rel_l2_rows(y[: rows * n].view(rows, n).cpu().numpy(), np.fft.fft(x0, axis=-1)).max())
-        out[str(n)] = {"batch": batch, "bluestein_m": p.describe()["bluestein_m"], "ms": round(ms, 3),
+        out[str(n)] = {"batch": batch, "bluestein_m": p.describe()["bluestein_m"],
+                       "hbm_passes": p.describe()["hbm_passes"], "ms": round(ms, 3),
                        "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": float(f"{err:.3e}")}
         p.close()
     return out

@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <unordered_map>
 #include <unordered_set>
 #include <vector>
@@ -594,9 +595,78 @@ __global__ void blue_post_kernel(const cf32* __restrict__ c, cf32* __restrict__ 
   }
 }
 
-// Chirp, the kernel spectrum FFT_M(b) / M and the work buffers of a plan.
+}  // extern "C"
+
+// M <= 2^14: the fused one-pass kernel (BlueSingleKernel), one tile shape per
+// M (ESTL_BLUE_TILES).
+template <class K>
+__global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) blue_fused_kernel(BlueArgs a) {
+  extern __shared__ float2 estl_blue_smem[];
+  K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_blue_smem));
+}
+
+namespace {
+struct BlueDesc {
+  int logm, logc, nt, smem_bytes;
+  const void* fn;
+  bool attr_set;
+};
+std::mutex g_blue_mu;
+std::vector<BlueDesc>& blue_table() {
+  static std::vector<BlueDesc> t = [] {
+    std::vector<BlueDesc> v;
+#define ESTL_BLUE_DESC(M, E, R, C)                                                          \
+  v.push_back(BlueDesc{M, C, BlueSingleKernel<M, E, R, C>::NT,                              \
+                       (int)(BlueSingleKernel<M, E, R, C>::SMEM_ELEMS * sizeof(cf32)),      \
+                       reinterpret_cast<const void*>(&blue_fused_kernel<BlueSingleKernel<M, E, R, C>>), false});
+    ESTL_BLUE_TILES(ESTL_BLUE_DESC)
+#undef ESTL_BLUE_DESC
+    return v;
+  }();
+  return t;
+}
+}  // namespace
+
+// `count` transforms through the fused kernel of M = 2^logm.
+static estl_status run_bluestein_fused(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
+  const long long N = p->layout.n, M = p->layout.blue_m;
+  const int logm = ilog2_exact(M);
+  BlueDesc* d = nullptr;
+  for (BlueDesc& b : blue_table())
+    if (b.logm == logm) d = &b;
+  if (!d) return fail(ESTL_UNSUPPORTED_SIZE, "no fused Bluestein kernel for M = 2^%d", logm);
+  if (!d->attr_set) {
+    std::lock_guard<std::mutex> g(g_blue_mu);
+    if (!d->attr_set) {
+      estl_status s = check_cuda(cudaFuncSetAttribute(d->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->smem_bytes),
+                                 "cudaFuncSetAttribute(Bluestein)");
+      if (s != ESTL_OK) return s;
+      d->attr_set = true;
+    }
+  }
+  const long long grid = (count + (1LL << d->logc) - 1) >> d->logc;
+  if (grid < 1 || grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "Bluestein grid of %lld CTAs", grid);
+  BlueArgs a;
+  a.in = Ptr<const cf32>{in, count * N};
+  a.out = Ptr<cf32>{out, count * N};
+  a.chirp = Ptr<const cf32>{p->blue_chirp, N};
+  a.spec = Ptr<const cf32>{p->blue_spec, M};
+  a.bank = Ptr<const cf32>{engine().bank, kBankSize};
+  a.n = N;
+  a.count = count;
+  a.sgn = p->sgn;
+  void* args[] = {&a};
+  return check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3((unsigned)d->nt), args, (size_t)d->smem_bytes, st),
+                    "Bluestein fused kernel");
+}
+
+extern "C" {
+
+// Chirp, the kernel spectrum FFT_M(b) / M and the work buffers of a plan
+// (one M-element buffer for the fused kernel's set-up).
 static estl_status bluestein_setup(estl_plan_s* p) {
-  const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
+  const long long N = p->layout.n, M = p->layout.blue_m;
+  const long long cmax = bluestein_fused(M) ? 1 : p->layout.blue_chunk;
   p->blue_chirp_bytes = (size_t)N * sizeof(cf32);
   p->blue_spec_bytes = (size_t)M * sizeof(cf32);
   p->blue_work_bytes = (size_t)(cmax * M) * sizeof(cf32);
@@ -625,6 +695,7 @@ static estl_status bluestein_setup(estl_plan_s* p) {
 // `count` transforms of a Bluestein plan: pre-multiply, M-point FFT, spectrum
 // multiply, M-point inverse FFT, post-multiply, in chunks of blue_chunk.
 static estl_status run_bluestein(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
+  if (bluestein_fused(p->layout.blue_m)) return run_bluestein_fused(p, count, in, out, st);
   const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
   const int logm = ilog2_exact(M);
   for (long long b0 = 0; b0 < count; b0 += cmax) {

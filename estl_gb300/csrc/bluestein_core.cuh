@@ -65,4 +65,109 @@ ESTL_HD cf32 bluestein_post(const cf32* c, const cf32* chirp, long long k, float
   return conj_if(cmul(c[k], chirp[k]), sgn);
 }
 
+// ---------------------------------------------------------------------------
+// M <= 2^14: the whole algorithm in one tile kernel, C transforms per CTA:
+//   v = a (pre-multiplied input, zero-padded to M)  -> FFT_M
+//   v = conj(v * Bs)                                -> FFT_M  (= conj(c))
+//   X_k = w_k conj(v_k)                             (k < N)
+// One HBM read of the input and one write of the output per transform (the
+// chirp and the kernel spectrum, N + M values shared by every transform,
+// stay in L2), instead of five passes over M-element work buffers.
+// ---------------------------------------------------------------------------
+constexpr int kBlueFusedMaxLog = 14;
+
+// Tile shapes of the fused kernel, one per M (X(log2 M, log2 elements a
+// thread, log2 radix, log2 transforms a CTA)): 256 threads up to 2^12, 512 at
+// 2^13 (radix 16, 148 bytes of register spill a thread) and 2^14 (radix 32,
+// 744 bytes: with two transforms and the chirp and spectrum products a thread
+// holds more than its 128 registers).
+#define ESTL_BLUE_TILES(X) \
+  X(3, 3, 4, 8)            \
+  X(4, 4, 4, 8)            \
+  X(5, 4, 4, 7)            \
+  X(6, 4, 4, 6)            \
+  X(7, 4, 4, 5)            \
+  X(8, 4, 4, 4)            \
+  X(9, 4, 4, 3)            \
+  X(10, 4, 4, 2)           \
+  X(11, 4, 4, 1)           \
+  X(12, 4, 4, 0)           \
+  X(13, 4, 4, 0)           \
+  X(14, 5, 5, 0)
+ESTL_CX bool bluestein_fused(long long m) { return m <= (1LL << kBlueFusedMaxLog); }
+
+// A point the compiler does not move memory accesses across (no instruction).
+ESTL_HD void compiler_order() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("" ::: "memory");
+#endif
+}
+
+struct BlueArgs {
+  Ptr<const cf32> in;     // count transforms of N
+  Ptr<cf32> out;          // count transforms of N
+  Ptr<const cf32> chirp;  // w_n, N values
+  Ptr<const cf32> spec;   // Bs = FFT_M(b) / M, M values
+  Ptr<const cf32> bank;
+  long long n;
+  long long count;
+  float sgn;
+};
+
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct BlueSingleKernel {
+  using K = SingleKernel<LOGM, LOGE, LOGR, LOGC>;
+  using TL = typename K::TL;
+  static constexpr int C = K::C;
+  static constexpr int NT = K::NT;
+  static constexpr int SMEM_ELEMS = K::SMEM_ELEMS;
+  // up to 128 registers a thread: the chirp and spectrum products beside the
+  // tile's elements spill at the plain tiles' 64
+  static constexpr int MIN_BLOCKS = NT <= 256 ? 2 : 1;
+
+  ESTL_HD static void run(const BlueArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const long long f = cta * C + c;
+    const bool valid = f < a.count;
+    const int n = (int)a.n;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, K::EXCH};
+    const typename K::Sidx sidx{};
+    const Ptr<const cf32> x = valid ? a.in.sub(f * a.n, a.n) : Ptr<const cf32>{a.in.p, 0};
+    // The chirp and spectrum factors are loaded in groups of 8 slots with a
+    // compiler ordering point between groups, so that they are not all
+    // hoisted beside the tile's elements.
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int m = t + TL::T * j;
+      v[j] = valid && m < n ? conj_if(ldcs(x, m), a.sgn) : cf32{0.f, 0.f};
+    }
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int m = t + TL::T * j;
+      if (m < n) v[j] = cmul(v[j], ldg(a.chirp, m));
+      if ((j & 7) == 7) compiler_order();
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const cf32 p = cmul(v[j], ldg(a.spec, t + TL::T * j));
+      v[j] = cf32{p.x, -p.y};
+      if ((j & 7) == 7) compiler_order();
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    if (valid) {
+      const Ptr<cf32> y = a.out.sub(f * a.n, a.n);
+#pragma unroll
+      for (int j = 0; j < TL::E; ++j) {
+        const int k = t + TL::T * j;
+        if (k < n) stcs(y, k, conj_if(cmul(cf32{v[j].x, -v[j].y}, ldg(a.chirp, k)), a.sgn));
+        if ((j & 7) == 7) compiler_order();
+      }
+    }
+  }
+};
+
 }  // namespace estl

@@ -464,7 +464,9 @@ bool make_plan_bluestein(long long n, long long batch, Plan1D* out, std::string*
   p.blue_m = m;
   p.blue_chunk = chunk;
   p.scratch_elems = inner.scratch_elems;
-  p.hbm_passes = 2 * inner.hbm_passes + 3;  // pre-multiply, two M-point FFTs, spectrum multiply, post-multiply
+  // M <= 2^14: one fused kernel (bluestein_core.cuh); above: pre-multiply, two
+  // M-point FFTs, spectrum multiply, post-multiply
+  p.hbm_passes = bluestein_fused(m) ? 1 : 2 * inner.hbm_passes + 3;
   *out = p;
   return true;
 }

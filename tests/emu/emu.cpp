@@ -516,6 +516,41 @@ int emu_bluestein_run(long long n, long long batch, int sign, const float* in, f
   for (cf32& v : spec) v = cf32{v.x / (float)M, v.y / (float)M};
   const cf32* x = reinterpret_cast<const cf32*>(in);
   cf32* y = reinterpret_cast<cf32*>(out);
+  if (bluestein_fused(M)) {
+    // the fused one-pass kernel of the GPU path, every transform in one launch
+    BlueArgs a;
+    a.in = Ptr<const cf32>{x, batch * n};
+    a.out = Ptr<cf32>{y, batch * n};
+    a.chirp = Ptr<const cf32>{chirp.data(), n};
+    a.spec = Ptr<const cf32>{spec.data(), M};
+    a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
+    a.n = n;
+    a.count = batch;
+    a.sgn = sgn;
+    bool ok = false, found = false;
+    auto go = [&](auto kernel_tag) {
+      using K = decltype(kernel_tag);
+      if (found || (1LL << K::TL::LM) != M) return;
+      found = true;
+      const long long grid = (batch + K::C - 1) / K::C;
+      ok = run_generic(K::NT, K::SMEM_ELEMS,
+                       [](const BlueArgs& args, long long cta, int tid, cf32* sm) { K::run(args, cta, tid, sm); }, a,
+                       grid);
+    };
+#define ESTL_BLUE_GO(M_, E_, R_, C_) go(BlueSingleKernel<M_, E_, R_, C_>{});
+    ESTL_BLUE_TILES(ESTL_BLUE_GO)
+#undef ESTL_BLUE_GO
+    if (!found) {
+      set_err(err, errlen, "no emulated fused Bluestein kernel");
+      return 3;
+    }
+    if (!ok) {
+      std::lock_guard<std::mutex> gl(g_msg_mu);
+      set_err(err, errlen, g_msg);
+      return 1;
+    }
+    return 0;
+  }
   for (long long b0 = 0; b0 < batch; b0 += p.blue_chunk) {
     const long long c = std::min(p.blue_chunk, batch - b0);
     Plan1D inner;
