@@ -597,44 +597,49 @@ __global__ void blue_post_kernel(const cf32* __restrict__ c, cf32* __restrict__ 
 
 }  // extern "C"
 
-// M <= 2^14: the fused one-pass kernel (BlueSingleKernel), one tile shape per
-// M (ESTL_BLUE_TILES).
+// Bluestein tile kernels (bluestein_core.cuh): the fused one-pass kernel of
+// M <= 2^14 (one tile shape per M, ESTL_BLUE_TILES) and the three four-step
+// kernels of M <= 2^22 (the convolution's tile shapes, conv_list.inc).
 template <class K>
-__global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) blue_fused_kernel(BlueArgs a) {
+__global__ void __launch_bounds__(K::NT, K::MIN_BLOCKS) bluestein_tile_kernel(BlueArgs a) {
   extern __shared__ float2 estl_blue_smem[];
   K::run(a, (long long)blockIdx.x, (int)threadIdx.x, reinterpret_cast<cf32*>(estl_blue_smem));
 }
 
 namespace {
+// kind 0: fused one-pass kernel (logm = log2 M); 1 / 2 / 3: four-step column,
+// middle and output kernels (logm = their tile length)
 struct BlueDesc {
-  int logm, logc, nt, smem_bytes;
+  int kind, logm, logc, nt, smem_bytes;
   const void* fn;
   bool attr_set;
 };
 std::mutex g_blue_mu;
+template <class K>
+BlueDesc blue_desc(int kind, int m, int c) {
+  return BlueDesc{kind, m, c, K::NT, (int)(K::SMEM_ELEMS * sizeof(cf32)),
+                  reinterpret_cast<const void*>(&bluestein_tile_kernel<K>), false};
+}
 std::vector<BlueDesc>& blue_table() {
   static std::vector<BlueDesc> t = [] {
     std::vector<BlueDesc> v;
-#define ESTL_BLUE_DESC(M, E, R, C)                                                          \
-  v.push_back(BlueDesc{M, C, BlueSingleKernel<M, E, R, C>::NT,                              \
-                       (int)(BlueSingleKernel<M, E, R, C>::SMEM_ELEMS * sizeof(cf32)),      \
-                       reinterpret_cast<const void*>(&blue_fused_kernel<BlueSingleKernel<M, E, R, C>>), false});
+#define ESTL_BLUE_DESC(M, E, R, C) v.push_back(blue_desc<BlueSingleKernel<M, E, R, C>>(0, M, C));
     ESTL_BLUE_TILES(ESTL_BLUE_DESC)
 #undef ESTL_BLUE_DESC
+#define ESTL_XC_COL(M, E, R, C) v.push_back(blue_desc<BlueColKernel<M, E, R, C>>(1, M, C));
+#define ESTL_XC_ROW(M, E, R, C) v.push_back(blue_desc<BlueMidKernel<M, E, R, C>>(2, M, C));
+#define ESTL_XC_OUT(M, E, R, C) v.push_back(blue_desc<BlueOutKernel<M, E, R, C>>(3, M, C));
+#include "conv_list.inc"
     return v;
   }();
   return t;
 }
-}  // namespace
 
-// `count` transforms through the fused kernel of M = 2^logm.
-static estl_status run_bluestein_fused(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
-  const long long N = p->layout.n, M = p->layout.blue_m;
-  const int logm = ilog2_exact(M);
+estl_status blue_launch(int kind, int logm, long long units, const BlueArgs& a, cudaStream_t st) {
   BlueDesc* d = nullptr;
   for (BlueDesc& b : blue_table())
-    if (b.logm == logm) d = &b;
-  if (!d) return fail(ESTL_UNSUPPORTED_SIZE, "no fused Bluestein kernel for M = 2^%d", logm);
+    if (b.kind == kind && b.logm == logm) d = &b;
+  if (!d) return fail(ESTL_UNSUPPORTED_SIZE, "no Bluestein kernel of kind %d for a tile of 2^%d", kind, logm);
   if (!d->attr_set) {
     std::lock_guard<std::mutex> g(g_blue_mu);
     if (!d->attr_set) {
@@ -644,8 +649,19 @@ static estl_status run_bluestein_fused(estl_plan p, long long count, const cf32*
       d->attr_set = true;
     }
   }
-  const long long grid = (count + (1LL << d->logc) - 1) >> d->logc;
+  // units: transforms (fused kernel) or tiles of C columns / rows (four-step)
+  const long long grid = kind == 0 ? (units + (1LL << d->logc) - 1) >> d->logc : units >> d->logc;
   if (grid < 1 || grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "Bluestein grid of %lld CTAs", grid);
+  BlueArgs args = a;
+  void* kargs[] = {&args};
+  return check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3((unsigned)d->nt), kargs, (size_t)d->smem_bytes,
+                                     st),
+                    "Bluestein kernel");
+}
+}  // namespace
+
+static BlueArgs blue_args(estl_plan p, long long count, const cf32* in, cf32* out) {
+  const long long N = p->layout.n, M = p->layout.blue_m;
   BlueArgs a;
   a.in = Ptr<const cf32>{in, count * N};
   a.out = Ptr<cf32>{out, count * N};
@@ -655,9 +671,42 @@ static estl_status run_bluestein_fused(estl_plan p, long long count, const cf32*
   a.n = N;
   a.count = count;
   a.sgn = p->sgn;
-  void* args[] = {&a};
-  return check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3((unsigned)d->nt), args, (size_t)d->smem_bytes, st),
-                    "Bluestein fused kernel");
+  a.logm = ilog2_exact(M);
+  return a;
+}
+
+// `count` transforms through the fused kernel of M.
+static estl_status run_bluestein_fused(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
+  const BlueArgs a = blue_args(p, count, in, out);
+  return blue_launch(0, a.logm, count, a, st);
+}
+
+// Four-step: chunks of blue_chunk transforms, the scratch in the work buffers.
+static estl_status run_bluestein_four_step(estl_plan p, long long count, const cf32* in, cf32* out,
+                                           cudaStream_t st) {
+  const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
+  const int logm = ilog2_exact(M), logn2 = bluestein_logn2(logm), logn1 = logm - logn2;
+  for (long long b0 = 0; b0 < count; b0 += cmax) {
+    const long long c = std::min(cmax, count - b0);
+    BlueArgs a = blue_args(p, c, in + b0 * N, out + b0 * N);
+    a.s1 = Ptr<cf32>{p->blue_a, c * M};
+    a.s2 = Ptr<cf32>{p->blue_c, c * M};
+    estl_status s = blue_launch(1, logn2, c << logn1, a, st);  // C columns of N2 per CTA
+    if (s == ESTL_OK) s = blue_launch(2, logn1, c << logn2, a, st);  // C rows of N1 per CTA
+    if (s == ESTL_OK) s = blue_launch(3, logn2, c << logn1, a, st);  // C rows of N2 per CTA
+    if (s != ESTL_OK) return s;
+  }
+  return ESTL_OK;
+}
+
+// Bp[k2*N1 + k1] = Bs[k2 + N2*k1]: the kernel spectrum in the order the
+// four-step middle kernel reads it.
+__global__ void blue_permute_kernel(const cf32* __restrict__ bs, cf32* __restrict__ bp, int logn1, int logn2) {
+  const long long m = 1LL << (logn1 + logn2);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const long long k2 = i >> logn1, k1 = i & ((1LL << logn1) - 1);
+    bp[i] = bs[k2 + (k1 << logn2)];
+  }
 }
 
 extern "C" {
@@ -688,6 +737,17 @@ static estl_status bluestein_setup(estl_plan_s* p) {
   if (s != ESTL_OK) return s;
   blue_scale_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_spec, M, 1.f / (float)M);
   s = check_cuda(cudaGetLastError(), "Bluestein set-up");
+  if (s == ESTL_OK && bluestein_four_step(M)) {
+    // the four-step middle kernel reads the spectrum permuted (the work
+    // buffer is free until the first execute)
+    const int logm = ilog2_exact(M), logn2 = bluestein_logn2(logm);
+    s = check_cuda(cudaMemcpyAsync(p->blue_a, p->blue_spec, (size_t)M * sizeof(cf32), cudaMemcpyDeviceToDevice, st),
+                   "Bluestein set-up");
+    if (s == ESTL_OK) {
+      blue_permute_kernel<<<flat_grid(M), 256, 0, st>>>(p->blue_a, p->blue_spec, logm - logn2, logn2);
+      s = check_cuda(cudaGetLastError(), "Bluestein set-up");
+    }
+  }
   if (s == ESTL_OK) s = check_cuda(cudaStreamSynchronize(st), "Bluestein set-up");
   return s;
 }
@@ -696,6 +756,7 @@ static estl_status bluestein_setup(estl_plan_s* p) {
 // multiply, M-point inverse FFT, post-multiply, in chunks of blue_chunk.
 static estl_status run_bluestein(estl_plan p, long long count, const cf32* in, cf32* out, cudaStream_t st) {
   if (bluestein_fused(p->layout.blue_m)) return run_bluestein_fused(p, count, in, out, st);
+  if (bluestein_four_step(p->layout.blue_m)) return run_bluestein_four_step(p, count, in, out, st);
   const long long N = p->layout.n, M = p->layout.blue_m, cmax = p->layout.blue_chunk;
   const int logm = ilog2_exact(M);
   for (long long b0 = 0; b0 < count; b0 += cmax) {

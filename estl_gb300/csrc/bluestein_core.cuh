@@ -16,6 +16,7 @@
 // Backward transforms conjugate the input and the output, like every other
 // plan here.
 #pragma once
+#include "conv_core.cuh"
 #include "fft_core.cuh"
 
 #if !defined(__CUDA_ARCH__)
@@ -107,11 +108,15 @@ struct BlueArgs {
   Ptr<const cf32> in;     // count transforms of N
   Ptr<cf32> out;          // count transforms of N
   Ptr<const cf32> chirp;  // w_n, N values
-  Ptr<const cf32> spec;   // Bs = FFT_M(b) / M, M values
+  Ptr<const cf32> spec;   // Bs = FFT_M(b) / M, M values (four-step: in the middle kernel's order)
   Ptr<const cf32> bank;
   long long n;
   long long count;
   float sgn;
+  // four-step (M > 2^14): M = 2^logm, scratch s1 / s2 of count * M
+  int logm = 0;
+  Ptr<cf32> s1{nullptr, 0};
+  Ptr<cf32> s2{nullptr, 0};
 };
 
 template <int LOGM, int LOGE, int LOGR, int LOGC>
@@ -166,6 +171,135 @@ struct BlueSingleKernel {
         if (k < n) stcs(y, k, conj_if(cmul(cf32{v[j].x, -v[j].y}, ldg(a.chirp, k)), a.sgn));
         if ((j & 7) == 7) compiler_order();
       }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// 2^14 < M <= 2^22: the convolution's three-launch four-step
+// (conv_core.cuh: ConvColKernel, ConvMidKernel, ConvOutKernel), M = N1 * N2,
+// with complex data and the chirps folded into its first load and last store:
+//   A  column n1 of the pre-multiplied input a_{n1 + N1 n2} (zero for n >= N):
+//      N2-point DFTs, times w_M^{n1 k2}            -> s1[f*M + k2*N1 + n1]
+//   B  row k2: N1-point DFT, times Bs (stored as Bp[k2*N1 + k1] = Bs[k2 + N2 k1]),
+//      conj, N1-point DFT, times w_M^{k2 n1}       -> s2[f*M + n1*N2 + k2]
+//   C  row n1 of s2: N2-point DFT = conj(c_k), k = n1 + N1 n2,
+//      X_k = w_k c_k (k < N)                        -> output
+// Three HBM round trips over M-element rows (the input and output only over
+// N) instead of five plus two per M-point FFT pass.
+// ---------------------------------------------------------------------------
+ESTL_CX bool bluestein_four_step(long long m) { return m > (1LL << kBlueFusedMaxLog) && m <= (1LL << 22); }
+ESTL_CX int bluestein_logn2(int logm) { return logm / 2; }  // column DFT length N2 (the convolution's split)
+
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct BlueColKernel {
+  using B = ConvColKernel<LOGM, LOGE, LOGR, LOGC>;
+  using TL = typename B::TL;
+  // up to 128 registers a thread (the chirp products spill at the plain column tile's 64)
+  static constexpr int C = B::C, NT = B::NT, SMEM_ELEMS = B::SMEM_ELEMS, MIN_BLOCKS = NT <= 256 ? 2 : 1;
+  ESTL_HD static void run(const BlueArgs& a, long long cta, int tid, cf32* smraw) {
+    const int c = tid & (C - 1);
+    const int t = tid >> LOGC;
+    const int logn1 = a.logm - LOGM;
+    const int M = 1 << a.logm, N1 = 1 << logn1;
+    const int nblk = N1 >> LOGC;
+    const long long f = cta / nblk;
+    const int n1 = (int)(cta - f * nblk) * C + c;
+    const int n = (int)a.n;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, B::EXCH};
+    const Ptr<const cf32> x = a.in.sub(f * a.n, a.n);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int m = n1 + ((t + TL::T * j) << logn1);
+      v[j] = m < n ? cmul(conj_if(ldcs(x, m), a.sgn), ldg(a.chirp, m)) : cf32{0.f, 0.f};
+    }
+    run_passes<TL, 0>(v, t, c, sm, tw, typename B::Sidx{});
+    const Ptr<cf32> o = a.s1.sub(f * M, M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k2 = t + TL::T * j;
+      o[(k2 << logn1) + n1] = cmul(v[j], twiddle_n(a.bank, a.logm, n1 * k2));
+    }
+  }
+};
+
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct BlueMidKernel {
+  using B = ConvMidKernel<LOGM, LOGE, LOGR, LOGC>;
+  using TL = typename B::TL;
+  static constexpr int C = B::C, NT = B::NT, SMEM_ELEMS = B::SMEM_ELEMS, MIN_BLOCKS = B::MINB;
+  ESTL_HD static void run(const BlueArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int M = 1 << a.logm;
+    const int logn2 = a.logm - LOGM;
+    const int nblk = 1 << (logn2 - LOGC);
+    const long long f = cta / nblk;
+    const int k2_0 = (int)(cta - f * nblk) * C;
+    const int k2 = k2_0 + c;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, B::EXCH};
+    const typename B::Sidx sidx{};
+    const Ptr<cf32> s1 = a.s1.sub(f * M + (long long)k2 * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s1[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    const Ptr<const cf32> h = a.spec.sub((long long)k2 * TL::M, TL::M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t + TL::T * j;
+      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logm, k2 * n1));
+    }
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const Ptr<cf32> o = a.s2.sub(f * M, M);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int n1 = t2 + TL::T * j;
+      o[(n1 << logn2) + k2_0 + c2] = sm[sidx(c2, n1)];
+    }
+  }
+};
+
+template <int LOGM, int LOGE, int LOGR, int LOGC>
+struct BlueOutKernel {
+  using B = ConvOutKernel<LOGM, LOGE, LOGR, LOGC>;
+  using TL = typename B::TL;
+  static constexpr int C = B::C, NT = B::NT, SMEM_ELEMS = B::SMEM_ELEMS, MIN_BLOCKS = B::MINB;
+  ESTL_HD static void run(const BlueArgs& a, long long cta, int tid, cf32* smraw) {
+    const int t = tid & (TL::T - 1);
+    const int c = tid >> TL::LOGT;
+    const int M = 1 << a.logm;
+    const int logn1 = a.logm - LOGM;
+    const int nblk = 1 << (logn1 - LOGC);
+    const long long f = cta / nblk;
+    const int n1_0 = (int)(cta - f * nblk) * C;
+    const Ptr<const cf32> tw = a.bank.sub(TL::M, TL::M);
+    const Ptr<cf32> sm{smraw, B::EXCH};
+    const typename B::Sidx sidx{};
+    const Ptr<cf32> s2 = a.s2.sub(f * M + (long long)(n1_0 + c) * TL::M, TL::M);
+    cf32 v[TL::E];
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) v[j] = s2[t + TL::T * j];
+    run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
+    ESTL_SYNC();
+    const int c2 = tid & (C - 1);
+    const int t2 = tid >> LOGC;
+    const int n = (int)a.n;
+    const Ptr<cf32> y = a.out.sub(f * a.n, a.n);
+#pragma unroll
+    for (int j = 0; j < TL::E; ++j) {
+      const int k = n1_0 + c2 + ((t2 + TL::T * j) << logn1);
+      if (k < n) stcs(y, k, conj_if(cmul(cconj(sm[sidx(c2, t2 + TL::T * j)]), ldg(a.chirp, k)), a.sgn));
     }
   }
 };

@@ -464,9 +464,10 @@ bool make_plan_bluestein(long long n, long long batch, Plan1D* out, std::string*
   p.blue_m = m;
   p.blue_chunk = chunk;
   p.scratch_elems = inner.scratch_elems;
-  // M <= 2^14: one fused kernel (bluestein_core.cuh); above: pre-multiply, two
+  // M <= 2^14: one fused kernel (bluestein_core.cuh); up to 2^22 the
+  // three-launch four-step with the chirps folded in; above: pre-multiply, two
   // M-point FFTs, spectrum multiply, post-multiply
-  p.hbm_passes = bluestein_fused(m) ? 1 : 2 * inner.hbm_passes + 3;
+  p.hbm_passes = bluestein_fused(m) ? 1 : bluestein_four_step(m) ? 3 : 2 * inner.hbm_passes + 3;
   *out = p;
   return true;
 }

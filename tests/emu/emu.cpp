@@ -551,6 +551,55 @@ int emu_bluestein_run(long long n, long long batch, int sign, const float* in, f
     }
     return 0;
   }
+  if (bluestein_four_step(M)) {
+    // the three four-step kernels of the GPU path, chunk by chunk
+    const int logm = ilog2_exact(M), logn2 = bluestein_logn2(logm), logn1 = logm - logn2;
+    std::vector<cf32> spec_p(M);  // Bp[k2*N1 + k1] = Bs[k2 + N2*k1]
+    for (long long i = 0; i < M; ++i) spec_p[i] = spec[(i >> logn1) + ((i & ((1LL << logn1) - 1)) << logn2)];
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    for (long long b0 = 0; b0 < batch; b0 += p.blue_chunk) {
+      const long long c = std::min(p.blue_chunk, batch - b0);
+      std::vector<cf32> s1(c * M, cf32{nan, nan}), s2(c * M, cf32{nan, nan});
+      BlueArgs a;
+      a.in = Ptr<const cf32>{x + b0 * n, c * n};
+      a.out = Ptr<cf32>{y + b0 * n, c * n};
+      a.chirp = Ptr<const cf32>{chirp.data(), n};
+      a.spec = Ptr<const cf32>{spec_p.data(), M};
+      a.bank = Ptr<const cf32>{host_bank().data(), kBankSize};
+      a.n = n;
+      a.count = c;
+      a.sgn = sgn;
+      a.logm = logm;
+      a.s1 = Ptr<cf32>{s1.data(), c * M};
+      a.s2 = Ptr<cf32>{s2.data(), c * M};
+      bool ok = true;
+      int ran = 0;
+      auto go = [&](auto kernel_tag, int tile_log, long long units) {
+        using K = decltype(kernel_tag);
+        if (!ok || K::TL::LM != tile_log) return;
+        ++ran;
+        ok = run_generic(K::NT, K::SMEM_ELEMS,
+                         [](const BlueArgs& args, long long cta, int tid, cf32* sm) { K::run(args, cta, tid, sm); }, a,
+                         units / K::C);
+      };
+#define ESTL_XC_COL(M_, E_, R_, C_) go(BlueColKernel<M_, E_, R_, C_>{}, logn2, c << logn1);
+#include "conv_list.inc"
+#define ESTL_XC_ROW(M_, E_, R_, C_) go(BlueMidKernel<M_, E_, R_, C_>{}, logn1, c << logn2);
+#include "conv_list.inc"
+#define ESTL_XC_OUT(M_, E_, R_, C_) go(BlueOutKernel<M_, E_, R_, C_>{}, logn2, c << logn1);
+#include "conv_list.inc"
+      if (!ok) {
+        std::lock_guard<std::mutex> gl(g_msg_mu);
+        set_err(err, errlen, g_msg);
+        return 1;
+      }
+      if (ran != 3) {
+        set_err(err, errlen, "no emulated four-step Bluestein kernel");
+        return 3;
+      }
+    }
+    return 0;
+  }
   for (long long b0 = 0; b0 < batch; b0 += p.blue_chunk) {
     const long long c = std::min(p.blue_chunk, batch - b0);
     Plan1D inner;
