@@ -48,9 +48,11 @@ def test_noalloc_matches_oracle(logn, direction):
     ref = oracle.fft(x, direction)
     xd = torch.from_numpy(x).cuda()
     stream = torch.cuda.current_stream().cuda_stream
+    import estl_gb300 as estl
     L = lib()
     free_after, reserved_after = [], []
     y = torch.empty_like(xd)
+    engine_used = estl.memory_usage()[0]
     for call in range(2):
         y.fill_(float("nan"))
         torch.cuda.synchronize()
@@ -67,6 +69,9 @@ def test_noalloc_matches_oracle(logn, direction):
     # allocate nothing: neither the driver's free memory nor torch's pool moves
     assert reserved_after[1] == reserved_after[0]
     assert free_after[1] == free_after[0]
+    # and the engine's own allocator (every device allocation of the library
+    # goes through its HBM budget) is not touched by either call
+    assert estl.memory_usage()[0] == engine_used
 
 
 def test_noalloc_rejects_sizes_beyond_the_limit():
