@@ -237,6 +237,28 @@ def test_gpu_correlation_and_compat(engine):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("flags", [2, 3])
+def test_gpu_compat_correlation_and_wrapped_crop(engine, flags):
+    """Reference-compatible mode on the GPU: correlation (the output shifted the
+    other way, the conjugate taken after the kernel shift) and crops that wrap
+    (a 1-tap filter on power-of-two signals), through the paired and unpaired
+    single tiles and the real-input and complex four-step forms, against
+    oracle.conv_compat (pinned to a restatement of Convolution.h:95-148)."""
+    shapes = [(4, 1), (16, 1), (1024, 1), (16384, 1), (32768, 1), (5, 1), (300, 40), (5000, 33), (20000, 257)]
+    reqs, sig, filt, _ = make_requests(shapes, 73)
+    filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L
+    for extra in (0, NO_PAIRING, COMPLEX):
+        out = gpu_conv_batch(engine, creqs, sig, filt, oo, flags=flags | extra)
+        for L, K, so, fo, o in creqs:
+            ref = compat_reference(sig[so:so + L], filt[fo:fo + K], correlate=bool(flags & 1))
+            assert rel(out[o:o + L], ref) < TOL, (L, K, flags, extra)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("L,K,count", [(1000, 31, 64), (50000, 1000, 8), (1 << 20, 4096, 2)])
 def test_gpu_conv_plan(engine, L, K, count):
     import torch
