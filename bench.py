@@ -1070,6 +1070,25 @@ def main():
     worst = min(per_n_out, key=lambda k: per_n_out[k]["frac"])
     roofline["worst_n"] = {"n": worst, "frac": per_n_out[worst]["frac"], "hbm_passes": per_n_out[worst]["hbm_passes"],
                            "plan": per_n_out[worst]["plan"]}
+    # the same launch times grouped by kernel template (one template serves
+    # several sizes): the template with the largest share of device time
+    by_tpl = {}
+    for (kind, logn), (cnt, ms, byts) in stats.items():
+        ks = [k for k in plans[logn][0].describe()["kernels"] if k["kind"] == kind]
+        name = kind + " " + "+".join(
+            f"<{k['logm']},{k['loge']},{k['logc']}" + (f",pipe {k['pipe']}" if k["pipe"] else "") +
+            (f",cluster {1 << k['cluster']}" if k["cluster"] else "") + ">" for k in ks)
+        t = by_tpl.setdefault(name, [0, 0.0, 0.0, []])
+        t[0] += cnt
+        t[1] += ms
+        t[2] += byts
+        t[3].append(f"2^{logn}")
+    tname, (tcnt, tms, tbytes, tsizes) = max(by_tpl.items(), key=lambda kv: kv[1][1])
+    t_ach = (tbytes / tcnt) / (tms / tcnt / 1e3) / 1e9
+    roofline["largest_template"] = {"template": tname, "sizes": tsizes,
+                                    "share_of_device_time": round(tms / sum(v[1] for v in stats.values()), 3),
+                                    "achieved": round(t_ach, 1), "frac": round(t_ach / peak, 4),
+                                    "avg_launch_us": round(1e3 * tms / tcnt, 2)}
 
     # end to end through the C ABI with pinned host buffers (H2D + D2H inside)
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 3))
