@@ -384,6 +384,32 @@ def bench_config1(estl, torch, autotune=True):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms_long = e0.elapsed_time(e1) / (long_replays * reps)
+    # independent batches in flight: the same 64 executes alternating between
+    # two streams of one graph, so two batches run at a time (throughput of
+    # independent batches, not the stream-ordered figure above; the one-launch
+    # plan holds no device state, so its executes may overlap)
+    s2 = torch.cuda.Stream()
+    g2 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g2, stream=s):
+        fork = torch.cuda.Event()
+        fork.record(s)
+        s2.wait_event(fork)
+        for i in range(reps):
+            st2 = s if i % 2 == 0 else s2
+            plan.execute_ptr(xs[i % rot].data_ptr(), ys[i % rot].data_ptr(), st2.cuda_stream)
+        join = torch.cuda.Event()
+        join.record(s2)
+        s.wait_event(join)
+    for _ in range(3):
+        g2.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(replays):
+        g2.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_two = e0.elapsed_time(e1) / (replays * reps)
+    del g2
     d = plan.describe()["kernels"]
     del g  # the graph holds the plan's ordering event
     plan.close()
@@ -432,6 +458,7 @@ def bench_config1(estl, torch, autotune=True):
                       "16 replays timed (1024 executes)",
             "plan": d, "autotune_fastest": tuned, "us_per_execute_by_batch": curve,
             "clocks_long_run": dict(clk, us_per_transform_batch=round(1e3 * ms_long, 3), executes=long_replays * reps),
+            "two_streams_us_per_batch": round(1e3 * ms_two, 3),
             "us_per_transform_batch": round(1e3 * ms, 3), "gbs": round(16 * n * batch / (ms * 1e-3) / 1e9, 1),
             "gflops": round(5 * n * 12 * batch / (ms * 1e-3) / 1e9, 1), "rel_l2_max": err}
 
