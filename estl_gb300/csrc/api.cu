@@ -289,10 +289,7 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     estl_status s = lookup_kernel(st, pipe, &d, &resident);
     if (s != ESTL_OK) return s;
     if (st.grid < 1 || st.grid > INT_MAX) return fail(ESTL_UNSUPPORTED_SIZE, "grid of %lld CTAs", st.grid);
-    // persistent kernels: at most the CTAs that fit the device at once (whole
-    // clusters for the persistent cluster tiles)
-    const long long cl = 1LL << d->cluster;
-    const long long grid = pipe ? std::min<long long>(st.grid, std::max(cl, (resident / cl) * cl)) : st.grid;
+    const long long grid = pipe ? std::min<long long>(st.grid, resident) : st.grid;
     TileArgs a;
     a.in = Ptr<const cf32>{src + st.src_off, st.src_len};
     a.out = Ptr<cf32>{dst + st.dst_off, st.dst_len};
@@ -324,10 +321,9 @@ estl_status launch_steps(const Plan1D& plan, const cf32* in, cf32* out, cf32* sc
     void* args[] = {&a, &map};
     // persistent bulk-load kernels keep plain stream order (measured: with
     // programmatic launch their three-pass chains ran 1-4% slower)
-    s = (pipe && !d->cluster)
-            ? check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
-                         "cudaLaunchKernel")
-            : launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx", d->cluster);
+    s = pipe ? check_cuda(cudaLaunchKernel(d->fn, dim3((unsigned)grid), dim3(d->nthreads), args, d->smem_bytes, stream),
+                          "cudaLaunchKernel")
+             : launch_pdl(d->fn, grid, d->nthreads, args, d->smem_bytes, stream, "cudaLaunchKernelEx", d->cluster);
     if (s != ESTL_OK) return s;
   }
   return ESTL_OK;

@@ -53,9 +53,6 @@ estl::cf32* estl_emu_cluster_smem(int rank, long long* n);
 
 namespace estl {
 
-// Kernel-table pipe value of the persistent cluster tiles (ClusterLoopKernel).
-constexpr int kPipeClusterLoop = 5;
-
 // Read-only view of a buffer of another CTA of the cluster: the same offset
 // in that CTA's shared memory as `local` has in this CTA's.
 struct PeerBuf {
@@ -184,98 +181,6 @@ struct ClusterKernel {
     run_passes<TB, 1>(v, t, c, sm, twb, SidxB{});
 #pragma unroll
     for (int j = 0; j < TB::E; ++j) stcs(out, k2 + ((t + TB::T * j) << LOGN2), conj_if(v[j], a.sgn));
-  }
-};
-
-// Persistent form of ClusterKernel: each cluster loops over transforms
-// f = cluster, cluster + clusters, ... with two buffers U[0], U[1] per CTA.
-// In iteration i (b = i & 1) phase A runs its column passes in U[b] and then
-// leaves its Z there; phase B gathers every CTA's U[b] and runs its row
-// passes in U[1 - b].  One cluster barrier per transform orders both
-//   * the release of this transform's Z (arrive.release after the Z stores,
-//     wait.acquire before the remote gather), and
-//   * the end of every CTA's reads of U[1 - b] as last transform's Z (those
-//     reads precede each thread's arrive), before U[1 - b] is written again
-//     by this transform's row passes and next transform's column passes,
-// where ClusterKernel needs two barriers (the second one only to free Z).  A
-// last barrier after the loop keeps every CTA's shared memory alive until the
-// cluster's remote reads of it are done.
-template <int LOGN, int LOGR, int LOGN2, int LOGE>
-struct ClusterLoopKernel {
-  using B = ClusterKernel<LOGN, LOGR, LOGN2, LOGE>;
-  using TA = typename B::TA;
-  using TB = typename B::TB;
-  static constexpr int R = B::R, N = B::N, LOGN1 = B::LOGN1, LOGW = B::LOGW, W = B::W, LOGH = B::LOGH,
-                       H = B::H, ZS = B::ZS, NT = B::NT;
-  static constexpr int U = B::SMEM_ELEMS;  // one buffer: Z, or either phase's exchange
-  static constexpr int SMEM_ELEMS = 2 * U;
-  // CTAs per SM that the two buffers allow: the registers are sized for those
-  static constexpr int SMEM_BLOCKS = (227 * 1024) / (SMEM_ELEMS * 8 + 1024);
-  static constexpr int MIN_BLOCKS =
-      SMEM_BLOCKS < 1 ? 1 : (SMEM_BLOCKS < B::MIN_BLOCKS ? SMEM_BLOCKS : B::MIN_BLOCKS);
-  static constexpr int LOG_CLUSTER = LOGR, LOG_SPLIT = LOGN2;
-  static constexpr bool PERSISTENT = true;
-  static_assert(U % 2 == 0, "16-byte aligned buffers");
-
-  ESTL_HD static void run(const TileArgs& a, long long cta, int tid, cf32* smraw) {
-    const int rank = (int)(cta & (R - 1));
-    const long long cl = cta >> LOGR, ncl = a.grid >> LOGR;  // the grid is a whole number of clusters
-    const Ptr<cf32> ub[2] = {Ptr<cf32>{smraw, U}, Ptr<cf32>{smraw + U, U}};
-    const Ptr<const cf32> twa = a.bank.sub(1 << LOGN2, 1 << LOGN2);
-    const Ptr<const cf32> twb = a.bank.sub(1 << LOGN1, 1 << LOGN1);
-    int it = 0;
-    for (long long f = cl; f < a.rows; f += ncl, ++it) {
-      const int b = it & 1;
-      const Ptr<const cf32> in = a.in.sub(xbase(a, f, N), N);
-      const Ptr<cf32> out = a.out.sub(xbase(a, f, N), N);
-      cf32 v[TA::E];
-      // phase A: column DFTs of this CTA's W columns, exchanges in U[b]
-      {
-        const int c = tid & (W - 1), t = tid >> LOGW;
-        const int n1 = rank * W + c;
-        int off = n1 + (t << LOGN1);
-#pragma unroll
-        for (int j = 0; j < TA::E; ++j, off += TA::T << LOGN1) v[j] = conj_if(ldcs(in, off), a.sgn);
-        run_passes<TA, 0>(v, t, c, ub[b], twa, typename B::SidxA{});
-        fourstep_twiddle<TA>(v, n1, t, LOGN, a.bank);
-        ESTL_SYNC();  // the last exchange's reads are done: Z overwrites U[b]
-#pragma unroll
-        for (int j = 0; j < TA::E; ++j) ub[b][c * ZS + t + TA::T * j] = v[j];
-      }
-      ESTL_CLUSTER_ARRIVE();  // release this CTA's Z; its reads of U[1 - b] are behind it
-      ESTL_SYNC();            // this CTA's Z to its own threads
-      const int c = tid & (H - 1), t = tid >> LOGH;
-      const int k2 = rank * H + c;
-      {
-        constexpr int SPAN = W / TB::T;  // slots per source CTA
-#pragma unroll
-        for (int j = 0; j < TB::E; ++j)
-          if (j / SPAN == rank) v[j] = ub[b][((t + TB::T * j) & (W - 1)) * ZS + k2];
-        ESTL_CLUSTER_WAIT();  // every CTA's Z is complete; every read of U[1 - b] is done
-        PeerBuf z[R];
-#pragma unroll
-        for (int q = 0; q < R; ++q) z[q] = peer_buf(ub[b].p, U, rank, q);
-#pragma unroll
-        for (int j = 0; j < TB::E; ++j)
-          if (j / SPAN != rank) v[j] = z[j / SPAN][((t + TB::T * j) & (W - 1)) * ZS + k2];
-      }
-      // phase B: row DFTs, exchanges in U[1 - b] (free since the wait)
-      TB::template compute<0>(v, t, twb);
-      if constexpr (TB::P > 1) {
-#pragma unroll
-        for (int j = 0; j < TB::E; ++j) ub[1 - b][typename B::SidxB{}(c, TB::template out_pos<0>(t, j))] = v[j];
-        ESTL_SYNC();
-#pragma unroll
-        for (int j = 0; j < TB::E; ++j) v[j] = ub[1 - b][typename B::SidxB{}(c, t + TB::T * j)];
-        ESTL_SYNC();
-      }
-      run_passes<TB, 1>(v, t, c, ub[1 - b], twb, typename B::SidxB{});
-#pragma unroll
-      for (int j = 0; j < TB::E; ++j) stcs(out, k2 + ((t + TB::T * j) << LOGN2), conj_if(v[j], a.sgn));
-    }
-    // the other CTAs' reads of this CTA's last Z end before it exits
-    ESTL_CLUSTER_ARRIVE();
-    ESTL_CLUSTER_WAIT();
   }
 };
 

@@ -21,8 +21,7 @@ struct KernelDesc {
   int smem_bytes;
   const void* fn;
   int pipe;  // 0: plain tile; 2: bulk-load ring (bulk_core.cuh);
-             // 3 / 4: resident whole transforms with a whole / half exchange buffer (resident_core.cuh);
-             // 5 (kPipeClusterLoop): persistent cluster tile (cluster_core.cuh ClusterLoopKernel)
+             // 3 / 4: resident whole transforms with a whole / half exchange buffer (resident_core.cuh)
   int tc;    // radix-16 passes on the tensor cores (tc_core.cuh)
   int tmap;  // launched with a 2D tensor map of its input as a second parameter (tma_tile_kernel)
   int cluster = 0;  // cluster tiles (cluster_core.cuh): log2 CTAs per cluster
@@ -70,8 +69,6 @@ constexpr long long kMaxSmemBytes = 227 * 1024;
 #define ESTL_BULK_COL(M, E, R, C) make_tma_desc<BulkColKernel<M, E, R, C>>(KIND_COL, M, E, R, C)
 #define ESTL_RES(M, E, R, H) make_desc<ResKernel<M, E, R, H>>(KIND_SINGLE, M, E, R, 0, 2 + H)
 #define ESTL_CLUSTER_TILE(N, LR, N2, E) make_desc<ClusterKernel<N, LR, N2, E>>(KIND_SINGLE, N, E, 4, 0)
-#define ESTL_CLUSTER_LOOP_TILE(N, LR, N2, E) \
-  make_desc<ClusterLoopKernel<N, LR, N2, E>>(KIND_SINGLE, N, E, 4, 0, kPipeClusterLoop)
 #define ESTL_COLUMN(M, E, C) make_desc<ColKernel<M, E, 4, C, false, false>>(KIND_COLUMN, M, E, 4, C)
 #define ESTL_TC_SINGLE(M, C) make_desc<SingleKernel<M, 4, 4, C, true>>(KIND_SINGLE, M, 4, 4, C, 0, 1)
 #define ESTL_TC_COL(M, C) make_desc<ColKernel<M, 4, 4, C, true>>(KIND_COL, M, 4, 4, C, 0, 1)

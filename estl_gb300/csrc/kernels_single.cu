@@ -7,8 +7,6 @@
   static_assert(ResKernel<M, E, R, H>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "resident tile too large");
 #define ESTL_X_CLUSTER(N, LR, N2, E) \
   static_assert(ClusterKernel<N, LR, N2, E>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "cluster tile too large");
-#define ESTL_X_CLUSTER_LOOP(N, LR, N2, E) \
-  static_assert(ClusterLoopKernel<N, LR, N2, E>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "cluster tile too large");
 #define ESTL_X_TC_COL(M, C) \
   static_assert(ColKernel<M, 4, 4, C, true>::SMEM_ELEMS * 8 <= kMaxSmemBytes, "tensor-core tile too large");
 #define ESTL_X_TC_ROW(M, C) \
@@ -24,7 +22,6 @@ static const KernelDesc kTable[] = {
 #define ESTL_X_TC_SINGLE(M, C) ESTL_TC_SINGLE(M, C),
 #define ESTL_X_RES(M, E, R, H) ESTL_RES(M, E, R, H),
 #define ESTL_X_CLUSTER(N, LR, N2, E) ESTL_CLUSTER_TILE(N, LR, N2, E),
-#define ESTL_X_CLUSTER_LOOP(N, LR, N2, E) ESTL_CLUSTER_LOOP_TILE(N, LR, N2, E),
 #include "kernel_list.inc"
 };
 

@@ -29,8 +29,6 @@ std::vector<TileCfg> build_configs() {
 #define ESTL_X_BULK_COL(M, E, R, C) v.push_back(cfg_of<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_RES(M, E, R, H) v.push_back(cfg_of<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));
 #define ESTL_X_CLUSTER(N, LR, N2, E) v.push_back(cfg_of<ClusterKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0));
-#define ESTL_X_CLUSTER_LOOP(N, LR, N2, E) \
-  v.push_back(cfg_of<ClusterLoopKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0, kPipeClusterLoop));
 #define ESTL_X_COLUMN(M, E, C) v.push_back(cfg_of<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) v.push_back(cfg_of<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) v.push_back(cfg_of<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -270,8 +268,8 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     const TileCfg* c =
         cluster_default
             ? default_cluster(logn)
-            : find_tile(STEP_SINGLE, logn, choice.single_loge >= 0 ? choice.single_loge : 4, 4, 0,
-                        choice.pipe == kPipeClusterLoop ? kPipeClusterLoop : 0, 0, choice.single_cluster, choice.logn2);
+            : find_tile(STEP_SINGLE, logn, choice.single_loge >= 0 ? choice.single_loge : 4, 4, 0, 0, 0,
+                        choice.single_cluster, choice.logn2);
     if (!c) {
       set_err(err, "no cluster tile instantiated for log2 n = %lld with 2^%lld CTAs per transform", logn,
               choice.single_cluster);
@@ -280,7 +278,6 @@ bool make_plan(long long n, long long batch, const PlanChoice& choice, Plan1D* o
     Step s{STEP_SINGLE, logn, c->loge, c->logr, 0, batch << c->cluster, BUF_IN, BUF_OUT, 0, total, 0, total, batch, logn};
     s.cluster = c->cluster;
     s.csplit = c->csplit;
-    s.pipe = c->pipe;
     p.steps.push_back(s);
     p.hbm_passes = 1;
     *out = p;
@@ -516,7 +513,6 @@ std::vector<PlanChoice> plan_candidates(long long n, long long batch) {
     ch.single_logc = 0;
     ch.single_cluster = c.cluster;
     ch.logn2 = c.csplit;
-    ch.pipe = c.pipe;  // 0, or the persistent form (kPipeClusterLoop)
     out.push_back(ch);
   }
   for (int lr = 7; lr <= 9; ++lr)

@@ -83,8 +83,6 @@ const std::vector<EmuKernel>& emu_kernels() {
 #define ESTL_X_BULK_COL(M, E, R, C) k.push_back(mk<BulkColKernel<M, E, R, C>>(STEP_COL, M, E, R, C, 2));
 #define ESTL_X_RES(M, E, R, H) k.push_back(mk<ResKernel<M, E, R, H>>(STEP_SINGLE, M, E, R, 0, 2 + H));
 #define ESTL_X_CLUSTER(N, LR, N2, E) k.push_back(mk<ClusterKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0));
-#define ESTL_X_CLUSTER_LOOP(N, LR, N2, E) \
-  k.push_back(mk<ClusterLoopKernel<N, LR, N2, E>>(STEP_SINGLE, N, E, 4, 0, kPipeClusterLoop));
 #define ESTL_X_COLUMN(M, E, C) k.push_back(mk<ColKernel<M, E, 4, C, false, false>>(STEP_COLUMN, M, E, 4, C));
 #define ESTL_X_TC_SINGLE(M, C) k.push_back(mk<SingleKernel<M, 4, 4, C, true>>(STEP_SINGLE, M, 4, 4, C, 0, 1));
 #define ESTL_X_TC_COL(M, C) k.push_back(mk<ColKernel<M, 4, 4, C, true>>(STEP_COL, M, 4, 4, C, 0, 1));
@@ -678,11 +676,9 @@ static int run_plan(const Plan1D& p, int sign, const float* in, float* out, char
       if (st.dst == BUF_OUT) a.out = Ptr<cf32>{cout, extent};
       a.xoff = Ptr<const long long>{xoff + first, st.rows};
     }
-    // pipelined kernels are grid-stride: emulate one or two CTAs (clusters, for
-    // the persistent cluster tiles) so that every CTA loops over several tiles
-    // and uses both tile buffers
-    const long long cl = 1LL << k->cluster;
-    const long long grid = k->pipe ? (st.grid >= 4 * cl ? 2 : 1) * cl : st.grid;
+    // pipelined kernels are grid-stride: emulate one or two CTAs so that every
+    // CTA loops over several tiles and uses both tile buffers
+    const long long grid = k->pipe ? (st.grid >= 4 ? 2 : 1) : st.grid;
     a.grid = grid;
     a.split = st.tc ? p.choice.split : SPLIT_NONE;
     a.err = nullptr;

@@ -252,25 +252,6 @@ def test_cluster_scheduler_orders_distributed_shared_memory(emu):
         assert emu.emu_cluster_barrier_selftest(ncta, 64, 0) < ncta * 64
 
 
-@pytest.mark.parametrize("logn", [14, 15, 16])
-def test_persistent_cluster_tiles_reuse_both_buffers(emu, logn):
-    """The persistent cluster tiles (ClusterLoopKernel, one cluster barrier per
-    transform, two buffers per CTA): five transforms on two emulated clusters,
-    so that each cluster reuses both buffers, in both scheduling orders; a read
-    of a peer's buffer that the barrier does not order sees the NaN poison."""
-    n = 1 << logn
-    cands = [c for c in cluster_candidates(emu, n) if c[10] == 5]
-    assert cands, "no persistent cluster tiles"
-    x = rand_c64((5, n), 70 + logn)
-    for c in cands:
-        for sign in (-1, +1):
-            rc, msg, y = emu_run(emu, n, 5, x, sign, c)
-            assert rc == 0, (c, msg)
-            assert oracle.rel_l2(y, oracle.fft(x, sign)).max() < TOL, c
-        d = describe(emu, n, 5, c)
-        assert d["kernels"][0]["pipe"] == 5 and d["kernels"][0]["cluster"] == c[16]
-
-
 @pytest.mark.parametrize("logn", range(12, 18))
 def test_cluster_tiles(emu, logn):
     """Every cluster tile (one transform per thread-block cluster, the

@@ -367,23 +367,20 @@ CLUSTER_TILES = [(12, 1, 6, 4), (12, 2, 6, 4), (13, 1, 7, 4), (14, 1, 7, 4), (14
                  (17, 4, 9, 4)]
 
 
-@pytest.mark.parametrize("pipe", [0, 5])
 @pytest.mark.parametrize("logn,lcl,logn2,loge", CLUSTER_TILES)
-def test_cluster_tiles(engine, logn, lcl, logn2, loge, pipe):
+def test_cluster_tiles(engine, logn, lcl, logn2, loge):
     """One transform per thread-block cluster of 2^lcl CTAs (cluster_core.cuh:
     column DFTs, the four-step transpose through distributed shared memory,
-    row DFTs; one HBM pass), both directions, against the oracle; pipe 5: the
-    persistent form (two buffers per CTA, one cluster barrier per transform)."""
+    row DFTs; one HBM pass), both directions, against the oracle."""
     import torch
     n = 1 << logn
     x = uniform_c64(((1 << 23) // n + 1, n), 1500 + logn + lcl)
     xd = torch.from_numpy(x).cuda()
     for direction in (-1, +1):
         p = engine.Plan(n, x.shape[0], direction, mode="single",
-                        tiles={"single_loge": loge, "single_cluster_log2": lcl, "split_log2": logn2,
-                               "pipelined": pipe})
+                        tiles={"single_loge": loge, "single_cluster_log2": lcl, "split_log2": logn2})
         d = p.describe()
-        assert d["hbm_passes"] == 1 and d["kernels"][0]["cluster"] == lcl and d["kernels"][0]["pipe"] == pipe
+        assert d["hbm_passes"] == 1 and d["kernels"][0]["cluster"] == lcl
         y = p.execute(xd)
         p.check()
         assert oracle.rel_l2(y.cpu().numpy(), oracle.fft(x, direction)).max() < tol(n)
