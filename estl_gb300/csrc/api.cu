@@ -447,7 +447,7 @@ estl_status estl_init(int device, size_t hbm_budget_bytes) {
   cudaDeviceProp prop;
   s = check_cuda(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
   if (s != ESTL_OK) return s;
-  if (prop.major < 10) return fail(ESTL_DEVICE_ERROR, "device %d is sm_%d%d; this build targets sm_103a", device, prop.major, prop.minor);
+  if (prop.major < 10) return fail(ESTL_DEVICE_ERROR, "device %d is sm_%d%d; the library is compiled for sm_103a", device, prop.major, prop.minor);
   E.device = device;
   E.num_sms = prop.multiProcessorCount;
   E.budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)(0.9 * (double)free_b);

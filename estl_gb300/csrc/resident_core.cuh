@@ -19,9 +19,9 @@
 //
 // Two-round exchange (H = 2): after pass p, output slot j of thread t goes to
 // position q = out_pos<p>(t, j); the next pass reads positions t + T*j, so
-// reads j < E/2 are exactly the positions q < M/2.  Round 0 writes the values
-// with q < M/2 and reads them into a temporary, round 1 writes the rest and
-// reads v[E/2..E); the temporary then fills v[0..E/2).
+// reads j < E/2 are exactly the positions q < M/2.  The first half-exchange
+// writes the values with q < M/2 and reads them into a temporary, the second
+// writes the rest and reads v[E/2..E); the temporary then fills v[0..E/2).
 //
 // Waits are bounded as in bulk_core.cuh.
 #pragma once

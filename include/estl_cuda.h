@@ -41,7 +41,7 @@ typedef enum estl_status {
 
 /* Arithmetic of a plan.  FP32 is the plain path. */
 #define ESTL_PREC_FP32 0
-/* Split precision (north star "Precision"): every radix-16 DFT stage runs as a
+/* Split precision: every radix-16 DFT stage runs as a
  * tensor-core GEMM (mma.sync m16n8k16, FP32 accumulate) on operands split
  * into 16-bit terms; twiddles and the other passes stay FP32.
  *   FP16:     fp16 hi + lo, each butterfly scaled by a power of two first

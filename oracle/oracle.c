@@ -1,4 +1,5 @@
-/* oracle.c — TEST INFRASTRUCTURE ONLY (the checker, never the product).
+/* oracle.c — TEST INFRASTRUCTURE ONLY (the tests' reference results, never
+ * the product).
  *
  * CPU FP64 restatement of the transform the reference's CPU backend computes:
  *   FFT_FFTW3.h:23-31  fftwf_plan_many_dft(rank 1, n = size, howmany = batch,

@@ -1,4 +1,4 @@
-/* ref_contiguous.c — TEST / BASELINE INFRASTRUCTURE ONLY.
+/* ref_contiguous.c — TEST AND CPU-BASELINE INFRASTRUCTURE ONLY.
  *
  * FP32 CPU restatement of the reference's own GPU algorithm for the path,
  * FFT_OpenCL_Contiguous<float>, used as the timed "reference algorithm on

@@ -1,4 +1,4 @@
-"""Pins the FP64 oracle before it is trusted as the checker.
+"""Pins the FP64 oracle before the other tests trust its results.
 
 * the known-answer test of the reference (tests/Test.cpp:60-77): a cosine of
   frequency effK transforms to M/2 at q = effK and q = M - effK, 0 elsewhere,
