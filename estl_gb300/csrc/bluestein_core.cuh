@@ -218,11 +218,9 @@ struct BlueColKernel {
     }
     run_passes<TL, 0>(v, t, c, sm, tw, typename B::Sidx{});
     const Ptr<cf32> o = a.s1.sub(f * M, M);
+    fourstep_twiddle<TL>(v, n1, t, a.logm, a.bank);  // times w_M^{n1 k2}, k2 = t + T j
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int k2 = t + TL::T * j;
-      o[(k2 << logn1) + n1] = cmul(v[j], twiddle_n(a.bank, a.logm, n1 * k2));
-    }
+    for (int j = 0; j < TL::E; ++j) o[((t + TL::T * j) << logn1) + n1] = v[j];
   }
 };
 
@@ -252,11 +250,9 @@ struct BlueMidKernel {
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
     run_passes<TL, 0>(v, t, c, sm, tw, sidx);
+    fourstep_twiddle<TL>(v, k2, t, a.logm, a.bank);  // times w_M^{k2 n1}, n1 = t + T j
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int n1 = t + TL::T * j;
-      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logm, k2 * n1));
-    }
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();
     const int c2 = tid & (C - 1);
     const int t2 = tid >> LOGC;

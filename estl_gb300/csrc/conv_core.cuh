@@ -428,11 +428,9 @@ struct ConvColKernel {
     }
     any_passes<TC, TL>(v, t, c, sm, tw, Sidx{}, smraw + TC_OFF, a.split, tid);
     const Ptr<cf32> o = a.s1.sub(f * N, N);
+    fourstep_twiddle<TL>(v, n1, t, a.logn, a.bank);  // times w_N^{n1 k2}, k2 = t + T j
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int k2 = t + TL::T * j;
-      o[(k2 << logn1) + n1] = cmul(v[j], twiddle_n(a.bank, a.logn, n1 * k2));
-    }
+    for (int j = 0; j < TL::E; ++j) o[((t + TL::T * j) << logn1) + n1] = v[j];
   }
 };
 
@@ -519,11 +517,9 @@ struct ConvMidKernel {
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) v[j] = cconj(cmul(v[j], ldg(h, t + TL::T * j)));
     any_passes<TC, TL>(v, t, c, sm, tw, sidx, smraw + TC_OFF, a.split, tid);
+    fourstep_twiddle<TL>(v, k2, t, a.logn, a.bank);  // times w_N^{k2 n1}, n1 = t + T j
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int n1 = t + TL::T * j;
-      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logn, k2 * n1));
-    }
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();
     const int c2 = tid & (C - 1);
     const int t2 = tid >> LOGC;
@@ -759,11 +755,9 @@ struct ConvMidHalfKernel {
     }
     run_passes<TL, 0>(v, t, c, sm, tw, sidx);
     if constexpr (TL::P == 1) ESTL_SYNC();
+    fourstep_twiddle<TL>(v, mr.k2, t, a.logn, a.bank);  // times w_N'^{k2 n1}, n1 = t + T j
 #pragma unroll
-    for (int j = 0; j < TL::E; ++j) {
-      const int n1 = t + TL::T * j;
-      sm[sidx(c, n1)] = cmul(v[j], twiddle_n(a.bank, a.logn, mr.k2 * n1));
-    }
+    for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();
     const int c2 = tid & (C - 1);
     const int t2 = tid >> LOGC;
