@@ -60,6 +60,34 @@ struct ConvArgs {
 
 ESTL_HD cf32 cconj(cf32 v) { return {v.x, -v.y}; }
 
+// w^j (0 <= j < 16) from w, w^2, w^4, w^8: at most three products.
+ESTL_HD cf32 pow16(int j, cf32 w1, cf32 w2, cf32 w4, cf32 w8) {
+  cf32 r{1.f, 0.f};
+  bool one = true;
+  const cf32 f[4] = {w1, w2, w4, w8};
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+    if (j & (1 << b)) {
+      r = one ? f[b] : cmul(r, f[b]);
+      one = false;
+    }
+  return r;
+}
+
+// The real-input split twiddles w_N^{k2 + N2 k1} of a row tile's slots
+// k1 = t + T j: the base w_N^{k2 + N2 t} and the step powers W^1, W^2, W^4,
+// W^8 (W = w_N^{N2 T}) from the table, slot j's factor as base * W^j.
+struct SplitTwiddles {
+  cf32 base, w1, w2, w4, w8;
+  ESTL_HD cf32 operator()(int j) const { return j ? cmul(base, pow16(j, w1, w2, w4, w8)) : base; }
+};
+ESTL_HD SplitTwiddles split_twiddles(const Ptr<const cf32>& bank, int logn_full, int k2, int t, int logn2, int T) {
+  const int s = T << logn2;
+  return SplitTwiddles{twiddle_n(bank, logn_full, k2 + (t << logn2)), twiddle_n(bank, logn_full, s),
+                       twiddle_n(bank, logn_full, 2 * s), twiddle_n(bank, logn_full, 4 * s),
+                       twiddle_n(bank, logn_full, 8 * s)};
+}
+
 // 1 / (N * spectrum DC) when the row asks for the reference's DC
 // normalisation, else 1 (the stored spectrum already carries 1/N).
 ESTL_HD float dc_factor(const ConvArgs& a, const ConvRow& r) {
@@ -673,13 +701,15 @@ struct SpecRowHalfKernel {
     for (int j = 0; j < TL::E; ++j) sm[sidx(c, t + TL::T * j)] = v[j];
     ESTL_SYNC();
     const Ptr<cf32> o = a.spec_out.sub(r.spec_off, NH + 2);
+    static_assert(TL::E == 16, "split twiddle powers for 16 slots");
+    const SplitTwiddles stw = split_twiddles(a.bank, a.logn + 1, mr.k2, t, logn2, TL::T);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int k1 = t + TL::T * j;
       const cf32 zm = sm[sidx(mr.partner, mirror_k1(mr.k2, k1, TL::M))];
       cf32 e, od;
       real_split(v[j], zm, e, od);
-      const cf32 w = twiddle_n(a.bank, a.logn + 1, mr.k2 + (k1 << logn2));
+      const cf32 w = stw(j);  // w_N^{k2 + N2 k1}
       const cf32 wo = cmul(w, od);
       const cf32 h = cadd(e, wo);
       o[mr.k2 * TL::M + k1] = cf32{h.x * r.scale, h.y * r.scale * r.conj};
@@ -737,13 +767,15 @@ struct ConvMidHalfKernel {
     for (int j = 0; j < TL::E; ++j) zm[j] = sm[sidx(mr.partner, mirror_k1(mr.k2, t + TL::T * j, TL::M))];
     ESTL_SYNC();  // the buffer is the next passes' exchange space
     const Ptr<const cf32> h = a.spec.sub(r.spec_off, NH + 2);
+    static_assert(TL::E == 16, "split twiddle powers for 16 slots");
+    const SplitTwiddles stw = split_twiddles(a.bank, a.logn + 1, mr.k2, t, logn2, TL::T);
 #pragma unroll
     for (int j = 0; j < TL::E; ++j) {
       const int k1 = t + TL::T * j;
       const int k1p = mirror_k1(mr.k2, k1, TL::M);
       cf32 e, od;
       real_split(v[j], zm[j], e, od);
-      const cf32 w = twiddle_n(a.bank, a.logn + 1, mr.k2 + (k1 << logn2));
+      const cf32 w = stw(j);  // w_N^{k2 + N2 k1}
       const cf32 wo = cmul(w, od);
       const cf32 xk = cadd(e, wo), xm = cconj(csub(e, wo));
       const cf32 hk = ldg(h, mr.k2 * TL::M + k1);
