@@ -511,8 +511,8 @@ struct ConvMidKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int EXCH = C * CS;
+  using XR = XposeRows<TL::T, C, TL::MP>;  // row-major passes, column-fastest stores
+  static constexpr int EXCH = XR::ELEMS;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
@@ -520,7 +520,7 @@ struct ConvMidKernel {
   // two DFTs, the spectrum multiply and the twiddle epilogue: allow 128 registers
   static constexpr int MINB = 1;
   struct Sidx {
-    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+    ESTL_HD int operator()(int c, int m) const { return XR::row(c) + TL::pad(m); }
   };
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
     const int t = tid & (TL::T - 1);
@@ -568,15 +568,15 @@ struct ConvOutKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int EXCH = C * CS;
+  using XR = XposeRows<TL::T, C, TL::MP>;  // row-major passes, column-fastest stores
+  static constexpr int EXCH = XR::ELEMS;
   static constexpr int TC_OFF = (EXCH + 1) & ~1;
   static constexpr int SMEM_ELEMS = TC ? TC_OFF + (int)((tc_area_words(NT / 32) + 1) / 2) : EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(!TC || NT % 32 == 0, "tensor-core tiles run whole warps");
   static constexpr int MINB = TC ? (NT <= 256 ? 2 : 1) : min_blocks(NT, TL::E);
   struct Sidx {
-    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+    ESTL_HD int operator()(int c, int m) const { return XR::row(c) + TL::pad(m); }
   };
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
     const int t = tid & (TL::T - 1);
@@ -730,14 +730,14 @@ struct ConvMidHalfKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int EXCH = C * CS;
+  using XR = XposeRows<TL::T, C, TL::MP>;  // row-major passes, column-fastest stores
+  static constexpr int EXCH = XR::ELEMS;
   static constexpr int SMEM_ELEMS = EXCH;
   static_assert(NT <= 1024, "too many threads");
   static_assert(C >= 2, "rows come in mirror pairs");
   static constexpr int MINB = 1;  // two DFTs, the spectrum algebra and the twiddle epilogue
   struct Sidx {
-    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+    ESTL_HD int operator()(int c, int m) const { return XR::row(c) + TL::pad(m); }
   };
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
     const int t = tid & (TL::T - 1);
@@ -811,13 +811,13 @@ struct ConvOutHalfKernel {
   using TL = Tile<LOGM, LOGE, LOGR>;
   static constexpr int C = 1 << LOGC;
   static constexpr int NT = TL::T * C;
-  static constexpr int CS = row_stride(TL::MP, C);
-  static constexpr int EXCH = C * CS;
+  using XR = XposeRows<TL::T, C, TL::MP>;  // row-major passes, column-fastest stores
+  static constexpr int EXCH = XR::ELEMS;
   static constexpr int SMEM_ELEMS = EXCH;
   static_assert(NT <= 1024, "too many threads");
   static constexpr int MINB = min_blocks(NT, TL::E);
   struct Sidx {
-    ESTL_HD int operator()(int c, int m) const { return c * CS + TL::pad(m); }
+    ESTL_HD int operator()(int c, int m) const { return XR::row(c) + TL::pad(m); }
   };
   ESTL_HD static void run(const ConvArgs& a, long long cta, int tid, cf32* smraw) {
     const int t = tid & (TL::T - 1);

@@ -417,6 +417,23 @@ struct Tile {
 // fastest, then 16/C positions per row) needs stride = 16/C (mod 16).
 ESTL_CX int row_stride(int mp, int c) { return c >= 16 ? (mp | 1) : ((mp + 15) / 16) * 16 + 16 / c; }
 
+// Rows of an exchange that is accessed both row-major (T threads a row, the
+// tile passes) and transposed (lanes over C rows at one position, the
+// column-fastest stores).  For T >= 16 or C < 16 this is row_stride(MP, C).
+// For T < 16 and C >= 16 a half-warp's row-major access spans 16/T rows: a
+// stride of T (mod 16) puts those rows on disjoint bank pairs, and each group
+// of 16/T rows is skewed by one more slot, so that 16 consecutive rows at one
+// position also fall on 16 distinct bank pairs (8-byte elements: bank pair =
+// index mod 16).  An odd stride alone doubles the row-major wavefronts there.
+template <int T, int C, int MP>
+struct XposeRows {
+  static constexpr bool SKEW = T < 16 && C >= 16;
+  static constexpr int LSK = T >= 16 ? 0 : T == 8 ? 1 : T == 4 ? 2 : T == 2 ? 3 : 4;  // log2(16 / T)
+  static constexpr int CS = SKEW ? MP + (((T - MP) % 16) + 16) % 16 : row_stride(MP, C);
+  static constexpr int ELEMS = C * CS + (SKEW ? (C >> LSK) : 0);
+  ESTL_HD static int row(int c) { return c * CS + (SKEW ? (c >> LSK) : 0); }
+};
+
 // Runs passes p..P-1 over the tile.  Between passes each thread writes its
 // outputs to shared memory at their Stockham positions and re-reads its next
 // inputs at t + T*j.  SIDX maps (column c, position m) to a shared index.
