@@ -89,6 +89,11 @@ bool build_packed_layout(const long long* offsets, const long long* sizes, long 
       if (err) *err = "convolution " + std::to_string(i) + ": lengths must be in [1, 2^22] and offsets >= 0";
       return false;
     }
+    const long long lim = 1LL << kMaxTotalLog;  // no sum of a length and an offset can overflow
+    if (q.sig_off > lim || q.filt_off > lim || q.out_off > lim) {
+      if (err) *err = "convolution " + std::to_string(i) + ": offsets must be at most 2^" + std::to_string(kMaxTotalLog);
+      return false;
+    }
     const int l = conv_logn(q.signal_len, q.filter_len);
     if (l > kConvMaxLogN) {
       if (err) *err = "convolution " + std::to_string(i) + ": padded length exceeds 2^" + std::to_string(kConvMaxLogN);

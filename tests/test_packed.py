@@ -410,7 +410,8 @@ def test_emulated_mixed_convolutions_only_and_magnitudes(emu):
 def test_emulated_mixed_validation(emu):
     offsets, sizes, x = make_batch(2, 4, 6, 1)
     empty = np.zeros(0, np.int64)
-    for bad in ([(0, 5, 0, 0, 0)], [(5, 5, -1, 0, 0)], [(1 << 22, 2, 0, 0, 0)]):
+    for bad in ([(0, 5, 0, 0, 0)], [(5, 5, -1, 0, 0)], [(1 << 22, 2, 0, 0, 0)], [(5, 5, 1 << 62, 0, 0)],
+                [(5, 5, 0, 0, (1 << 40) + 1)]):
         reqs = np.array(bad, np.int64)
         sig = np.zeros(8, np.float32)
         rc, msg, _, _ = emu_mixed(emu, offsets, sizes, x, 1, -1, reqs, sig, sig, 16, 0)
