@@ -57,6 +57,16 @@ def memory_usage():
     return used.value, budget.value
 
 
+def _check_host(a, dtype, numel, what, writable=False):
+    """A host buffer handed to the library by pointer: a C-contiguous numpy
+    array of `dtype` with at least `numel` elements."""
+    import numpy as np
+    if (not isinstance(a, np.ndarray) or a.dtype != np.dtype(dtype) or not a.flags.c_contiguous or a.size < numel
+            or (writable and not a.flags.writeable)):
+        raise EstlError(1, f"{what} must be a C-contiguous{' writable' if writable else ''} "
+                           f"{np.dtype(dtype).name} numpy array of >= {numel} elements")
+
+
 def _stream_handle(stream):
     if stream is None:
         import torch
@@ -122,6 +132,8 @@ class Plan:
             raise EstlError(1, f"input has {x.numel()} elements, plan expects {self.n * self.batch}")
         if out is None:
             out = torch.empty_like(x)
+        if out.dtype != torch.complex64 or not out.is_cuda or not out.is_contiguous() or out.numel() != x.numel():
+            raise EstlError(1, f"output must be a contiguous complex64 CUDA tensor of {x.numel()} elements")
         self.execute_ptr(x.data_ptr(), out.data_ptr(), _stream_handle(stream))
         return out
 
@@ -136,18 +148,27 @@ class Plan:
             raise EstlError(1, f"input must be a contiguous float32 CUDA tensor of >= {floats} floats")
         if out is None:
             out = torch.zeros(floats, dtype=torch.float32, device=x.device)
+        if out.dtype != torch.float32 or not out.is_cuda or not out.is_contiguous() or out.numel() < floats:
+            raise EstlError(1, f"output must be a contiguous float32 CUDA tensor of >= {floats} floats")
         check(lib().estl_execute_layout(self._h, int(layout), ctypes.c_void_p(x.data_ptr()),
                                         ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(_stream_handle(stream))))
         return out
 
     def execute_host_layout(self, x, out, layout):
         """Host float32 numpy arrays in `layout` (see execute_layout)."""
+        floats = int(lib().estl_layout_floats(int(layout), self.n * self.batch))
+        if floats < 0:
+            raise EstlError(1, f"unknown layout {layout}")
+        _check_host(x, "float32", floats, "input")
+        _check_host(out, "float32", floats, "output", writable=True)
         check(lib().estl_execute_host_layout(self._h, int(layout), ctypes.c_void_p(x.ctypes.data),
                                              ctypes.c_void_p(out.ctypes.data)))
         return out
 
     def execute_host(self, x, out):
         """Host numpy complex64 arrays (pinned memory recommended)."""
+        _check_host(x, "complex64", self.n * self.batch, "input")
+        _check_host(out, "complex64", self.n * self.batch, "output", writable=True)
         check(lib().estl_execute_host(self._h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(out.ctypes.data)))
         return out
 
@@ -293,15 +314,23 @@ class PackedPlan:
             check(lib().estl_packed_plan_create(self._offsets.ctypes.data, self._sizes.ctypes.data, self._sizes.size,
                                                 self.direction, self.MODES[mode], ctypes.byref(h)))
         self._h = h
+        # floats the signal, filter and output arrays must hold (0 without convolutions)
+        d = self.describe()
+        self.conv_extents = (d.get("conv_signal_floats", 0), d.get("conv_filter_floats", 0),
+                             d.get("conv_out_floats", 0))
 
     def execute_mixed(self, x, out, signals, filters, conv_out, stream=None):
         """A mixed batch: x / out as execute (None when there are no
         transforms); signals, filters, conv_out: contiguous float32 CUDA
-        tensors holding the convolutions' offsets."""
+        tensors holding the convolutions' offsets, of at least
+        conv_extents floats each."""
         import torch
-        for name, t in (("signals", signals), ("filters", filters), ("conv_out", conv_out)):
-            if t is not None and (t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous()):
-                raise EstlError(1, f"{name} must be a contiguous float32 CUDA tensor")
+        for name, t, need in zip(("signals", "filters", "conv_out"), (signals, filters, conv_out), self.conv_extents):
+            if need and t is None:
+                raise EstlError(1, f"{name} is required: the plan has convolutions")
+            if t is not None and (t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous()
+                                  or t.numel() < need):
+                raise EstlError(1, f"{name} must be a contiguous float32 CUDA tensor of >= {need} elements")
         for name, t in (("x", x), ("out", out)):
             if t is not None and (t.dtype != torch.complex64 or not t.is_cuda or not t.is_contiguous()
                                   or t.numel() < self.extent):

@@ -62,6 +62,8 @@ struct estl_packed_plan_s {
   ConvLayout conv_layout;
   void* conv_ws = nullptr;  // in ws
   long long conv_sig_elems = 0, conv_filt_elems = 0;
+  // floats each convolution array must hold: the largest offset + length over every request
+  long long need_sig = 0, need_filt = 0, need_out = 0;
   cudaStream_t conv_stream = nullptr;
   cudaEvent_t conv_fork = nullptr, conv_join = nullptr;
   // test hook (estl_packed_plan_set_test_hook)
@@ -204,6 +206,9 @@ static estl_status packed_create(const int64_t* offsets, const int64_t* sizes, i
     return fail(ESTL_INVALID_ARG, "%s", err.c_str());
   p->direction = direction;
   p->nconv = nconv;
+  p->need_sig = L.conv_sig_elems;
+  p->need_filt = L.conv_filt_elems;
+  p->need_out = L.conv_out_elems;
   // bucketed: every convolution runs the convolution engine's own launches
   if (mode == ESTL_PACKED_BUCKETED)
     p->conv_engine_reqs.assign(reqs, reqs + nconv);
@@ -496,12 +501,13 @@ estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len)
     }
     size_t ntf = 0;
     for (const PackedBucket& b : p->buckets) ntf += b.xoff.size();
-    char tail[384];
+    char tail[640];
     std::snprintf(tail, sizeof tail,
                   "], \"transforms\": %zu, \"launches\": %lld, \"elements\": %lld, \"flops\": %.6g, "
-                  "\"convolutions\": %lld, \"conv_items\": 0, \"conv_engine\": %zu, \"conv_launches\": %zu}",
+                  "\"convolutions\": %lld, \"conv_items\": 0, \"conv_engine\": %zu, \"conv_launches\": %zu, "
+                  "\"conv_signal_floats\": %lld, \"conv_filter_floats\": %lld, \"conv_out_floats\": %lld}",
                   ntf, launches + (long long)p->conv_layout.launches.size(), elems, flops, p->nconv,
-                  p->conv_engine_reqs.size(), p->conv_layout.launches.size());
+                  p->conv_engine_reqs.size(), p->conv_layout.launches.size(), p->need_sig, p->need_filt, p->need_out);
     d += tail;
     if (d.size() + 1 > len) return fail(ESTL_INVALID_ARG, "describe buffer of %zu bytes is too small", len);
     std::snprintf(buf, len, "%s", d.c_str());
@@ -512,10 +518,12 @@ estl_status estl_packed_plan_describe(estl_packed_plan p, char* buf, size_t len)
       buf, len,
       "{\"transforms\": %zu, \"items\": %zu, \"launches\": %zu, \"persistent\": %s, \"grid\": %d, "
       "\"elements\": %lld, \"flops\": %.6g, \"scratch_bytes\": %lld, \"smem_bytes\": %zu, \"convolutions\": %lld, "
-      "\"conv_items\": %zu, \"conv_engine\": %zu, \"conv_launches\": %zu, \"conv_flops\": %.6g}",
+      "\"conv_items\": %zu, \"conv_engine\": %zu, \"conv_launches\": %zu, \"conv_flops\": %.6g, "
+      "\"conv_signal_floats\": %lld, \"conv_filter_floats\": %lld, \"conv_out_floats\": %lld}",
       L.offsets.size(), L.items.size(), L.launch_begin.size() + p->conv_layout.launches.size(),
       L.persistent ? "true" : "false", L.persistent ? p->grid : 0, L.elements, L.flops, L.scratch_elems * 8, p->smem,
-      p->nconv, L.convs.size(), p->conv_engine_reqs.size(), p->conv_layout.launches.size(), L.conv_flops);
+      p->nconv, L.convs.size(), p->conv_engine_reqs.size(), p->conv_layout.launches.size(), L.conv_flops, p->need_sig,
+      p->need_filt, p->need_out);
   if (n < 0 || (size_t)n >= len) return fail(ESTL_INVALID_ARG, "describe buffer of %zu bytes is too small", len);
   return ESTL_OK;
 }

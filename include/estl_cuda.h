@@ -410,7 +410,10 @@ estl_status estl_packed_mixed_plan_create(const int64_t* offsets, const int64_t*
                                           estl_packed_plan* plan);
 /* d_in / d_out: the transforms' buffers (may be NULL when count is 0);
  * d_signals, d_filters, d_conv_out: the convolutions' float arrays (4-byte
- * aligned).  A plan with convolutions runs only through this call. */
+ * aligned), at least the conv_signal_floats / conv_filter_floats /
+ * conv_out_floats that estl_packed_plan_describe reports (the largest offset
+ * + length over the requests): the call cannot check the size behind a raw
+ * pointer.  A plan with convolutions runs only through this call. */
 estl_status estl_packed_mixed_execute(estl_packed_plan plan, const void* d_in, void* d_out, const float* d_signals,
                                       const float* d_filters, float* d_conv_out, void* stream);
 /* One blocking call for a batch used once: plan (persistent mode), execute on

@@ -82,3 +82,20 @@ def test_product_does_not_use_the_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h", ".inc")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert not re.search(r"\bimport oracle\b|from oracle\b|liboracle|oracle/", text), f
+
+
+def test_host_buffers_are_checked_before_the_call():
+    """Host arrays go to the library as raw pointers, so the binding refuses a
+    wrong dtype, a short, non-contiguous or read-only array first."""
+    import numpy as np
+    from estl_gb300 import EstlError, _check_host
+    ok = np.zeros(16, np.complex64)
+    _check_host(ok, "complex64", 16, "input")
+    _check_host(ok, "complex64", 8, "output", writable=True)
+    ro = ok.copy()
+    ro.flags.writeable = False
+    for bad, numel, writable in ((ok, 17, False), (ok.astype(np.complex128), 16, False), (ok[::2], 8, False),
+                                 (ro, 16, True), (list(ok), 16, False)):
+        with pytest.raises(EstlError):
+            _check_host(bad, "complex64", numel, "buffer", writable=writable)
+    _check_host(ro, "complex64", 16, "input")  # read-only is fine for an input

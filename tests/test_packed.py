@@ -475,11 +475,13 @@ def test_gpu_mixed_transforms_and_convolutions(engine, mode, flags):
 @pytest.mark.gpu
 def test_gpu_mixed_convolutions_only_and_errors(engine):
     """A plan of convolutions alone (no transform buffers), its describe, and
-    the refusals: a mixed plan through estl_packed_execute, NULL convolution
-    buffers, split precision."""
+    the refusals: a mixed plan through estl_packed_execute, NULL or short
+    convolution buffers (before any launch), split precision."""
     import torch
-    reqs, sig, filt, olen = make_convs(random_conv_shapes(50, 91), 92)
+    reqs, sig, filt, olen = make_convs(random_conv_shapes(50, 91, engine=[(20000, 300)]), 92)
     p = engine.PackedPlan([], [], -1, "persistent", convolutions=reqs)
+    # the last request ends one float before the end of each array
+    assert p.conv_extents == (sig.size - 1, filt.size - 1, olen - 1)
     sd, fd = torch.from_numpy(sig).cuda(), torch.from_numpy(filt).cuda()
     cd = torch.full((olen,), float("nan"), dtype=torch.float32, device="cuda")
     p.execute_mixed(None, None, sd, fd, cd)
@@ -489,6 +491,12 @@ def test_gpu_mixed_convolutions_only_and_errors(engine):
         p.execute(torch.zeros(4, dtype=torch.complex64, device="cuda"))
     with pytest.raises(engine.EstlError):
         p.execute_mixed(None, None, sd, fd, None)
+    for short in ((sd[:-2], fd, cd), (sd, fd[:-2], cd), (sd, fd, cd[:-2])):
+        with pytest.raises(engine.EstlError):
+            p.execute_mixed(None, None, *short)
     p.close()
+    b = engine.PackedPlan([], [], -1, "bucketed", convolutions=reqs)
+    assert b.conv_extents == (sig.size - 1, filt.size - 1, olen - 1)
+    b.close()
     with pytest.raises(engine.EstlError):
         engine.PackedPlan([], [], -1, "persistent", convolutions=reqs, conv_flags=1 << 8)
