@@ -25,7 +25,13 @@ class Server:
 
     def submit_conv(self, signal, filt, out, flags=0):
         """signal, filt, out: contiguous float32 numpy arrays; flags: CONV_* bits,
-        plus conv_precision(PREC_SPLIT_*) for the tensor-core FFT stages."""
+        plus conv_precision(PREC_SPLIT_*) for the tensor-core FFT stages; out
+        holds estl_conv_output_length floats."""
+        from . import _check_host
+        _check_host(signal, "float32", 0, "signal")  # lengths themselves are checked by the server
+        _check_host(filt, "float32", 0, "filter")
+        need = int(lib().estl_conv_output_length(signal.size, filt.size, int(flags)))
+        _check_host(out, "float32", need, "out", writable=True)
         r = ServeRequest(REQ_CONV, 0, int(flags), 0, 0, signal.size, filt.size, signal.ctypes.data, filt.ctypes.data,
                          out.ctypes.data)
         return self._submit(r, (signal, filt, out))
@@ -33,6 +39,9 @@ class Server:
     def submit_fft(self, x, out, direction=-1, precision=0):
         """x, out: contiguous complex64 numpy arrays of one power-of-two length;
         precision: PREC_FP32 or a PREC_SPLIT_* tensor-core form."""
+        from . import _check_host
+        _check_host(x, "complex64", 0, "x")
+        _check_host(out, "complex64", x.size, "out", writable=True)
         r = ServeRequest(REQ_FFT, int(direction), int(precision) << 8, 0, x.size, 0, 0, x.ctypes.data, None,
                          out.ctypes.data)
         return self._submit(r, (x, out))

@@ -157,3 +157,30 @@ def test_admission_budget(engine):
         srv.stop()
     for (s, f), out in zip(convs, outs):
         assert rel(out, oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))) < 1e-6
+
+
+def test_submit_checks_host_arrays(engine):
+    """The server copies results into the caller's host arrays by pointer, so
+    submit refuses a short output, a wrong dtype or a read-only output before
+    the request is queued; a well-formed request then runs as usual."""
+    from estl_gb300 import EstlError
+    from estl_gb300.serve import Server
+    srv = Server(max_inflight_batches=1)
+    try:
+        s = np.ones(100, np.float32)
+        f = np.ones(10, np.float32)
+        ro = np.zeros(109, np.float32)
+        ro.flags.writeable = False
+        for bad in ((s, f, np.zeros(108, np.float32)), (s.astype(np.float64), f, np.zeros(109, np.float32)),
+                    (s, f, ro)):
+            with pytest.raises(EstlError):
+                srv.submit_conv(*bad)
+        with pytest.raises(EstlError):
+            srv.submit_fft(np.zeros(64, np.complex64), np.zeros(63, np.complex64))
+        out = np.full(109, np.nan, np.float32)
+        res = srv.poll(srv.submit_conv(s, f, out))
+        assert res.status == 0
+        assert rel(out, oracle.conv_fft(s.astype(np.float64), f.astype(np.float64))) < 1e-6
+        assert srv.stats()["submitted"] == 1  # the refused ones never reached the queue
+    finally:
+        srv.stop()
