@@ -1,6 +1,6 @@
 """Oracle package — TEST INFRASTRUCTURE ONLY.
 
-The checker for the FFT engine, never the product: only ``tests/``,
+The reference results the FFT engine is tested against, never the product: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline`` leg and
 the ``--impl reference`` arm) may import it.
 
