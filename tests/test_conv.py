@@ -378,3 +378,58 @@ def test_emulated_compat_crop_wraps(emu, flags):
         for L, K, so, fo, o in creqs:
             ref = compat_reference(sig[so:so + L], filt[fo:fo + K], correlate=bool(flags & 1))
             assert rel(out[o:o + L], ref) < TOL, (L, K, flags, extra)
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_emulated_filter_longer_than_signal(emu, flags):
+    """Filters longer than their signals (K > L), from 1 sample against 5 taps
+    to 500 samples against 20000 taps (padded 2^15: the real-input
+    four-step): full convolution and correlation (L + K - 1 samples) and the
+    reference-compatible mode (L samples of the kernel-shifted circular
+    result), paired, unpaired and complex, against the oracle."""
+    shapes = [(1, 5), (3, 40), (100, 1000), (50, 3000), (700, 9000), (500, 20000)]
+    reqs, sig, filt, _ = make_requests(shapes, 101 + flags)
+    compat = bool(flags & 2)
+    if compat:
+        filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L if compat else L + K - 1
+    for extra in (0, NO_PAIRING, COMPLEX):
+        out = emu_conv(emu, creqs, sig, filt, oo, flags=flags | extra)
+        for L, K, so, fo, o in creqs:
+            s, f = sig[so:so + L], filt[fo:fo + K]
+            if compat:
+                ref, n = compat_reference(s, f, correlate=bool(flags & 1)), L
+            else:
+                ref = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1))
+                n = L + K - 1
+            assert rel(out[o:o + n], ref) < TOL, (L, K, flags, extra)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_gpu_filter_longer_than_signal(engine, flags):
+    """K > L on the GPU through estl_conv_execute, up to a 4000-sample signal
+    against a 200000-tap filter (padded 2^18), every mode and form, against
+    the oracle."""
+    shapes = [(1, 5), (3, 40), (100, 1000), (50, 3000), (700, 9000), (500, 20000), (4000, 200000)]
+    reqs, sig, filt, _ = make_requests(shapes, 111 + flags)
+    compat = bool(flags & 2)
+    if compat:
+        filt = np.abs(filt) + 0.1
+    creqs, oo = [], 0
+    for L, K, so, fo, _ in reqs:
+        creqs.append((L, K, so, fo, oo))
+        oo += L if compat else L + K - 1
+    for extra in (0, NO_PAIRING, COMPLEX):
+        out = gpu_conv_batch(engine, creqs, sig, filt, oo, flags=flags | extra)
+        for L, K, so, fo, o in creqs:
+            s, f = sig[so:so + L], filt[fo:fo + K]
+            if compat:
+                ref, n = compat_reference(s, f, correlate=bool(flags & 1)), L
+            else:
+                ref = oracle.conv_fft(s.astype(np.float64), f.astype(np.float64), correlate=bool(flags & 1))
+                n = L + K - 1
+            assert rel(out[o:o + n], ref) < TOL, (L, K, flags, extra)

@@ -159,7 +159,7 @@ def test_conv_compat_follows_the_reference_loops():
     samples of the inverse scaled by 1 / (width * K^[0]) (:141-148); the
     spectra are taken as direct DFTs."""
     rng = np.random.default_rng(5)
-    for L, K in [(4, 1), (5, 1), (7, 3), (8, 2), (13, 6), (16, 16)]:
+    for L, K in [(4, 1), (5, 1), (7, 3), (8, 2), (13, 6), (16, 16), (1, 4), (2, 5), (3, 11), (6, 30)]:
         s = rng.standard_normal(L)
         h = np.abs(rng.standard_normal(K)) + 0.1
         width = 1
