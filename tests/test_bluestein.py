@@ -64,11 +64,13 @@ def test_emulated_bluestein(emu, n):
         assert rel(y, direct(x, sign)).max() < TOL, (n, sign)
 
 
-@pytest.mark.parametrize("n", [9000, 40000])
+@pytest.mark.parametrize("n", [8191, 8193, 9000, 40000])
 def test_emulated_bluestein_four_step(emu, n):
-    """M = 2^15 and 2^17: the three four-step kernels with the chirps folded
-    into the first load and the last store (emulated, bounds-checked), against
-    the oracle's direct DFT on sampled bins."""
+    """Both sides of the fused / four-step boundary (8191: M = 2^14, the last
+    fused length; 8193: M = 2^15), and M = 2^15 and 2^17: the three four-step
+    kernels with the chirps folded into the first load and the last store
+    (emulated, bounds-checked), against the oracle's direct DFT on sampled
+    bins."""
     x = rand_c64((2, n), n)
     rng = np.random.default_rng(n)
     bins = np.concatenate([[0, 1, n // 2, n - 1], rng.integers(0, n, 28)])
@@ -90,8 +92,9 @@ def test_emulated_bluestein_rejects(emu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,batch", [(3, 7), (12, 5), (1000, 9), (4095, 3), (10000, 2), (123457, 2),
-                                     (1000000, 2), ((1 << 23) - 1, 1)])
+@pytest.mark.parametrize("n,batch", [(3, 7), (12, 5), (1000, 9), (4095, 3), (8191, 3), (8193, 3), (10000, 2),
+                                     (123457, 2), (1000000, 2), ((1 << 21) - 1, 1), ((1 << 21) + 1, 1),
+                                     ((1 << 23) - 1, 1)])
 def test_gpu_bluestein(engine, n, batch):
     import torch
     x = rand_c64((batch, n), n % 1000 + batch)
